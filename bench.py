@@ -1,0 +1,467 @@
+#!/usr/bin/env python
+"""Training-throughput benchmark of the SuperNormal hot path on GB300.
+
+Workload (the reference-equivalent GPU configuration): a displaced torus
+(R=0.5, r=0.2, amplitude 0.02, frequency 20) seen by 20 views of 612x512 on an
+elevated ring; hash grid 16 levels x 2 features, 2^19 entries per level, base
+resolution 16, scale 1.447; SDF MLP 35 -> 64 -> 16; 128^3 occupancy grid
+(threshold 0.1, updated every 8 iterations with the post-warm-up cell
+sampling); marching step 2/1024; 2048 patches of 3x3 per iteration; FP32;
+all 16 levels active (the most expensive bandwidth of the schedule).  Data
+are synthetic (no dataset is shipped).  A step is one full training
+iteration: marching, culling, patch expansion, field forward, render + loss +
+adjoint, field backward, learning-rate schedule and Adam, plus the amortised
+occupancy update.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs as independent replicas (one process per GPU via torchrun; the
+path has no exchange step), value = all ranks' rays / max rank time.
+--impl reference times the reference's CPU implementation of the path (the
+float64 restatement in oracle/, the reference having no CPU path of its own)
+on host cores over a bounded, proportional sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import torch  # noqa: E402
+
+METRIC = "train_rays_per_s"
+UNIT = "rays/s"
+ENC = dict(otype="HashGrid", n_levels=16, n_features_per_level=2, log2_hashmap_size=19,
+           base_resolution=16, per_level_scale=1.447)
+WORKLOAD = "patch-NeuS training iteration, displaced torus 20x612x512, hashgrid L16 F2 T2^19, 128^3 grid, dt=2/1024"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--batch", type=int, default=2048)
+    p.add_argument("--views", type=int, default=20)
+    p.add_argument("--height", type=int, default=512)
+    p.add_argument("--width", type=int, default=612)
+    p.add_argument("--pretrain", type=int, default=200, help="untimed iterations before warm-up")
+    p.add_argument("--cpu-sample-patches", type=int, default=8)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-clocks", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int, enabled: bool):
+        self.proc = None
+        self.gpu = gpu_index
+        if enabled:
+            try:
+                self.proc = subprocess.Popen(
+                    ["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
+                     "--format=csv,noheader,nounits", "-lms", "200"],
+                    stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            except OSError:
+                self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def build_workload(args, device, seed):
+    from supernormal_gb300 import scenes
+    from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
+    from supernormal_gb300.trainer import FusedTrainer, TrainConfig
+
+    torch.manual_seed(seed)
+    scene = scenes.displaced_torus(0.5, 0.2, 0.02, 20.0)
+    rig = scenes.ring_cameras(args.views, args.height, args.width, radius=3.0, elevation_deg=30.0,
+                              fov_deg=40.0)
+    net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=ENC,
+                     input_concat=True).to(device)
+    var = SingleVarianceNetwork(0.5).to(device)
+    cfg = TrainConfig(batch_size=args.batch, step_size=2.0 / 1024, occ_update_freq=8,
+                      occ_threshold=0.1, increase_bandwidth_every=0, end_iter=5000, seed=seed)
+    tr = FusedTrainer(net, var, cfg, device=device)
+    net.bindwidth = ENC["n_levels"]
+    return scene, rig, net, var, tr
+
+
+def run_ours(args, world, rank, local):
+    from supernormal_gb300 import scenes
+    from supernormal_gb300._lib import lib
+
+    dev = torch.device("cuda", local)
+    scene, rig, net, var, tr = build_workload(args, dev, seed=1234 + rank)
+    ds = scenes.SyntheticDataset(scene, rig, dev)
+    g = torch.Generator(device=dev).manual_seed(99 + rank)
+    pool = [ds.gen_random_patches(args.batch, generator=g) for _ in range(16)]
+    # warm state: occupancy warm-up from the initial field, a short pre-training
+    tr.occupancy_update(0)
+    for i in range(args.pretrain):
+        tr.train_step(*pool[i % len(pool)])
+    tr.iter_step = max(tr.iter_step, tr.cfg.occ_warmup_steps)   # post-warm-up occupancy regime
+    for i in range(args.warmup):
+        tr.train_step(*pool[i % len(pool)])
+    torch.cuda.synchronize()
+    tr.check_status()
+
+    # ---------------- device-resident timed region ----------------
+    K = args.steps
+    tr.profile = True
+    tr.marks.clear()
+    tr.q_hist.clear()
+    clocks = ClockSampler(local, not args.no_clocks and rank == 0)
+    launches0 = lib().sn_kernel_launches()
+    barrier(world)
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for i in range(K):
+        tr.train_step(*pool[i % len(pool)])
+    end.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    launches = lib().sn_kernel_launches() - launches0
+    clk = clocks.stop()
+    ms = start.elapsed_time(end)
+    tr.check_status()
+    stages = stage_times(tr.marks)
+    q = torch.cat(tr.q_hist).double().cpu().numpy() if tr.q_hist else None
+    tr.profile = False
+    ms_max = max_over_ranks(ms, world)
+    rays = args.batch * tr.P * K * world
+    value = rays / (ms_max / 1e3)
+
+    # ---------------- end-to-end through host buffers ----------------
+    host = [tuple(t.cpu().pin_memory() for t in b) for b in pool[:8]]
+    dev_in = tuple(torch.empty_like(t) for t in pool[0])
+    loss_host = torch.empty((5,), dtype=torch.float32).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in host[0])
+    d2h = loss_host.numel() * loss_host.element_size()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(K):
+        for dst, src in zip(dev_in, host[i % len(host)]):
+            dst.copy_(src, non_blocking=True)
+        loss = tr.train_step(*dev_in)
+        loss_host.copy_(loss, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), world)
+    e2e_value = rays / (e2e_ms / 1e3)
+
+    if rank != 0:
+        return None
+    peaks, peak_kind = load_peaks()
+    rl = roofline(stages, q, tr, peaks, peak_kind, K)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": ms_max / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "patches_per_step": args.batch, "patch": "3x3",
+                   "rays_per_step": args.batch * tr.P, "views": args.views,
+                   "resolution": [args.height, args.width], "hash_levels": 16, "log2_table": 19,
+                   "active_levels": net.active_levels(), "step_size": 2.0 / 1024,
+                   "occupancy_update_every": 8,
+                   "samples_per_ray": float(tr.S.item()) / args.batch,
+                   "l2": "step working set > L2: table + Adam state 4 x 64 MiB streamed every step",
+                   "parallelism": f"replicas{world}"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "roofline": rl,
+        "stages_ms_per_step": {k: v / K for k, v in stages.items()},
+    }
+    if clk:
+        out["clocks"] = clk
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args, tr, scene, rig, budget_s=20.0)
+    return out
+
+
+def stage_times(marks):
+    """Sum of event intervals per stage over all profiled steps (ms)."""
+    pairs = {"field_fwd": ("field_fwd_begin", "field_fwd_end"),
+             "field_bwd": ("field_bwd_begin", "field_bwd_end"),
+             "adam": ("adam_begin", "adam_end")}
+    tot = {k: 0.0 for k in pairs}
+    open_ev = {}
+    for tag, ev in marks:
+        for k, (b, e) in pairs.items():
+            if tag == b:
+                open_ev[k] = ev
+            elif tag == e and k in open_ev:
+                tot[k] += open_ev.pop(k).elapsed_time(ev)
+    return tot
+
+
+def roofline(stages, q, tr, peaks, peak_kind, K):
+    """Dominant kernel's achieved algorithmic bandwidth vs the measured HBM peak."""
+    L = tr.net.active_levels()
+    F = 2
+    bytes_per = {
+        # xyz + d sdf in, recomputed gather of 8 corners x F fp32 per level, float2 gradient scatter
+        "field_bwd": lambda: float(q.sum()) * (12 + 4 + 2 * L * 8 * F * 4),
+        # xyz in, gather, sdf out
+        "field_fwd": lambda: float(q.sum()) * (12 + L * 8 * F * 4 + 4),
+        # p, g, m, v read; p, m, v, g(=0) written
+        "adam": lambda: float(tr.n_params) * 32 * K,
+    }
+    top = max(stages, key=lambda k: stages[k])
+    achieved = bytes_per[top]() / (stages[top] / 1e3) / 1e9
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", f"{top}_dram_traffic.json")
+    if os.path.exists(tpath) and q is not None:
+        with open(tpath) as f:
+            t = json.load(f)
+        # captured bytes per field point (or per parameter), scaled to this run's launch
+        per_unit = t["dram_bytes_per_unit"]
+        units = float(q.mean()) if top != "adam" else float(tr.n_params)
+        traffic = per_unit * units
+    return {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+            "algorithmic_bytes_per_launch": bytes_per[top]() / K}
+
+
+# ---------------------------------------------------------------------------
+def cpu_step_factory(args, net_state, scene, rig, seed):
+    """One proportional sample of a training iteration on host cores (float64 oracle)."""
+    import numpy as np
+
+    from oracle import field as OF
+    from oracle import march as OM
+    from oracle import renderer as OR
+    from supernormal_gb300 import scenes
+
+    B_s = args.cpu_sample_patches
+    frac = B_s / args.batch
+    prm, geom, variance, binary, n_params = net_state
+    table = prm["table"]
+    g = torch.Generator().manual_seed(seed)
+    n_occ = max(1, int(round((128 ** 3 // 2) / 8 * frac)))      # amortised occupancy points
+    n_adam = max(4, int(round(n_params * frac)))
+    adam_p = torch.zeros(n_adam, dtype=torch.float64, requires_grad=True)
+    opt = torch.optim.Adam([adam_p], lr=5e-4)
+    roi = np.array([-1, -1, -1, 1, 1, 1], np.float32)
+    fld = lambda x: OF.sdf_network(x, **prm, geom=geom, active_levels=16, out_cols=1)
+
+    def step():
+        ro, rd, pn, vinv, nrm, mask = scenes.sample_patches(scene, rig, B_s, generator=g)
+        ro_c = ro[:, 1, 1].numpy()
+        rd_c = rd[:, 1, 1].numpy()
+        b = 2 * (ro_c * rd_c).sum(1)
+        c = (ro_c * ro_c).sum(1) - 1
+        a = (rd_c * rd_c).sum(1)
+        disc = np.sqrt(np.maximum(b * b - 4 * a * c, 0))
+        near = ((-b - disc) / (2 * a)).astype(np.float32)
+        far = ((-b + disc) / (2 * a)).astype(np.float32)
+        jit = torch.rand(B_s, generator=g).numpy().astype(np.float32)
+        packed, ri, ts, te = OM.ray_marching(ro_c, rd_c, near, far, roi, binary, 2.0 / 1024, jitter=jit)
+        if ri.size:
+            vis, _ = OR.cull(fld, packed, ri, ts, te, ro_c, rd_c, variance.detach())
+            ri, ts, te = ri[vis], ts[vis], te[vis]
+        if ri.size:
+            out = OR.patch_forward(fld, ri, ts, te, ro.numpy(), rd.numpy(), pn.numpy(), vinv.numpy(),
+                                   variance)
+            L = OR.losses(out["comp_normal"], out["weight_sum"], out["gradients"], nrm.numpy(),
+                          mask.numpy())
+            L["total"].backward()
+        with torch.no_grad():
+            x = torch.rand((n_occ, 3), generator=g, dtype=torch.float64) * 2 - 1
+            torch.sigmoid(-fld(x) * 80.0)
+        adam_p.grad = torch.randn(n_adam, generator=g, dtype=torch.float64)
+        opt.step()
+        for p in list(prm.values()) + [variance]:
+            p.grad = None
+        return B_s * 9
+
+    return step
+
+
+def cpu_state(tr):
+    from oracle import field as OF
+
+    prm = OF.params_from_module(tr.net)
+    geom = OF.geometry_from_module(tr.net)
+    variance = tr.dev_net.variance.detach().cpu().double().clone().requires_grad_(True)
+    binary = tr.grid.binary.cpu().numpy().astype("uint8")
+    return prm, geom, variance, binary, tr.n_params
+
+
+def cpu_baseline(args, tr, scene, rig, budget_s=20.0):
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    step = cpu_step_factory(args, cpu_state(tr), scene, rig, seed=7)
+    step()  # warm-up
+    rays, t0 = 0, time.perf_counter()
+    n = 0
+    while time.perf_counter() - t0 < budget_s and n < 50:
+        rays += step()
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": rays / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} iterations of {args.cpu_sample_patches} patches (1/{args.batch // args.cpu_sample_patches} "
+                      f"of a step: patches, amortised occupancy points and Adam elements scaled alike), "
+                      f"float64 oracle, {dt:.1f} s"}
+
+
+def run_reference(args, world, rank, local):
+    """CPU arm: the reference path's math (oracle port) on host cores."""
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    dev = torch.device("cuda", local) if torch.cuda.is_available() else torch.device("cpu")
+    from supernormal_gb300 import scenes
+    from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
+    from oracle import field as OF
+
+    torch.manual_seed(1234)
+    scene = scenes.displaced_torus(0.5, 0.2, 0.02, 20.0)
+    rig = scenes.ring_cameras(args.views, args.height, args.width, radius=3.0, elevation_deg=30.0,
+                              fov_deg=40.0)
+    net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=ENC, input_concat=True)
+    var = SingleVarianceNetwork(0.5)
+    prm = OF.params_from_module(net)
+    geom = OF.geometry_from_module(net)
+    variance = var.variance.detach().double().clone().requires_grad_(True)
+    # occupancy of the initial field (all cells) on host cores
+    import numpy as np
+
+    r = 128
+    c = (np.stack(np.meshgrid(*[np.arange(r)] * 3, indexing="ij"), -1).reshape(-1, 3) + 0.5) / r * 2 - 1
+    # the sphere-initialised SDF is |x| - 0.5 (+ small table terms): binarise its occupancy
+    occ = 1.0 / (1.0 + np.exp(np.clip((np.linalg.norm(c, axis=1) - 0.5) * 80.0, -50, 50)))
+    binary = (occ > min(occ.mean(), 0.1)).reshape(r, r, r).astype(np.uint8)
+    n_params = net.encoding.params.numel() + sum(p.numel() for n_, p in net.named_parameters()
+                                                 if not n_.startswith("encoding"))
+    step = cpu_step_factory(args, (prm, geom, variance, binary, n_params), scene, rig, seed=11)
+    for _ in range(max(args.warmup, 1)):
+        step()
+    rays, t0 = 0, time.perf_counter()
+    for _ in range(args.steps):
+        rays += step()
+    dt = time.perf_counter() - t0
+    value = rays / dt
+    sample = (f"{args.steps} iterations of {args.cpu_sample_patches} patches each (1/"
+              f"{args.batch // args.cpu_sample_patches} of a step, occupancy points and Adam elements "
+              f"scaled alike), float64 restatement of the reference math, {threads} threads")
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "patches_per_step": args.batch,
+                       "sampled_patches_per_step": args.cpu_sample_patches, "device": "host cores"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        out = run_reference(args, world, rank, local)
+    else:
+        out = run_ours(args, world, rank, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

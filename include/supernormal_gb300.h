@@ -1,0 +1,380 @@
+/*
+ * supernormal_gb300 — C ABI of the GB300 (sm_103a) kernels behind the
+ * SuperNormal training hot path: occupancy-grid ray marching, the
+ * multi-resolution hash-grid SDF field, NeuS SDF->alpha, patch-based
+ * render weights and ray accumulation.
+ *
+ * Conventions (every entry point):
+ *   - plain C types only: device pointers, element counts, scalars;
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy stream);
+ *   - outputs go to caller-allocated device buffers (nothing is allocated
+ *     inside the library except where an entry point says so);
+ *   - the return value is an SN_* status; on failure sn_last_error() holds
+ *     a message (thread-local).  Launches are asynchronous: device-side
+ *     conditions (iteration limits, capacity overflow) are reported through
+ *     the optional `status` device word an entry point takes.
+ *
+ * Reference paths below are relative to the SuperNormal repository;
+ * "NA/" abbreviates third_parties/nerfacc-0.3.5/nerfacc-0.3.5/.
+ */
+#ifndef SUPERNORMAL_GB300_H
+#define SUPERNORMAL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SN_OK 0
+#define SN_ERR_INVALID 1     /* bad argument (shape, size, null pointer)      */
+#define SN_ERR_CAPACITY 2    /* output capacity smaller than required         */
+#define SN_ERR_CUDA 3        /* CUDA launch / runtime error                   */
+#define SN_ERR_LIMIT 4       /* a device loop hit its iteration limit         */
+#define SN_ERR_UNSUPPORTED 5 /* configuration outside what the kernels cover  */
+
+/* device status word bits (OR-ed by kernels into an int32 device word) */
+#define SN_STATUS_MARCH_LIMIT 1   /* a ray exceeded the marching iteration cap */
+#define SN_STATUS_CAPACITY 2      /* a sample buffer overflowed its capacity   */
+
+/* contraction types; same values as nerfacc's ContractionType
+ * (NA/nerfacc/cuda/csrc/include/helpers_contraction.h:9-14) */
+#define SN_CONTRACTION_AABB 0
+#define SN_CONTRACTION_UN_BOUNDED_TANH 1
+#define SN_CONTRACTION_UN_BOUNDED_SPHERE 2
+
+/* ---- library ------------------------------------------------------------ */
+/* Version string of the library build. */
+const char* sn_version(void);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* sn_last_error(void);
+/* Number of kernels this library has launched in the process (all threads). */
+uint64_t sn_kernel_launches(void);
+
+/* ---- packing (NA/nerfacc/pack.py) ---------------------------------------- */
+/* Bytes of device workspace sn_pack_counts needs for n entries. */
+size_t sn_scan_workspace_bytes(int64_t n);
+/* packed_info[i] = {exclusive prefix sum of counts, counts[i]}; *total = sum.
+ * Replaces the cumsum/stack in NA/nerfacc/cuda/csrc/ray_marching.cu:257-258
+ * and NA/nerfacc/pack.py:73-75, without a host synchronisation. */
+int sn_pack_counts(int64_t n, const int32_t* counts, int32_t* packed_info,
+                   int32_t* total, void* workspace, void* stream);
+/* counts[r] = number of samples with ray_indices == r (counts zeroed here).
+ * Replaces the scatter_add_ in NA/nerfacc/pack.py:70-72. */
+int sn_count_indices(int64_t n_samples, const int64_t* ray_indices,
+                     int64_t n_rays, int32_t* counts, void* stream);
+/* ray_indices of each sample from packed_info.
+ * Replaces unpack_info_kernel (NA/nerfacc/cuda/csrc/pack.cu:7-27). */
+int sn_unpack_info(int64_t n_rays, const int32_t* packed_info,
+                   int64_t n_samples, int64_t* ray_indices, void* stream);
+
+/* ---- ray marching (NA/nerfacc/cuda/csrc/ray_marching.cu) ----------------- */
+/* Count pass of the marcher: num_steps[i] = samples on ray i.
+ * Replaces the first launch of ray_marching_kernel
+ * (NA/nerfacc/cuda/csrc/ray_marching.cu:81-192, host :194-255).
+ * jitter (nullable, n_rays) adds jitter[i]*step_size to t_min[i] exactly as
+ * NA/nerfacc/ray_marching.py:157-158 does; grid_binary is (rx,ry,rz) uint8
+ * (torch.bool) and roi is 6 floats on the device. status (nullable) gets
+ * SN_STATUS_MARCH_LIMIT if a ray exceeds max_iters loop iterations
+ * (max_iters <= 0 selects 1<<24). */
+int sn_march_count(int64_t n_rays, const float* rays_o, const float* rays_d,
+                   const float* t_min, const float* t_max, const float* jitter,
+                   const float* roi, const uint8_t* grid_binary, int rx, int ry,
+                   int rz, int contraction_type, float step_size,
+                   float cone_angle, int64_t max_iters, int32_t* num_steps,
+                   int32_t* status, void* stream);
+/* Fill pass: writes ray_indices / t_starts / t_ends at packed_info offsets.
+ * Replaces the second launch of ray_marching_kernel
+ * (NA/nerfacc/cuda/csrc/ray_marching.cu:263-286).  Samples beyond
+ * `capacity` are dropped and flag SN_STATUS_CAPACITY. */
+int sn_march_fill(int64_t n_rays, const float* rays_o, const float* rays_d,
+                  const float* t_min, const float* t_max, const float* jitter,
+                  const float* roi, const uint8_t* grid_binary, int rx, int ry,
+                  int rz, int contraction_type, float step_size,
+                  float cone_angle, int64_t max_iters,
+                  const int32_t* packed_info, int64_t capacity,
+                  int64_t* ray_indices, float* t_starts, float* t_ends,
+                  int32_t* status, void* stream);
+/* out[i] = grid_binary at samples[i] (0 outside the AABB roi).
+ * Replaces query_occ_kernel (NA/nerfacc/cuda/csrc/ray_marching.cu:295-358). */
+int sn_grid_query(int64_t n, const float* samples, const float* roi,
+                  const uint8_t* grid_binary, int rx, int ry, int rz,
+                  int contraction_type, uint8_t* out, void* stream);
+
+/* ---- occupancy grid (NA/nerfacc/grid.py:196-239) -------------------------- */
+/* World-space query points of grid cells:
+ * x = contract_inv((coords(cell) + jitter) / res) (NA/nerfacc/grid.py:210-225).
+ * cells (nullable => cell i for point i), jitter (n,3) in [0,1). */
+int sn_occ_points(int64_t n, const int64_t* cells, const float* jitter,
+                  int rx, int ry, int rz, const float* roi,
+                  int contraction_type, float* x_out, void* stream);
+/* occs[c] = max(occs[c]*ema_decay, occ[i]) for c = cells[i]
+ * (NA/nerfacc/grid.py:229-230); duplicate cells resolve to the max. */
+int sn_occ_ema_update(int64_t n, const int64_t* cells, const float* occ,
+                      float ema_decay, float* occs, void* stream);
+size_t sn_occ_binarize_workspace_bytes(int64_t n_cells);
+/* binary[c] = occs[c] > min(mean(occs), occ_thre) (NA/nerfacc/grid.py:235-237);
+ * mean_out (nullable, device) receives the mean. */
+int sn_occ_binarize(int64_t n_cells, const float* occs, float occ_thre,
+                    uint8_t* binary, float* mean_out, void* workspace,
+                    void* stream);
+/* Device-count forms used by the fused training step (no host sync):
+ * query points of cells[i] (nullable => cell i) for i < *count with jitter
+ * drawn in-kernel from (seed, *stream_counter). */
+int sn_occ_points_n(int64_t cap, const int32_t* count, const int64_t* cells,
+                    uint64_t seed, const int32_t* stream_counter, int rx,
+                    int ry, int rz, const float* roi, int contraction_type,
+                    float* x_out, void* stream);
+/* occs[c] = max(occs[c]*ema_decay, sigmoid(-sigmoid_k * sdf[i])): the
+ * renderer's occ_eval_fn (models/renderer.py:56-60) fused with the EMA. */
+int sn_occ_ema_sdf(int64_t cap, const int32_t* count, const int64_t* cells,
+                   const float* sdf, float sigmoid_k, float ema_decay,
+                   float* occs, void* stream);
+size_t sn_occ_sample_workspace_bytes(int64_t n_cells);
+/* Post-warm-up cell sampling (NA/nerfacc/grid.py:168-182): n_uniform
+ * uniform cells followed by min(n_occupied, n_uniform) occupied cells (all,
+ * or a uniform draw); *count = total (cells needs 2*n_uniform entries). */
+int sn_occ_sample_cells(int64_t n_cells, const uint8_t* binary,
+                        int64_t n_uniform, uint64_t seed,
+                        const int32_t* stream_counter, int64_t* cells,
+                        int32_t* count, void* workspace, void* stream);
+
+/* ---- volume rendering (NA/nerfacc/vol_rendering.py) ----------------------- */
+/* Exclusive transmittance T_i = prod_{j<i}(1 - alpha_j) per ray segment of
+ * packed_info, with patch_size pixel lanes per sample (1 = per-ray).
+ * Replaces transmittance_from_alpha_forward_cub / _naive
+ * (NA/nerfacc/cuda/csrc/render_transmittance_cub.cu:111-134). */
+int sn_transmittance_from_alpha(int64_t n_rays, int patch_size,
+                                const int32_t* packed_info,
+                                const float* alphas, float* transmittance,
+                                void* stream);
+/* visibility[s] = T_s >= early_stop_eps && (alpha_thre <= 0 || alpha_s >= alpha_thre)
+ * and vis_counts[r] (nullable) = visible samples of ray r.
+ * Replaces render_visibility (NA/nerfacc/vol_rendering.py:680-748). */
+int sn_visibility_from_alpha(int64_t n_rays, const int32_t* packed_info,
+                             const float* alphas, float early_stop_eps,
+                             float alpha_thre, uint8_t* visibility,
+                             int32_t* vis_counts, void* stream);
+/* Weights w = alpha * T per (ray, pixel lane); patch_size = 1 gives the
+ * per-ray variant.  Replaces weight_from_alpha_patch_based_forward_kernel
+ * (NA/nerfacc/cuda/csrc/render_weight.cu:87-118, host :502-543) and
+ * weight_from_alpha_forward_kernel (:154-183). */
+int sn_weight_from_alpha_fwd(int64_t n_rays, int patch_size,
+                             const int32_t* packed_info, const float* alphas,
+                             float* weights, void* stream);
+/* grad_alpha_j = (g_j T_j - sum_{i>=j} g_i w_i) / max(1 - alpha_j, 1e-10).
+ * Replaces weight_from_alpha_patch_based_backward_kernel
+ * (NA/nerfacc/cuda/csrc/render_weight.cu:298-340, host :583-626). */
+int sn_weight_from_alpha_bwd(int64_t n_rays, int patch_size,
+                             const int32_t* packed_info, const float* alphas,
+                             const float* weights, const float* grad_weights,
+                             float* grad_alphas, void* stream);
+/* out[ray_indices[s], k, :] += weights[s,k] * values[s,k,:] (values NULL =>
+ * dim 1, value 1).  out is zero-filled here.  Replaces the scatter_add_ of
+ * accumulate_along_rays(_patch_based) (NA/nerfacc/vol_rendering.py:132-335). */
+int sn_accumulate_fwd(int64_t n_samples, int patch_size, int dim,
+                      const int64_t* ray_indices, const float* weights,
+                      const float* values, int64_t n_rays, float* out,
+                      void* stream);
+/* Adjoint of sn_accumulate_fwd: grad_weights[s,k] = sum_d g[r,k,d] v[s,k,d],
+ * grad_values[s,k,d] = g[r,k,d] w[s,k] (either output nullable). */
+int sn_accumulate_bwd(int64_t n_samples, int patch_size, int dim,
+                      const int64_t* ray_indices, const float* weights,
+                      const float* values, const float* grad_out,
+                      float* grad_weights, float* grad_values, void* stream);
+
+/* ---- SDF field (models/fields.py SDFNetwork + tcnn HashGrid) --------------- */
+#define SN_MAX_LEVELS 32
+
+/* Hash-grid geometry in tiny-cuda-nn's layout (entry-major, n_features per
+ * entry, levels concatenated).  Filled by sn_grid_desc_init. */
+typedef struct sn_grid_desc {
+  int32_t n_levels;
+  int32_t n_features;
+  uint32_t offsets[SN_MAX_LEVELS + 1]; /* first entry of each level; [L] = total */
+  uint32_t resolutions[SN_MAX_LEVELS];
+  float scales[SN_MAX_LEVELS];
+} sn_grid_desc;
+
+/* One-hidden-layer MLP with effective (post weight-norm) weights, row-major
+ * like torch.nn.Linear.weight: w0 (d_hidden, d_in), w1 (d_out, d_hidden). */
+typedef struct sn_mlp_desc {
+  int32_t d_in;      /* 3 + n_levels * n_features (input_concat) */
+  int32_t d_hidden;  /* 64 */
+  int32_t d_out;     /* 1..16 */
+  float beta;        /* Softplus beta (100) */
+  float threshold;   /* Softplus threshold (20) */
+  const float* w0;
+  const float* b0;
+  const float* w1;
+  const float* b1;
+} sn_mlp_desc;
+
+/* Level offsets, resolutions and scales of tcnn's GridEncoding for
+ * {otype: HashGrid, n_levels, n_features_per_level, log2_hashmap_size,
+ *  base_resolution, per_level_scale} (models/fields.py:26, config/*.conf). */
+int sn_grid_desc_init(sn_grid_desc* desc, int n_levels, int n_features,
+                      int log2_hashmap_size, int base_resolution,
+                      float per_level_scale);
+/* Encoding forward: out (n, L*F); levels >= active_levels give zeros.
+ * Replaces tcnn.Encoding.forward (models/fields.py:78) plus the bandwidth
+ * mask (:81-83). */
+int sn_hashgrid_fwd(int64_t n, const float* x, const float* table,
+                    const sn_grid_desc* grid, int active_levels, float* out,
+                    void* stream);
+/* Encoding backward: grad_table += d out / d table ^T grad_out (atomics). */
+int sn_hashgrid_bwd(int64_t n, const float* x, const float* grad_out,
+                    const sn_grid_desc* grid, int active_levels,
+                    float* grad_table, void* stream);
+/* Fused field forward: out (n, out_cols) = first out_cols outputs of
+ * SDFNetwork.forward (models/fields.py:76-99).  count (nullable, device)
+ * bounds n at run time (n is then a capacity). */
+int sn_field_fwd(int64_t n, const int32_t* count, const float* x,
+                 const float* table, const sn_grid_desc* grid,
+                 int active_levels, const sn_mlp_desc* mlp, int out_cols,
+                 float* out, void* stream);
+/* Fused field backward with recomputation: accumulates (+=) the gradients of
+ * sum(grad_out * out) into grad_table / grad_w0 / grad_b0 / grad_w1 /
+ * grad_b1 and writes grad_x (each nullable).  Replaces the autograd backward
+ * through the torch MLP and tcnn's encoding backward. */
+int sn_field_bwd(int64_t n, const int32_t* count, const float* x,
+                 const float* grad_out, int out_cols, const float* table,
+                 const sn_grid_desc* grid, int active_levels,
+                 const sn_mlp_desc* mlp, float* grad_table, float* grad_w0,
+                 float* grad_b0, float* grad_w1, float* grad_b1,
+                 float* grad_x, void* stream);
+/* torch.nn.utils.weight_norm (dim=0): w = g * v / ||v||_row (models/fields.py:66-67). */
+int sn_weightnorm_fwd(int rows, int cols, const float* v, const float* g,
+                      float* w, float* norms, void* stream);
+int sn_weightnorm_bwd(int rows, int cols, const float* v, const float* g,
+                      const float* norms, const float* grad_w, float* grad_v,
+                      float* grad_g, void* stream);
+
+/* ---- renderer glue (models/renderer.py:63-276) ----------------------------- */
+/* diff[i] = t_ends[i] != t_starts[i+1] over the flattened samples (the last
+ * sample compares with its own start): models/renderer.py:88-93, :151-154.
+ * count (nullable, device) bounds cap at run time; diff[count..cap) = 0. */
+int sn_end_diff(int64_t cap, const int32_t* count, const float* t_starts,
+                const float* t_ends, int32_t* diff, void* stream);
+/* Query points of patch-centre samples for the culling alpha_fn
+ * (models/renderer.py:80-98): xyz[i] = o + d*t_start, and for diff samples
+ * xyz[n + slot] = o + d*t_end (end_packed = sn_pack_counts of diff).
+ * n_points (device) receives n + n_ends. */
+int sn_center_points(int64_t cap, const int32_t* count,
+                     const int64_t* ray_indices, const float* t_starts,
+                     const float* t_ends, const float* rays_o,
+                     const float* rays_d, const int32_t* end_packed,
+                     const int32_t* n_ends, float* xyz, int32_t* n_points,
+                     void* stream);
+/* NeuS alpha at centre samples from the field output (column 0 of a
+ * row-major (points, sdf_stride) array): models/renderer.py:100-117. */
+int sn_center_alpha(int64_t cap, const int32_t* count, const float* sdf,
+                    int sdf_stride, const int32_t* end_packed,
+                    const float* variance, float* alpha, void* stream);
+/* Order-preserving compaction of visible samples (the boolean indexing of
+ * NA/nerfacc/ray_marching.py:216-220); packed_out = sn_pack_counts of the
+ * per-ray visible counts. */
+int sn_compact_samples(int64_t n_rays, const int32_t* packed_in,
+                       const uint8_t* visibility, const int32_t* packed_out,
+                       const int64_t* ray_indices, const float* t_starts,
+                       const float* t_ends, int64_t* ray_indices_out,
+                       float* t_starts_out, float* t_ends_out, void* stream);
+/* Patch expansion through the marching plane (models/renderer.py:146-159):
+ * t_pix = t_c * (d_c . n) / (d_pix . n) for every pixel, start points at
+ * xyz[i*P + k] and end points of diff samples at xyz[(S + slot)*P + k].
+ * n_points (device) receives (S + n_ends) * P. */
+int sn_patch_points(int64_t cap, const int32_t* count, int patch_h,
+                    int patch_w, const int64_t* patch_indices,
+                    const float* t_starts, const float* t_ends,
+                    const float* rays_o, const float* rays_d,
+                    const float* plane_normal, const int32_t* end_packed,
+                    const int32_t* n_ends, float* xyz, float* t_pix_starts,
+                    float* t_pix_ends, int32_t* n_points, void* stream);
+/* Fused patch render forward: NeuS alpha (models/renderer.py:164-179),
+ * patch weights (:180), dfd gradients (:187-223) and accumulation of
+ * normals and mask (:263-267).  One warp per patch, one lane per pixel.
+ * alpha / weights / gradients (nullable) are per sample; comp_normal
+ * (n_patches, P, 3) and weight_sum (n_patches, P) per patch pixel. */
+int sn_patch_render_fwd(int64_t n_patches, int patch_h, int patch_w,
+                        const int32_t* packed_info, const int32_t* s_count,
+                        int64_t s_cap, const int32_t* end_packed,
+                        const float* sdf, const float* t_pix_starts,
+                        const float* t_pix_ends, const float* rays_o,
+                        const float* rays_d, const float* v_inverse,
+                        const float* variance, float* alpha, float* weights,
+                        float* gradients, float* comp_normal,
+                        float* weight_sum, void* stream);
+/* Adjoint of sn_patch_render_fwd: d_sdf (field-point layout; every live
+ * entry written) and per-patch partials[4p] = d loss / d inv_s.  carry
+ * (n_patches, P) receives the end adjoint a patch owes the next sample when
+ * that sample starts a later patch; sn_patch_carry_fixup adds it. */
+int sn_patch_render_bwd(int64_t n_patches, int patch_h, int patch_w,
+                        const int32_t* packed_info, const int32_t* s_count,
+                        int64_t s_cap, const int32_t* end_packed,
+                        const float* sdf, const float* t_pix_starts,
+                        const float* t_pix_ends, const float* rays_o,
+                        const float* rays_d, const float* v_inverse,
+                        const float* variance, const float* grad_comp_normal,
+                        const float* grad_weight_sum,
+                        const float* grad_gradients, float* d_sdf,
+                        float* partials, float* carry, void* stream);
+/* Training form: forward, the losses of exp_runner.py:191-203 (normal L2 or
+ * L1 over sum(mask), eikonal mean, mask BCE) and the adjoint in one pass.
+ * partials[4p..4p+3] = d/d inv_s, normal-loss sum, BCE sum, eikonal sum. */
+int sn_patch_render_train(int64_t n_patches, int patch_h, int patch_w,
+                          const int32_t* packed_info, const int32_t* s_count,
+                          int64_t s_cap, const int32_t* end_packed,
+                          const float* sdf, const float* t_pix_starts,
+                          const float* t_pix_ends, const float* rays_o,
+                          const float* rays_d, const float* v_inverse,
+                          const float* variance, const float* gt_normal,
+                          const float* gt_mask, const float* mask_sum,
+                          int loss_l1, float w_normal, float w_eikonal,
+                          float w_mask, float* d_sdf, float* partials,
+                          float* carry, void* stream);
+/* d_sdf[start after the last sample of patch p] += carry[p] where that
+ * sample's end was not evaluated separately (run after the render adjoint). */
+int sn_patch_carry_fixup(int64_t n_patches, int patch_size,
+                         const int32_t* packed_info, const int32_t* s_count,
+                         int64_t s_cap, const int32_t* end_packed,
+                         const float* carry, float* d_sdf, void* stream);
+/* Reduces per-patch partials: grad_variance (nullable) += d loss/d variance;
+ * out (nullable, 5 floats) = {d/d variance, normal, bce, eikonal, total}. */
+int sn_patch_finalize(int64_t n_patches, int patch_size, const float* partials,
+                      const int32_t* s_count, int64_t s_cap,
+                      const float* variance, const float* mask_sum,
+                      float w_normal, float w_eikonal, float w_mask,
+                      float* out, float* grad_variance, void* stream);
+/* near/far of the unit-sphere chord (models/dataset_loader.py:279-297) for
+ * rays read every `stride` floats (NaN when the ray misses: no samples),
+ * jitter (nullable) in [0,1) drawn from (seed, *stream_counter), and
+ * optional contiguous (n, 3) copies of the rays read. */
+int sn_near_far_sphere(int64_t n, const float* rays_o, const float* rays_d,
+                       int64_t stride, float* near, float* far, float* jitter,
+                       uint64_t seed, const int32_t* stream_counter,
+                       float* rays_o_out, float* rays_d_out, void* stream);
+/* mask_out = (mask_in > 0.5), *mask_sum = sum(mask_out) + 1e-5
+ * (exp_runner.py:169-175). */
+int sn_mask_prep(int64_t n, const float* mask_in, float* mask_out,
+                 float* mask_sum, void* stream);
+
+/* ---- optimiser (exp_runner.py:97, 205-210, 270-279) ------------------------ */
+/* Reads iteration k from *iter, writes lr(k) of the warm-up + cosine schedule
+ * and adam_step = k + 1, then stores k + 1 in *iter. */
+int sn_lr_schedule(int32_t* iter, float* lr, int32_t* adam_step, float base_lr,
+                   int warm_up_end, int end_iter, float alpha, void* stream);
+/* torch.optim.Adam step over a flat buffer (16-byte aligned).  lr_dev /
+ * step_dev (nullable) override lr / step; zero_grad clears grad after use;
+ * param_half (nullable) receives an fp16 copy of the updated parameters. */
+int sn_adam_step(int64_t n, float* param, float* grad, float* exp_avg,
+                 float* exp_avg_sq, void* param_half, const float* lr_dev,
+                 const int32_t* step_dev, float lr, int step, float beta1,
+                 float beta2, float eps, int zero_grad, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SUPERNORMAL_GB300_H */

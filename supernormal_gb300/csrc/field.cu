@@ -1,0 +1,656 @@
+// SDF field: multi-resolution hash-grid encoding + one-hidden-layer MLP.
+//
+// Encoding: Instant-NGP multiresolution hash encoding (Mueller et al. 2022)
+// with tiny-cuda-nn's conventions as used by SuperNormal's
+// `tcnn.Encoding(3, {otype: HashGrid, ...})` (models/fields.py:26,78):
+//   scale_l = 2^(l*log2(per_level_scale)) * base_resolution - 1
+//   resolution_l = ceil(scale_l) + 1
+//   pos = fma(scale_l, x, 0.5); cell = floor(pos); frac = pos - cell
+//   dense index (cell_x + cell_y*res + cell_z*res^2) when res^3 fits the
+//   level, else the XOR prime hash (1, 2654435761, 805459861); both taken
+//   modulo the level size in uint32 arithmetic (so SuperNormal's [-1,1]
+//   inputs wrap exactly as they do there), trilinear weights over the 8
+//   corners in corner order 0..7.
+// Table layout: entry-major, F features contiguous per entry, levels
+// concatenated at offsets[l] (the tcnn `params` layout).
+//
+// MLP: SDFNetwork with n_layers = 1 and input_concat
+// (models/fields.py:76-99): in = [x, enc], h = W0 in + b0,
+// a = softplus_beta(h), y = W1 a + b1, with W0/W1 the weight-normed
+// matrices.  Levels at or beyond `active_levels` are the encoding features
+// SuperNormal masks to zero (bandwidth, models/fields.py:81-83); their
+// gather and gradient are skipped, which is exact because the mask
+// multiplies them by zero.
+#include "common.cuh"
+
+#include <math.h>
+#include <string.h>
+
+namespace sn {
+
+constexpr int kH = 64;                    // hidden width (fixed, models/fields.py conf d_hidden)
+constexpr int kMaxL = 16;                 // levels handled by the fused kernels
+constexpr int kF = 2;                     // features per level (SuperNormal hard-codes 2)
+constexpr int kDinMax = 3 + kMaxL * kF;   // 35
+constexpr int kDinPad = 36;               // row stride of W0 in shared memory
+constexpr int kDoutMax = 16;
+
+struct GridDev {
+  int L;
+  uint32_t offset[kMaxL];
+  uint32_t res[kMaxL];
+  uint32_t size[kMaxL];     // entries in the level (tcnn hashmap_size)
+  uint32_t magic[kMaxL];    // Granlund-Montgomery reciprocal of size
+  uint8_t sh1[kMaxL], sh2[kMaxL];
+  uint8_t dense[kMaxL];
+  float scale[kMaxL];
+};
+
+// n mod d for uint32 n and invariant d (Granlund & Montgomery 1994, fig. 4.1).
+__device__ __forceinline__ uint32_t fast_mod(uint32_t n, uint32_t d, uint32_t m, int s1, int s2) {
+  const uint32_t t = __umulhi(m, n);
+  const uint32_t q = (t + ((n - t) >> s1)) >> s2;
+  return n - q * d;
+}
+
+struct LevelCorners {
+  uint32_t idx[8];
+  float w[8];
+  float frac[3];
+};
+
+__device__ __forceinline__ void level_corners(const GridDev& g, int l, const float x[3],
+                                              LevelCorners& c) {
+  const float s = g.scale[l];
+  uint32_t cell[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float p = __fmaf_rn(s, x[d], 0.5f);
+    const float f = floorf(p);
+    cell[d] = (uint32_t)(int)f;
+    c.frac[d] = __fsub_rn(p, f);
+  }
+  const uint32_t res = g.res[l];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    float w = 1.0f;
+    uint32_t q[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const bool hi = (k >> d) & 1;
+      w = __fmul_rn(w, hi ? c.frac[d] : __fsub_rn(1.0f, c.frac[d]));
+      q[d] = cell[d] + (hi ? 1u : 0u);
+    }
+    uint32_t index;
+    if (g.dense[l])
+      index = q[0] + q[1] * res + q[2] * (res * res);
+    else
+      index = q[0] ^ (q[1] * 2654435761u) ^ (q[2] * 805459861u);
+    c.idx[k] = g.offset[l] + fast_mod(index, g.size[l], g.magic[l], g.sh1[l], g.sh2[l]);
+    c.w[k] = w;
+  }
+}
+
+// d w_k / d x_d for linear interpolation (scale * +-1 * product of the other two factors).
+__device__ __forceinline__ float corner_dw(const LevelCorners& c, int k, int d, float s) {
+  float w = 1.0f;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    if (e == d) continue;
+    const bool hi = (k >> e) & 1;
+    w *= hi ? c.frac[e] : 1.0f - c.frac[e];
+  }
+  return ((k >> d) & 1) ? s * w : -s * w;
+}
+
+__device__ __forceinline__ void encode_level(const float* __restrict__ table, const GridDev& g,
+                                             int l, const float x[3], float& e0, float& e1) {
+  LevelCorners c;
+  level_corners(g, l, x, c);
+  const float2* t2 = reinterpret_cast<const float2*>(table);
+  float2 v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = __ldg(t2 + c.idx[k]);
+  float a = 0.0f, b = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    a = __fmaf_rn(c.w[k], v[k].x, a);
+    b = __fmaf_rn(c.w[k], v[k].y, b);
+  }
+  e0 = a;
+  e1 = b;
+}
+
+struct FieldArgs {
+  int64_t cap;
+  const int32_t* count;   // optional device count (n = min(*count, cap))
+  const float* x;
+  const float* table;
+  GridDev g;
+  int active;             // active levels
+  int din;                // 3 + L*F
+  int dout;               // rows of W1
+  int out_cols;           // outputs computed / gradients read (<= dout)
+  float beta, thresh;
+  const float* w0;        // (64, din)
+  const float* b0;        // (64)
+  const float* w1;        // (dout, 64)
+  const float* b1;        // (dout)
+  float* out;             // (n, out_cols)
+  const float* grad_out;  // (n, out_cols)
+  float* grad_table;
+  float* grad_w0;
+  float* grad_b0;
+  float* grad_w1;
+  float* grad_b1;
+  float* grad_x;          // (n, 3) optional
+};
+
+__device__ __forceinline__ int64_t effective_n(const FieldArgs& a) {
+  if (!a.count) return a.cap;
+  const int64_t c = *a.count;
+  return c < a.cap ? c : a.cap;
+}
+
+// Load W0 (row stride kDinPad, zero padded), b0, W1 rows < out_cols, b1.
+__device__ void load_mlp(const FieldArgs& a, float* s_w0, float* s_b0, float* s_w1, float* s_b1) {
+  for (int t = threadIdx.x; t < kH * kDinPad; t += blockDim.x) {
+    const int j = t / kDinPad, i = t - j * kDinPad;
+    s_w0[t] = i < a.din ? a.w0[j * a.din + i] : 0.0f;
+  }
+  for (int t = threadIdx.x; t < kH; t += blockDim.x) s_b0[t] = a.b0[t];
+  for (int t = threadIdx.x; t < kDoutMax * kH; t += blockDim.x) {
+    const int o = t / kH;
+    s_w1[t] = o < a.out_cols ? a.w1[t] : 0.0f;
+  }
+  for (int t = threadIdx.x; t < kDoutMax; t += blockDim.x) s_b1[t] = t < a.out_cols ? a.b1[t] : 0.0f;
+}
+
+constexpr int kSmemMlpFloats = kH * kDinPad + kH + kDoutMax * kH + kDoutMax;
+
+__device__ __forceinline__ void build_input(const FieldArgs& a, int64_t p, float in[kDinPad]) {
+  const float x[3] = {a.x[3 * p], a.x[3 * p + 1], a.x[3 * p + 2]};
+  in[0] = x[0];
+  in[1] = x[1];
+  in[2] = x[2];
+#pragma unroll
+  for (int l = 0; l < kMaxL; ++l) {
+    float e0 = 0.0f, e1 = 0.0f;
+    if (l < a.active) encode_level(a.table, a.g, l, x, e0, e1);
+    in[3 + 2 * l] = e0;
+    in[4 + 2 * l] = e1;
+  }
+  in[kDinPad - 1] = 0.0f;
+}
+
+__device__ __forceinline__ float hidden_pre(const float* s_w0, const float* s_b0, int j,
+                                            const float in[kDinPad], int n_in4) {
+  const float4* wr = reinterpret_cast<const float4*>(s_w0 + j * kDinPad);
+  float h = s_b0[j];
+#pragma unroll
+  for (int q = 0; q < kDinPad / 4; ++q) {
+    if (q < n_in4) {
+      const float4 w = wr[q];
+      h = fmaf(w.x, in[4 * q], h);
+      h = fmaf(w.y, in[4 * q + 1], h);
+      h = fmaf(w.z, in[4 * q + 2], h);
+      h = fmaf(w.w, in[4 * q + 3], h);
+    }
+  }
+  return h;
+}
+
+__global__ void __launch_bounds__(128) field_fwd_kernel(FieldArgs a) {
+  extern __shared__ float4 smem4[];
+  float* s_w0 = reinterpret_cast<float*>(smem4);
+  float* s_b0 = s_w0 + kH * kDinPad;
+  float* s_w1 = s_b0 + kH;
+  float* s_b1 = s_w1 + kDoutMax * kH;
+  load_mlp(a, s_w0, s_b0, s_w1, s_b1);
+  __syncthreads();
+  const int64_t n = effective_n(a);
+  const int n_in4 = (3 + 2 * a.active + 3) / 4;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    float in[kDinPad];
+    build_input(a, p, in);
+    float out[kDoutMax];
+#pragma unroll
+    for (int o = 0; o < kDoutMax; ++o) out[o] = s_b1[o];
+#pragma unroll 4
+    for (int j = 0; j < kH; ++j) {
+      const float h = hidden_pre(s_w0, s_b0, j, in, n_in4);
+      const float act = softplus_fwd(h, a.beta, a.thresh);
+#pragma unroll
+      for (int o = 0; o < kDoutMax; ++o)
+        if (o < a.out_cols) out[o] = fmaf(s_w1[o * kH + j], act, out[o]);
+    }
+#pragma unroll
+    for (int o = 0; o < kDoutMax; ++o)
+      if (o < a.out_cols) a.out[p * a.out_cols + o] = out[o];
+  }
+}
+
+// Backward with recomputation: per 128-point batch, each thread rebuilds its
+// point's encoding and hidden layer, forms dL/dh and dL/denc, scatters the
+// table gradient with float2 atomics, and stages (in, dh, act, g) in shared
+// memory; the block then reduces the weight gradients over the batch with
+// thread-owned accumulators, flushed to global memory once per block.
+constexpr int kBwdThreads = 128;
+
+__global__ void __launch_bounds__(kBwdThreads) field_bwd_kernel(FieldArgs a) {
+  extern __shared__ float4 smem4[];
+  float* s_w0 = reinterpret_cast<float*>(smem4);
+  float* s_b0 = s_w0 + kH * kDinPad;
+  float* s_w1 = s_b0 + kH;
+  float* s_b1 = s_w1 + kDoutMax * kH;
+  float* s_in = s_b1 + kDoutMax;                  // [128][kDinPad]
+  float* s_dh = s_in + kBwdThreads * kDinPad;     // [128][64]
+  float* s_act = s_dh + kBwdThreads * kH;         // [128][64]
+  float* s_g = s_act + kBwdThreads * kH;          // [128][kDoutMax]
+  load_mlp(a, s_w0, s_b0, s_w1, s_b1);
+  __syncthreads();
+
+  const int64_t n = effective_n(a);
+  const int n_in4 = (3 + 2 * a.active + 3) / 4;
+  const int din_used = 3 + 2 * a.active;
+  const int t = threadIdx.x;
+  const int own_j = t >> 1, half = t & 1;
+
+  // thread-owned weight-gradient accumulators
+  float acc_w0[(kDinPad + 1) / 2];
+  float acc_w1[kDoutMax / 2];
+  float acc_b0 = 0.0f, acc_b1 = 0.0f;
+#pragma unroll
+  for (int q = 0; q < (kDinPad + 1) / 2; ++q) acc_w0[q] = 0.0f;
+#pragma unroll
+  for (int q = 0; q < kDoutMax / 2; ++q) acc_w1[q] = 0.0f;
+
+  const int64_t stride = (int64_t)gridDim.x * kBwdThreads;
+  for (int64_t b0 = (int64_t)blockIdx.x * kBwdThreads; b0 < n; b0 += stride) {
+    const int64_t p = b0 + t;
+    const bool live = p < n;
+    // ---- phase 1: recompute forward, dL/dh, dL/denc ----
+    float in[kDinPad];
+    float g[kDoutMax];
+    if (live) {
+      build_input(a, p, in);
+#pragma unroll
+      for (int o = 0; o < kDoutMax; ++o) g[o] = o < a.out_cols ? a.grad_out[p * a.out_cols + o] : 0.0f;
+    } else {
+#pragma unroll
+      for (int i = 0; i < kDinPad; ++i) in[i] = 0.0f;
+#pragma unroll
+      for (int o = 0; o < kDoutMax; ++o) g[o] = 0.0f;
+    }
+    float denc[2 * kMaxL + 3];  // [0..2] = dL/dx from the linear part
+#pragma unroll
+    for (int i = 0; i < 2 * kMaxL + 3; ++i) denc[i] = 0.0f;
+#pragma unroll 2
+    for (int j = 0; j < kH; ++j) {
+      const float h = hidden_pre(s_w0, s_b0, j, in, n_in4);
+      const float act = softplus_fwd(h, a.beta, a.thresh);
+      const float sg = softplus_grad(h, a.beta, a.thresh);
+      float da = 0.0f;
+#pragma unroll
+      for (int o = 0; o < kDoutMax; ++o) da = fmaf(g[o], s_w1[o * kH + j], da);
+      const float dh = da * sg;
+      s_dh[t * kH + j] = dh;
+      s_act[t * kH + j] = act;
+      const float4* wr = reinterpret_cast<const float4*>(s_w0 + j * kDinPad);
+#pragma unroll
+      for (int q = 0; q < kDinPad / 4; ++q) {
+        if (q < n_in4) {
+          const float4 w = wr[q];
+          if (4 * q + 0 < 2 * kMaxL + 3) denc[4 * q + 0] = fmaf(w.x, dh, denc[4 * q + 0]);
+          if (4 * q + 1 < 2 * kMaxL + 3) denc[4 * q + 1] = fmaf(w.y, dh, denc[4 * q + 1]);
+          if (4 * q + 2 < 2 * kMaxL + 3) denc[4 * q + 2] = fmaf(w.z, dh, denc[4 * q + 2]);
+          if (4 * q + 3 < 2 * kMaxL + 3) denc[4 * q + 3] = fmaf(w.w, dh, denc[4 * q + 3]);
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < kDinPad; ++i) s_in[t * kDinPad + i] = in[i];
+#pragma unroll
+    for (int o = 0; o < kDoutMax; ++o) s_g[t * kDoutMax + o] = g[o];
+
+    // ---- phase 2: table gradient scatter (and optional dL/dx) ----
+    if (live && (a.grad_table || a.grad_x)) {
+      const float x[3] = {in[0], in[1], in[2]};
+      float dx[3] = {denc[0], denc[1], denc[2]};
+      float2* gt2 = reinterpret_cast<float2*>(a.grad_table);
+#pragma unroll
+      for (int l = 0; l < kMaxL; ++l) {
+        if (l < a.active) {
+          LevelCorners c;
+          level_corners(a.g, l, x, c);
+          const float d0 = denc[3 + 2 * l], d1 = denc[4 + 2 * l];
+          if (a.grad_table) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+              atomicAdd(gt2 + c.idx[k], make_float2(c.w[k] * d0, c.w[k] * d1));
+          }
+          if (a.grad_x) {
+            const float2* t2 = reinterpret_cast<const float2*>(a.table);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              const float2 v = __ldg(t2 + c.idx[k]);
+              const float gv = d0 * v.x + d1 * v.y;
+#pragma unroll
+              for (int d = 0; d < 3; ++d) dx[d] = fmaf(gv, corner_dw(c, k, d, a.g.scale[l]), dx[d]);
+            }
+          }
+        }
+      }
+      if (a.grad_x) {
+        a.grad_x[3 * p] = dx[0];
+        a.grad_x[3 * p + 1] = dx[1];
+        a.grad_x[3 * p + 2] = dx[2];
+      }
+    }
+    __syncthreads();
+
+    // ---- phase 3: weight gradients over the batch ----
+    const int batch = (int)((n - b0) < kBwdThreads ? (n - b0) : kBwdThreads);
+    for (int q = 0; q < batch; ++q) {
+      const float dh = s_dh[q * kH + own_j];
+      const float act = s_act[q * kH + own_j];
+      const float* iq = s_in + q * kDinPad;
+      const float* gq = s_g + q * kDoutMax;
+#pragma unroll
+      for (int c = 0; c < (kDinPad + 1) / 2; ++c) {
+        const int i = half + 2 * c;
+        if (i < din_used) acc_w0[c] = fmaf(dh, iq[i], acc_w0[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < kDoutMax / 2; ++c) {
+        const int o = half + 2 * c;
+        if (o < a.out_cols) acc_w1[c] = fmaf(gq[o], act, acc_w1[c]);
+      }
+      if (half == 0) acc_b0 += dh;
+      if (t < a.out_cols) acc_b1 += gq[t];
+    }
+    __syncthreads();
+  }
+
+  // ---- flush ----
+  if (a.grad_w0) {
+#pragma unroll
+    for (int c = 0; c < (kDinPad + 1) / 2; ++c) {
+      const int i = half + 2 * c;
+      if (i < din_used && acc_w0[c] != 0.0f) atomicAdd(a.grad_w0 + own_j * a.din + i, acc_w0[c]);
+    }
+  }
+  if (a.grad_b0 && half == 0 && acc_b0 != 0.0f) atomicAdd(a.grad_b0 + own_j, acc_b0);
+  if (a.grad_w1) {
+#pragma unroll
+    for (int c = 0; c < kDoutMax / 2; ++c) {
+      const int o = half + 2 * c;
+      if (o < a.out_cols && acc_w1[c] != 0.0f) atomicAdd(a.grad_w1 + o * kH + own_j, acc_w1[c]);
+    }
+  }
+  if (a.grad_b1 && t < a.out_cols && acc_b1 != 0.0f) atomicAdd(a.grad_b1 + t, acc_b1);
+}
+
+constexpr size_t kFwdSmem = kSmemMlpFloats * sizeof(float);
+constexpr size_t kBwdSmem =
+    (kSmemMlpFloats + kBwdThreads * (kDinPad + 2 * kH + kDoutMax)) * sizeof(float);
+
+// --- standalone encoding (tcnn.Encoding forward / backward) -----------------
+__global__ void hashgrid_fwd_kernel(int64_t n, const float* __restrict__ x,
+                                    const float* __restrict__ table, GridDev g, int active,
+                                    float* __restrict__ out) {
+  const int64_t total = n * g.L;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = t / g.L;
+    const int l = (int)(t - p * g.L);
+    float e0 = 0.0f, e1 = 0.0f;
+    if (l < active) {
+      const float xp[3] = {x[3 * p], x[3 * p + 1], x[3 * p + 2]};
+      encode_level(table, g, l, xp, e0, e1);
+    }
+    reinterpret_cast<float2*>(out)[t] = make_float2(e0, e1);
+  }
+}
+
+__global__ void hashgrid_bwd_kernel(int64_t n, const float* __restrict__ x,
+                                    const float* __restrict__ gout, GridDev g, int active,
+                                    float* __restrict__ gtable) {
+  const int64_t total = n * g.L;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = t / g.L;
+    const int l = (int)(t - p * g.L);
+    if (l >= active) continue;
+    const float xp[3] = {x[3 * p], x[3 * p + 1], x[3 * p + 2]};
+    const float2 go = reinterpret_cast<const float2*>(gout)[t];
+    LevelCorners c;
+    level_corners(g, l, xp, c);
+    float2* gt2 = reinterpret_cast<float2*>(gtable);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) atomicAdd(gt2 + c.idx[k], make_float2(c.w[k] * go.x, c.w[k] * go.y));
+  }
+}
+
+// --- weight normalisation (torch.nn.utils.weight_norm, dim=0) ----------------
+__global__ void weightnorm_fwd_kernel(int rows, int cols, const float* __restrict__ v,
+                                      const float* __restrict__ gain, float* __restrict__ w,
+                                      float* __restrict__ norms) {
+  const int r = blockIdx.x;
+  if (r >= rows) return;
+  float s = 0.0f;
+  for (int c = threadIdx.x; c < cols; c += 32) s = fmaf(v[r * cols + c], v[r * cols + c], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  const float nrm = sqrtf(s);
+  const float k = gain[r] / nrm;
+  for (int c = threadIdx.x; c < cols; c += 32) w[r * cols + c] = v[r * cols + c] * k;
+  if (threadIdx.x == 0 && norms) norms[r] = nrm;
+}
+
+__global__ void weightnorm_bwd_kernel(int rows, int cols, const float* __restrict__ v,
+                                      const float* __restrict__ gain,
+                                      const float* __restrict__ norms,
+                                      const float* __restrict__ gw, float* __restrict__ gv,
+                                      float* __restrict__ gg) {
+  const int r = blockIdx.x;
+  if (r >= rows) return;
+  float s = 0.0f;
+  for (int c = threadIdx.x; c < cols; c += 32) s = fmaf(gw[r * cols + c], v[r * cols + c], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  const float nrm = norms[r];
+  const float dg = s / nrm;
+  const float k = gain[r] / nrm;
+  const float m = dg / nrm;
+  for (int c = threadIdx.x; c < cols; c += 32)
+    gv[r * cols + c] = k * (gw[r * cols + c] - v[r * cols + c] * m);
+  if (threadIdx.x == 0) gg[r] = dg;
+}
+
+int make_grid_dev(const sn_grid_desc* d, GridDev& g) {
+  SN_REQUIRE(d != nullptr, "grid descriptor is null");
+  SN_REQUIRE(d->n_features == kF, "only %d features per level are supported (got %d)", kF,
+             d->n_features);
+  if (d->n_levels < 1 || d->n_levels > kMaxL) {
+    set_error("1..%d levels supported (got %d)", kMaxL, d->n_levels);
+    return SN_ERR_UNSUPPORTED;
+  }
+  memset(&g, 0, sizeof(g));
+  g.L = d->n_levels;
+  for (int l = 0; l < g.L; ++l) {
+    const uint32_t size = d->offsets[l + 1] - d->offsets[l];
+    SN_REQUIRE(size > 0, "empty level %d", l);
+    g.offset[l] = d->offsets[l];
+    g.res[l] = d->resolutions[l];
+    g.size[l] = size;
+    g.scale[l] = d->scales[l];
+    const uint64_t r = d->resolutions[l];
+    g.dense[l] = (r * r * r <= (uint64_t)size) ? 1 : 0;
+    int lg = 0;
+    while (((uint64_t)1 << lg) < size) ++lg;
+    const uint64_t m = (((uint64_t)1 << 32) * (((uint64_t)1 << lg) - size)) / size + 1;
+    g.magic[l] = (uint32_t)m;
+    g.sh1[l] = lg < 1 ? lg : 1;
+    g.sh2[l] = lg > 1 ? lg - 1 : 0;
+  }
+  return SN_OK;
+}
+
+static int fill_field_args(FieldArgs& a, int64_t n, const int32_t* count, const float* x,
+                           const float* table, const sn_grid_desc* grid, int active_levels,
+                           const sn_mlp_desc* mlp, int out_cols) {
+  memset(&a, 0, sizeof(a));
+  SN_REQUIRE(n >= 0, "field: n < 0");
+  SN_REQUIRE(mlp != nullptr, "field: mlp descriptor is null");
+  SN_TRY(make_grid_dev(grid, a.g));
+  if (mlp->d_hidden != kH) {
+    set_error("field: hidden width %d unsupported (kernels are built for %d)", mlp->d_hidden, kH);
+    return SN_ERR_UNSUPPORTED;
+  }
+  SN_REQUIRE(mlp->d_in == 3 + grid->n_levels * grid->n_features,
+             "field: d_in %d != 3 + levels*features", mlp->d_in);
+  if (mlp->d_out < 1 || mlp->d_out > kDoutMax) {
+    set_error("field: d_out %d outside 1..%d", mlp->d_out, kDoutMax);
+    return SN_ERR_UNSUPPORTED;
+  }
+  SN_REQUIRE(out_cols >= 1 && out_cols <= mlp->d_out, "field: out_cols %d outside 1..d_out", out_cols);
+  SN_REQUIRE(x && table && mlp->w0 && mlp->b0 && mlp->w1 && mlp->b1, "field: null buffer");
+  a.cap = n;
+  a.count = count;
+  a.x = x;
+  a.table = table;
+  a.active = active_levels < 0 ? 0 : (active_levels > a.g.L ? a.g.L : active_levels);
+  a.din = mlp->d_in;
+  a.dout = mlp->d_out;
+  a.out_cols = out_cols;
+  a.beta = mlp->beta;
+  a.thresh = mlp->threshold;
+  a.w0 = mlp->w0;
+  a.b0 = mlp->b0;
+  a.w1 = mlp->w1;
+  a.b1 = mlp->b1;
+  return SN_OK;
+}
+
+}  // namespace sn
+
+using namespace sn;
+
+extern "C" {
+
+int sn_grid_desc_init(sn_grid_desc* d, int n_levels, int n_features, int log2_hashmap_size,
+                      int base_resolution, float per_level_scale) {
+  SN_REQUIRE(d != nullptr, "grid_desc_init: null descriptor");
+  SN_REQUIRE(n_levels >= 1 && n_levels <= SN_MAX_LEVELS, "grid_desc_init: n_levels outside 1..%d",
+             SN_MAX_LEVELS);
+  SN_REQUIRE(n_features >= 1, "grid_desc_init: n_features < 1");
+  SN_REQUIRE(log2_hashmap_size >= 1 && log2_hashmap_size <= 30, "grid_desc_init: bad log2 size");
+  SN_REQUIRE(base_resolution >= 1, "grid_desc_init: base_resolution < 1");
+  SN_REQUIRE(per_level_scale >= 1.0f, "grid_desc_init: per_level_scale < 1");
+  memset(d, 0, sizeof(*d));
+  d->n_levels = n_levels;
+  d->n_features = n_features;
+  // float32 level constants, each rounded once from a double evaluation so
+  // every host (x86 or Arm libm) produces the same bits
+  const float log2_pls = (float)log2((double)per_level_scale);
+  uint32_t offset = 0;
+  for (int l = 0; l < n_levels; ++l) {
+    const float scale =
+        (float)(exp2((double)l * (double)log2_pls) * (double)base_resolution - 1.0);
+    const uint32_t res = (uint32_t)ceilf(scale) + 1u;
+    const uint32_t max_params = 0xffffffffu / 2;
+    const double dense = pow((double)res, 3.0);
+    uint32_t params = dense > (double)max_params ? max_params : res * res * res;
+    params = (params + 7u) / 8u * 8u;
+    const uint32_t hsize = 1u << log2_hashmap_size;
+    if (params > hsize) params = hsize;
+    d->scales[l] = scale;
+    d->resolutions[l] = res;
+    d->offsets[l] = offset;
+    offset += params;
+  }
+  d->offsets[n_levels] = offset;
+  return SN_OK;
+}
+
+int sn_hashgrid_fwd(int64_t n, const float* x, const float* table, const sn_grid_desc* grid,
+                    int active_levels, float* out, void* stream) {
+  GridDev g;
+  SN_TRY(make_grid_dev(grid, g));
+  SN_REQUIRE(n >= 0, "hashgrid_fwd: n < 0");
+  if (n == 0) return SN_OK;
+  const int act = active_levels < 0 ? 0 : (active_levels > g.L ? g.L : active_levels);
+  hashgrid_fwd_kernel<<<stride_grid(n * g.L, 256, 8), 256, 0, as_stream(stream)>>>(n, x, table, g,
+                                                                                  act, out);
+  return check_launch("hashgrid_fwd");
+}
+
+int sn_hashgrid_bwd(int64_t n, const float* x, const float* grad_out, const sn_grid_desc* grid,
+                    int active_levels, float* grad_table, void* stream) {
+  GridDev g;
+  SN_TRY(make_grid_dev(grid, g));
+  SN_REQUIRE(n >= 0, "hashgrid_bwd: n < 0");
+  if (n == 0) return SN_OK;
+  const int act = active_levels < 0 ? 0 : (active_levels > g.L ? g.L : active_levels);
+  hashgrid_bwd_kernel<<<stride_grid(n * g.L, 256, 8), 256, 0, as_stream(stream)>>>(
+      n, x, grad_out, g, act, grad_table);
+  return check_launch("hashgrid_bwd");
+}
+
+int sn_field_fwd(int64_t n, const int32_t* count, const float* x, const float* table,
+                 const sn_grid_desc* grid, int active_levels, const sn_mlp_desc* mlp, int out_cols,
+                 float* out, void* stream) {
+  FieldArgs a;
+  SN_TRY(fill_field_args(a, n, count, x, table, grid, active_levels, mlp, out_cols));
+  SN_REQUIRE(out != nullptr, "field_fwd: out is null");
+  a.out = out;
+  if (n == 0) return SN_OK;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(field_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
+    attr = true;
+  }
+  field_fwd_kernel<<<stride_grid(n, 128, 8), 128, kFwdSmem, as_stream(stream)>>>(a);
+  return check_launch("field_fwd");
+}
+
+int sn_field_bwd(int64_t n, const int32_t* count, const float* x, const float* grad_out,
+                 int out_cols, const float* table, const sn_grid_desc* grid, int active_levels,
+                 const sn_mlp_desc* mlp, float* grad_table, float* grad_w0, float* grad_b0,
+                 float* grad_w1, float* grad_b1, float* grad_x, void* stream) {
+  FieldArgs a;
+  SN_TRY(fill_field_args(a, n, count, x, table, grid, active_levels, mlp, out_cols));
+  SN_REQUIRE(grad_out != nullptr, "field_bwd: grad_out is null");
+  a.grad_out = grad_out;
+  a.grad_table = grad_table;
+  a.grad_w0 = grad_w0;
+  a.grad_b0 = grad_b0;
+  a.grad_w1 = grad_w1;
+  a.grad_b1 = grad_b1;
+  a.grad_x = grad_x;
+  if (n == 0) return SN_OK;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(field_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
+    attr = true;
+  }
+  field_bwd_kernel<<<stride_grid(n, kBwdThreads, 2), kBwdThreads, kBwdSmem, as_stream(stream)>>>(a);
+  return check_launch("field_bwd");
+}
+
+int sn_weightnorm_fwd(int rows, int cols, const float* v, const float* g, float* w, float* norms,
+                      void* stream) {
+  SN_REQUIRE(rows > 0 && cols > 0, "weightnorm_fwd: bad shape");
+  weightnorm_fwd_kernel<<<rows, 32, 0, as_stream(stream)>>>(rows, cols, v, g, w, norms);
+  return check_launch("weightnorm_fwd");
+}
+
+int sn_weightnorm_bwd(int rows, int cols, const float* v, const float* g, const float* norms,
+                      const float* grad_w, float* grad_v, float* grad_g, void* stream) {
+  SN_REQUIRE(rows > 0 && cols > 0, "weightnorm_bwd: bad shape");
+  weightnorm_bwd_kernel<<<rows, 32, 0, as_stream(stream)>>>(rows, cols, v, g, norms, grad_w, grad_v,
+                                                            grad_g);
+  return check_launch("weightnorm_bwd");
+}
+
+}  // extern "C"

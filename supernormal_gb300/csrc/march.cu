@@ -1,0 +1,840 @@
+// Occupancy-grid ray marching, sample packing and grid queries.
+//
+// The marcher restates nerfacc's fixed-step marcher with empty-space
+// skipping (NA/nerfacc/cuda/csrc/ray_marching.cu:9-192,
+// NA/nerfacc/cuda/csrc/include/helpers_contraction.h:16-114) so that, for
+// the same rays, t_min, step size and grid, the emitted samples are
+// bit-identical: every floating-point operation below is written with an
+// explicit rounding intrinsic in the order the reference evaluates it.
+// nvcc contracts the reference's `origin + t_mid * dir` into one FMA
+// (default -fmad=true); all other products there are exact scalings by 0.5
+// or are not followed by an addition, so they are plain roundings.
+#include "common.cuh"
+
+#include <string.h>
+
+namespace sn {
+
+static thread_local char g_err[512];
+static unsigned long long g_launches = 0;
+
+void count_launches(int k) { __atomic_fetch_add(&g_launches, (unsigned long long)k, __ATOMIC_RELAXED); }
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+int num_sms() {
+  static int cached = 0;
+  if (cached == 0) {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+      cached = v;
+    else
+      cached = 132;
+  }
+  return cached;
+}
+
+// ---------------------------------------------------------------------------
+// block-wide scan of int32 (1024 threads x 4 items = one 4096-entry tile)
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+// Exclusive scan of v[] (ITEMS consecutive entries per thread, thread-major);
+// returns the block total.  Requires blockDim.x == kScanThreads.
+__device__ int block_exclusive_scan(int (&v)[kScanItems]) {
+  __shared__ int warp_tot[kScanThreads / 32];
+  int run = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    int t = v[i];
+    v[i] = run;
+    run += t;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int w = warp_tot[lane];
+    int wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    warp_tot[lane] = wi - w;  // exclusive warp offsets
+  }
+  __syncthreads();
+  const int off = warp_tot[warp] + incl - run;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) v[i] += off;
+  int total = warp_tot[31];
+  // the last warp's exclusive offset + its inclusive total = block total
+  __shared__ int s_total;
+  if (threadIdx.x == kScanThreads - 1) s_total = off + run;
+  __syncthreads();
+  total = s_total;
+  __syncthreads();
+  return total;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+scan_tile_reduce(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ tile_sums) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  int s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i)
+    if (base + i < n) s += in[base + i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ int ws[32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int t = ws[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = t;
+  }
+}
+
+// Single block: exclusive scan of the tile sums in place; writes the total.
+__global__ void __launch_bounds__(kScanThreads)
+scan_tile_offsets(int32_t* __restrict__ tile_sums, int64_t n_tiles, int32_t* __restrict__ total) {
+  int carry = 0;
+  for (int64_t t0 = 0; t0 < n_tiles; t0 += kScanTile) {
+    int v[kScanItems];
+    const int64_t base = t0 + (int64_t)threadIdx.x * kScanItems;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) v[i] = (base + i < n_tiles) ? tile_sums[base + i] : 0;
+    int tot = block_exclusive_scan(v);
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i)
+      if (base + i < n_tiles) tile_sums[base + i] = v[i] + carry;
+    carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && total) *total = carry;
+}
+
+// Scans each tile, adds the tile offset and writes packed_info = {offset, count}.
+__global__ void __launch_bounds__(kScanThreads)
+scan_tile_apply(const int32_t* __restrict__ in, int64_t n, const int32_t* __restrict__ tile_offsets,
+                int32_t* __restrict__ packed, int32_t* __restrict__ total) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  int v[kScanItems], c[kScanItems];
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) c[i] = v[i] = (base + i < n) ? in[base + i] : 0;
+  int tot = block_exclusive_scan(v);
+  const int off = tile_offsets ? tile_offsets[blockIdx.x] : 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    if (base + i < n) {
+      int2 pk = make_int2(v[i] + off, c[i]);
+      reinterpret_cast<int2*>(packed)[base + i] = pk;
+    }
+  }
+  if (!tile_offsets && threadIdx.x == 0 && total) *total = tot;
+}
+
+int pack_counts(int64_t n, const int32_t* counts, int32_t* packed, int32_t* total, void* ws,
+                cudaStream_t st) {
+  if (n == 0) {
+    if (total) {
+      if (cudaMemsetAsync(total, 0, sizeof(int32_t), st) != cudaSuccess) {
+        set_error("pack_counts: memset failed");
+        return SN_ERR_CUDA;
+      }
+    }
+    return SN_OK;
+  }
+  const int64_t n_tiles = (n + kScanTile - 1) / kScanTile;
+  if (n_tiles == 1) {
+    scan_tile_apply<<<1, kScanThreads, 0, st>>>(counts, n, nullptr, packed, total);
+    return check_launch("pack_counts");
+  }
+  SN_REQUIRE(ws != nullptr, "pack_counts: workspace required for n=%lld", (long long)n);
+  int32_t* tiles = reinterpret_cast<int32_t*>(ws);
+  scan_tile_reduce<<<(unsigned)n_tiles, kScanThreads, 0, st>>>(counts, n, tiles);
+  scan_tile_offsets<<<1, kScanThreads, 0, st>>>(tiles, n_tiles, total);
+  scan_tile_apply<<<(unsigned)n_tiles, kScanThreads, 0, st>>>(counts, n, tiles, packed, nullptr);
+  return check_launch("pack_counts", 3);
+}
+
+// ---------------------------------------------------------------------------
+// counts / unpack
+// ---------------------------------------------------------------------------
+__global__ void count_indices_kernel(int64_t n, const int64_t* __restrict__ idx, int64_t n_rays,
+                                     int32_t* __restrict__ counts) {
+  // warp-uniform loop so the whole warp takes part in every ballot/match
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) - lane;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t b = warp0; b < n; b += stride) {
+    const int64_t s = b + lane;
+    const int64_t r = s < n ? idx[s] : -1;
+    const bool ok = r >= 0 && r < n_rays;
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (ok) {
+      // samples of one ray are usually adjacent: one atomic per distinct key
+      const unsigned peers = __match_any_sync(m, r);
+      if (lane == __ffs(peers) - 1) atomicAdd(&counts[r], __popc(peers));
+    }
+  }
+}
+
+__global__ void unpack_info_kernel(int64_t n_rays, const int32_t* __restrict__ packed,
+                                   int64_t n_samples, int64_t* __restrict__ out) {
+  // one warp per ray: lanes write the ray's samples cooperatively
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < n_rays;
+       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int base = packed[2 * r], cnt = packed[2 * r + 1];
+    for (int j = lane; j < cnt; j += 32) {
+      int64_t s = (int64_t)base + j;
+      if (s < n_samples) out[s] = r;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// marcher
+// ---------------------------------------------------------------------------
+struct GridView {
+  const float* roi;  // device, 6 floats: {min xyz, max xyz}
+  float lo[3], hi[3];
+  int res[3];
+  const uint8_t* bits;
+  int ctype;
+};
+
+__device__ __forceinline__ void load_roi(GridView& g) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    g.lo[d] = g.roi[d];
+    g.hi[d] = g.roi[3 + d];
+  }
+}
+
+// roi -> [0,1]^3 and the two unbounded contractions
+// (NA/nerfacc/cuda/csrc/include/helpers_contraction.h:16-114).
+__device__ __forceinline__ void contract(const GridView& g, const float p[3], float u[3]) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) u[d] = __fdiv_rn(__fsub_rn(p[d], g.lo[d]), __fsub_rn(g.hi[d], g.lo[d]));
+  if (g.ctype == SN_CONTRACTION_UN_BOUNDED_TANH) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) u[d] = __fmaf_rn(tanhf(__fsub_rn(u[d], 0.5f)), 0.5f, 0.5f);
+  } else if (g.ctype == SN_CONTRACTION_UN_BOUNDED_SPHERE) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) u[d] = __fmaf_rn(u[d], 2.0f, -1.0f);
+    float nsq = __fmaf_rn(u[2], u[2], __fmaf_rn(u[1], u[1], __fmul_rn(u[0], u[0])));
+    float nrm = sqrtf(nsq);
+    if (nrm > 1.0f) {
+      float k = __fsub_rn(2.0f, __fdiv_rn(1.0f, nrm));
+#pragma unroll
+      for (int d = 0; d < 3; ++d) u[d] = __fmul_rn(k, __fdiv_rn(u[d], nrm));
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) u[d] = __fmaf_rn(u[d], 0.25f, 0.5f);
+  }
+}
+
+// grid_occupied_at + grid_idx_at (NA/nerfacc/cuda/csrc/ray_marching.cu:16-45):
+// AABB rejection, contraction, truncating int conversion, clamp, x-major index.
+__device__ __forceinline__ bool occupied_at(const GridView& g, const float p[3]) {
+  if (g.ctype == SN_CONTRACTION_AABB &&
+      (p[0] < g.lo[0] || p[0] > g.hi[0] || p[1] < g.lo[1] || p[1] > g.hi[1] ||
+       p[2] < g.lo[2] || p[2] > g.hi[2]))
+    return false;
+  float u[3];
+  contract(g, p, u);
+  int ix[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    int v = (int)__fmul_rn(u[d], (float)g.res[d]);
+    v = v < 0 ? 0 : v;
+    v = v > g.res[d] - 1 ? g.res[d] - 1 : v;
+    ix[d] = v;
+  }
+  const int idx = ix[0] * (g.res[1] * g.res[2]) + ix[1] * g.res[2] + ix[2];
+  return g.bits[idx] != 0;
+}
+
+// distance_to_next_voxel + advance_to_next_voxel
+// (NA/nerfacc/cuda/csrc/ray_marching.cu:47-75): DDA target, then stepping in
+// dt_min increments (at least one) so samples stay on the marching lattice.
+__device__ __forceinline__ float advance_voxel(const GridView& g, float t, float dt_min,
+                                               const float p[3], const float dir[3],
+                                               const float inv[3], float far) {
+  float tx[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float ext = __fsub_rn(g.hi[d], g.lo[d]);
+    const float res = (float)g.res[d];
+    const float xu = __fmul_rn(__fdiv_rn(__fsub_rn(p[d], g.lo[d]), ext), res);
+    const float f = floorf(__fadd_rn(__fadd_rn(xu, 0.5f), copysignf(0.5f, dir[d])));
+    tx[d] = __fmul_rn(__fdiv_rn(__fmul_rn(__fsub_rn(f, xu), inv[d]), res), ext);
+  }
+  float dist = fminf(fminf(tx[0], tx[1]), tx[2]);
+  dist = fmaxf(dist, 0.0f);
+  float target = fminf(__fadd_rn(t, dist), far);
+  float s = t;
+  do {
+    s = __fadd_rn(s, dt_min);
+  } while (s < target);
+  return s;
+}
+
+__device__ __forceinline__ float calc_dt(float t, float cone, float dt_min, float dt_max) {
+  return fminf(fmaxf(__fmul_rn(t, cone), dt_min), dt_max);
+}
+
+struct MarchArgs {
+  int64_t n_rays;
+  const float* rays_o;
+  const float* rays_d;
+  const float* t_min;
+  const float* t_max;
+  const float* jitter;
+  GridView grid;
+  float step;
+  float cone;
+  int64_t max_iters;
+  const int32_t* packed;
+  int64_t capacity;
+  int32_t* num_steps;
+  int64_t* ray_indices;
+  float* t_starts;
+  float* t_ends;
+  int32_t* status;
+};
+
+template <bool FILL>
+__global__ void __launch_bounds__(128) march_kernel(MarchArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= a.n_rays) return;
+  GridView g = a.grid;
+  load_roi(g);
+  float o[3], d[3], inv[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    o[k] = a.rays_o[3 * i + k];
+    d[k] = a.rays_d[3 * i + k];
+    inv[k] = __fdiv_rn(1.0f, d[k]);
+  }
+  float near = a.t_min[i];
+  const float far = a.t_max[i];
+  if (a.jitter) near = __fadd_rn(near, __fmul_rn(a.jitter[i], a.step));
+
+  int64_t base = 0, room = 0;
+  if (FILL) {
+    base = a.packed[2 * i];
+    room = a.packed[2 * i + 1];
+  }
+  const float dt_min = a.step, dt_max = 1e10f;
+  int64_t j = 0, iters = 0;
+  float t0 = near;
+  float dt = calc_dt(t0, a.cone, dt_min, dt_max);
+  float t1 = __fadd_rn(t0, dt);
+  float tm = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
+  bool overflow = false;
+  while (tm < far) {
+    if (++iters > a.max_iters) {
+      atomicOr(a.status, SN_STATUS_MARCH_LIMIT);
+      break;
+    }
+    float p[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) p[k] = __fmaf_rn(tm, d[k], o[k]);
+    if (occupied_at(g, p)) {
+      if (FILL) {
+        if (j < room && base + j < a.capacity) {
+          a.t_starts[base + j] = t0;
+          a.t_ends[base + j] = t1;
+          a.ray_indices[base + j] = i;
+        } else {
+          overflow = true;
+        }
+      }
+      ++j;
+      t0 = t1;
+      t1 = __fadd_rn(t0, calc_dt(t0, a.cone, dt_min, dt_max));
+      tm = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
+    } else if (g.ctype == SN_CONTRACTION_AABB) {
+      tm = advance_voxel(g, tm, dt_min, p, d, inv, far);
+      dt = calc_dt(tm, a.cone, dt_min, dt_max);
+      t0 = __fsub_rn(tm, __fmul_rn(dt, 0.5f));
+      t1 = __fadd_rn(tm, __fmul_rn(dt, 0.5f));
+    } else {
+      t0 = t1;
+      t1 = __fadd_rn(t0, calc_dt(t0, a.cone, dt_min, dt_max));
+      tm = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
+    }
+  }
+  if (!FILL) a.num_steps[i] = (int32_t)j;
+  if (FILL && overflow && a.status) atomicOr(a.status, SN_STATUS_CAPACITY);
+}
+
+__global__ void grid_query_kernel(int64_t n, const float* __restrict__ x, GridView g,
+                                  uint8_t* __restrict__ out) {
+  load_roi(g);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float p[3] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+    out[i] = occupied_at(g, p) ? 1 : 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// occupancy grid maintenance
+// ---------------------------------------------------------------------------
+// contract_inv for the three contraction types
+// (NA/nerfacc/cuda/csrc/include/helpers_contraction.h:23-129).
+__device__ __forceinline__ void contract_inv(const float lo[3], const float hi[3], int ctype,
+                                             float u[3]) {
+  if (ctype == SN_CONTRACTION_UN_BOUNDED_TANH) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      float v = atanhf(__fmaf_rn(u[d], 2.0f, -1.0f));
+      v = fminf(fmaxf(v, -1e10f), 1e10f);
+      u[d] = __fadd_rn(v, 0.5f);
+    }
+  } else if (ctype == SN_CONTRACTION_UN_BOUNDED_SPHERE) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) u[d] = __fmul_rn(__fsub_rn(u[d], 0.5f), 4.0f);
+    float nsq = __fmaf_rn(u[2], u[2], __fmaf_rn(u[1], u[1], __fmul_rn(u[0], u[0])));
+    float nrm = sqrtf(nsq);
+    if (nrm > 1.0f) {
+      float den = fmaxf(__fsub_rn(__fmul_rn(2.0f, nrm), __fmul_rn(1.0f, nsq)), 1e-10f);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) u[d] = __fdiv_rn(u[d], den);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) u[d] = __fmaf_rn(u[d], 0.5f, 0.5f);
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) u[d] = __fmaf_rn(u[d], __fsub_rn(hi[d], lo[d]), lo[d]);
+}
+
+__global__ void occ_points_kernel(int64_t n, const int64_t* __restrict__ cells,
+                                  const float* __restrict__ jitter, int rx, int ry, int rz,
+                                  const float* __restrict__ roi, int ctype, float* __restrict__ x) {
+  float lo[3], hi[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = roi[d];
+    hi[d] = roi[3 + d];
+  }
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = cells ? cells[i] : i;
+    const int64_t cz = c % rz, cy = (c / rz) % ry, cx = c / ((int64_t)ry * rz);
+    float u[3];
+    u[0] = __fdiv_rn(__fadd_rn((float)cx, jitter[3 * i + 0]), (float)rx);
+    u[1] = __fdiv_rn(__fadd_rn((float)cy, jitter[3 * i + 1]), (float)ry);
+    u[2] = __fdiv_rn(__fadd_rn((float)cz, jitter[3 * i + 2]), (float)rz);
+    contract_inv(lo, hi, ctype, u);
+    x[3 * i + 0] = u[0];
+    x[3 * i + 1] = u[1];
+    x[3 * i + 2] = u[2];
+  }
+}
+
+// occs >= 0 always (EMA of sigmoid values), so float order == int bit order.
+__global__ void occ_ema_kernel(int64_t n, const int64_t* __restrict__ cells,
+                               const float* __restrict__ occ, float decay, float* __restrict__ occs) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = cells ? cells[i] : i;
+    const float v = fmaxf(__fmul_rn(occs[c], decay), occ[i]);
+    if (cells)
+      atomicMax(reinterpret_cast<int*>(occs) + c, __float_as_int(fmaxf(v, 0.0f)));
+    else
+      occs[c] = v;
+  }
+}
+
+constexpr int kReduceThreads = 512;
+
+__global__ void __launch_bounds__(kReduceThreads)
+occ_partial_sum(int64_t n, const float* __restrict__ occs, double* __restrict__ partial) {
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    s += (double)occs[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ double ws[kReduceThreads / 32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = threadIdx.x < kReduceThreads / 32 ? ws[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(kReduceThreads)
+occ_threshold_kernel(int64_t n, const float* __restrict__ occs, const double* __restrict__ partial,
+                     int n_partial, float thre, uint8_t* __restrict__ binary, float* mean_out) {
+  __shared__ float s_thr;
+  if (threadIdx.x < 32) {
+    double t = 0.0;
+    for (int k = threadIdx.x; k < n_partial; k += 32) t += partial[k];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) {
+      const float mean = (float)(t / (double)n);
+      s_thr = fminf(mean, thre);
+      if (mean_out && blockIdx.x == 0) *mean_out = mean;
+    }
+  }
+  __syncthreads();
+  const float thr = s_thr;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    binary[i] = occs[i] > thr ? 1 : 0;
+}
+
+// ---- device-side occupancy update (no host synchronisation) ----------------
+// Query points of cells[i] (or cell i) with in-kernel jitter for i < *count.
+__global__ void occ_points_n_kernel(int64_t cap, const int32_t* __restrict__ count,
+                                    const int64_t* __restrict__ cells, uint64_t seed,
+                                    const int32_t* __restrict__ stream_dev, int rx, int ry, int rz,
+                                    const float* __restrict__ roi, int ctype, float* __restrict__ x) {
+  const int64_t n = count ? min((int64_t)*count, cap) : cap;
+  const uint64_t sid = stream_dev ? (uint64_t)(uint32_t)*stream_dev : 0ull;
+  float lo[3], hi[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = roi[d];
+    hi[d] = roi[3 + d];
+  }
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = cells ? cells[i] : i;
+    const int64_t cz = c % rz, cy = (c / rz) % ry, cx = c / ((int64_t)ry * rz);
+    float u[3];
+    u[0] = __fdiv_rn(__fadd_rn((float)cx, uniform01(seed, sid, 3 * (uint64_t)i + 0)), (float)rx);
+    u[1] = __fdiv_rn(__fadd_rn((float)cy, uniform01(seed, sid, 3 * (uint64_t)i + 1)), (float)ry);
+    u[2] = __fdiv_rn(__fadd_rn((float)cz, uniform01(seed, sid, 3 * (uint64_t)i + 2)), (float)rz);
+    contract_inv(lo, hi, ctype, u);
+    x[3 * i + 0] = u[0];
+    x[3 * i + 1] = u[1];
+    x[3 * i + 2] = u[2];
+  }
+}
+
+// occs[c] = max(occs[c]*decay, sigmoid(-k*sdf)) (renderer occ_eval_fn,
+// models/renderer.py:56-60, fused with NA/nerfacc/grid.py:229-230).
+__global__ void occ_ema_sdf_kernel(int64_t cap, const int32_t* __restrict__ count,
+                                   const int64_t* __restrict__ cells, const float* __restrict__ sdf,
+                                   float k, float decay, float* __restrict__ occs) {
+  const int64_t n = count ? min((int64_t)*count, cap) : cap;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = cells ? cells[i] : i;
+    const float occ = 1.0f / (1.0f + expf(__fmul_rn(sdf[i], k)));
+    const float v = fmaxf(__fmul_rn(occs[c], decay), occ);
+    if (cells)
+      atomicMax(reinterpret_cast<int*>(occs) + c, __float_as_int(fmaxf(v, 0.0f)));
+    else
+      occs[c] = v;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+u8_tile_count(const uint8_t* __restrict__ bits, int64_t n, int32_t* __restrict__ tile_sums) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  int s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i)
+    if (base + i < n) s += bits[base + i] ? 1 : 0;
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ int ws[32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int t = ws[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+u8_tile_compact(const uint8_t* __restrict__ bits, int64_t n, const int32_t* __restrict__ tile_off,
+                int32_t* __restrict__ list) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  int v[kScanItems], f[kScanItems];
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) f[i] = v[i] = (base + i < n && bits[base + i]) ? 1 : 0;
+  block_exclusive_scan(v);
+  const int off = tile_off[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i)
+    if (f[i]) list[off + v[i]] = (int32_t)(base + i);
+}
+
+// cells[0, n_uniform) uniform over the grid; then min(n_occ, n_uniform)
+// occupied cells (all of them, or a uniform draw when there are more),
+// as NA/nerfacc/grid.py:168-182 does; *count = total.
+__global__ void occ_select_kernel(int64_t n_cells, int64_t n_uniform, const int32_t* __restrict__ list,
+                                  const int32_t* __restrict__ n_occ_dev, uint64_t seed,
+                                  const int32_t* __restrict__ stream_dev, int64_t* __restrict__ cells,
+                                  int32_t* __restrict__ count) {
+  const int64_t n_occ = *n_occ_dev;
+  const uint64_t sid = stream_dev ? (uint64_t)(uint32_t)*stream_dev : 0ull;
+  const int64_t n_take = n_occ < n_uniform ? n_occ : n_uniform;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *count = (int32_t)(n_uniform + n_take);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_uniform;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    cells[i] = (int64_t)(uniform_u32(seed, sid ^ 0x5151u, (uint64_t)i) % (uint64_t)n_cells);
+    if (i < n_take) {
+      const int64_t j = n_occ > n_uniform
+                            ? (int64_t)(uniform_u32(seed, sid ^ 0xA3A3u, (uint64_t)i) % (uint64_t)n_occ)
+                            : i;
+      cells[n_uniform + i] = list[j];
+    }
+  }
+}
+
+static int make_grid(GridView& g, const float* roi, const uint8_t* bits, int rx, int ry, int rz,
+                     int ctype) {
+  SN_REQUIRE(roi != nullptr, "roi is null");
+  g.roi = roi;
+  SN_REQUIRE(rx > 0 && ry > 0 && rz > 0, "grid resolution must be positive (%d,%d,%d)", rx, ry, rz);
+  SN_REQUIRE(ctype >= 0 && ctype <= 2, "unknown contraction type %d", ctype);
+  SN_REQUIRE(bits != nullptr, "grid_binary is null");
+  g.res[0] = rx;
+  g.res[1] = ry;
+  g.res[2] = rz;
+  g.bits = bits;
+  g.ctype = ctype;
+  return SN_OK;
+}
+
+}  // namespace sn
+
+using namespace sn;
+
+extern "C" {
+
+const char* sn_version(void) { return "supernormal_gb300 0.1.0 (sm_103a)"; }
+
+const char* sn_last_error(void) { return sn::g_err; }
+
+uint64_t sn_kernel_launches(void) { return __atomic_load_n(&sn::g_launches, __ATOMIC_RELAXED); }
+
+size_t sn_scan_workspace_bytes(int64_t n) {
+  const int64_t n_tiles = (n + sn::kScanTile - 1) / sn::kScanTile;
+  size_t b = (size_t)(n_tiles > 0 ? n_tiles : 1) * sizeof(int32_t);
+  return (b + 255) & ~(size_t)255;
+}
+
+int sn_pack_counts(int64_t n, const int32_t* counts, int32_t* packed_info, int32_t* total,
+                   void* workspace, void* stream) {
+  SN_REQUIRE(n >= 0, "pack_counts: n < 0");
+  SN_REQUIRE(n <= ((int64_t)1 << 31) - 1, "pack_counts: n too large");
+  SN_REQUIRE(n == 0 || (counts && packed_info), "pack_counts: null buffer");
+  return sn::pack_counts(n, counts, packed_info, total, workspace, as_stream(stream));
+}
+
+int sn_count_indices(int64_t n_samples, const int64_t* ray_indices, int64_t n_rays, int32_t* counts,
+                     void* stream) {
+  SN_REQUIRE(n_samples >= 0 && n_rays >= 0, "count_indices: negative size");
+  cudaStream_t st = as_stream(stream);
+  if (n_rays > 0 && cudaMemsetAsync(counts, 0, (size_t)n_rays * sizeof(int32_t), st) != cudaSuccess) {
+    set_error("count_indices: memset failed");
+    return SN_ERR_CUDA;
+  }
+  if (n_samples == 0) return SN_OK;
+  count_indices_kernel<<<stride_grid(n_samples, 256, 8), 256, 0, st>>>(n_samples, ray_indices,
+                                                                       n_rays, counts);
+  return check_launch("count_indices");
+}
+
+int sn_unpack_info(int64_t n_rays, const int32_t* packed_info, int64_t n_samples,
+                   int64_t* ray_indices, void* stream) {
+  SN_REQUIRE(n_rays >= 0 && n_samples >= 0, "unpack_info: negative size");
+  if (n_rays == 0 || n_samples == 0) return SN_OK;
+  unpack_info_kernel<<<stride_grid(n_rays * 32, 256, 8), 256, 0, as_stream(stream)>>>(
+      n_rays, packed_info, n_samples, ray_indices);
+  return check_launch("unpack_info");
+}
+
+static int march_common(MarchArgs& a, int64_t n_rays, const float* rays_o, const float* rays_d,
+                        const float* t_min, const float* t_max, const float* jitter,
+                        const float* roi, const uint8_t* grid_binary, int rx, int ry, int rz,
+                        int ctype, float step, float cone, int64_t max_iters, int32_t* status) {
+  SN_REQUIRE(n_rays >= 0, "march: n_rays < 0");
+  SN_REQUIRE(step > 0.0f && step < 1e30f, "march: step_size must be positive and finite (got %g)",
+             (double)step);
+  SN_REQUIRE(cone >= 0.0f && cone < 1e30f, "march: cone_angle must be >= 0 (got %g)", (double)cone);
+  SN_REQUIRE(status != nullptr, "march: a device status word is required");
+  SN_REQUIRE(roi != nullptr, "march: roi is null");
+  memset(&a, 0, sizeof(a));
+  SN_TRY(make_grid(a.grid, roi, grid_binary, rx, ry, rz, ctype));
+  a.n_rays = n_rays;
+  a.rays_o = rays_o;
+  a.rays_d = rays_d;
+  a.t_min = t_min;
+  a.t_max = t_max;
+  a.jitter = jitter;
+  a.step = step;
+  a.cone = cone;
+  a.max_iters = max_iters > 0 ? max_iters : ((int64_t)1 << 24);
+  a.status = status;
+  return SN_OK;
+}
+
+
+int sn_march_count(int64_t n_rays, const float* rays_o, const float* rays_d, const float* t_min,
+                   const float* t_max, const float* jitter, const float* roi,
+                   const uint8_t* grid_binary, int rx, int ry, int rz, int contraction_type,
+                   float step_size, float cone_angle, int64_t max_iters, int32_t* num_steps,
+                   int32_t* status, void* stream) {
+  MarchArgs a;
+  SN_TRY(march_common(a, n_rays, rays_o, rays_d, t_min, t_max, jitter, roi, grid_binary, rx, ry, rz,
+                      contraction_type, step_size, cone_angle, max_iters, status));
+  if (n_rays == 0) return SN_OK;
+  a.num_steps = num_steps;
+  march_kernel<false><<<div_up(n_rays, 128), 128, 0, as_stream(stream)>>>(a);
+  return check_launch("march_count");
+}
+
+int sn_march_fill(int64_t n_rays, const float* rays_o, const float* rays_d, const float* t_min,
+                  const float* t_max, const float* jitter, const float* roi,
+                  const uint8_t* grid_binary, int rx, int ry, int rz, int contraction_type,
+                  float step_size, float cone_angle, int64_t max_iters,
+                  const int32_t* packed_info, int64_t capacity, int64_t* ray_indices,
+                  float* t_starts, float* t_ends, int32_t* status, void* stream) {
+  MarchArgs a;
+  SN_TRY(march_common(a, n_rays, rays_o, rays_d, t_min, t_max, jitter, roi, grid_binary, rx, ry, rz,
+                      contraction_type, step_size, cone_angle, max_iters, status));
+  SN_REQUIRE(capacity >= 0, "march_fill: capacity < 0");
+  if (n_rays == 0) return SN_OK;
+  SN_REQUIRE(packed_info != nullptr, "march_fill: packed_info is null");
+  a.packed = packed_info;
+  a.capacity = capacity;
+  a.ray_indices = ray_indices;
+  a.t_starts = t_starts;
+  a.t_ends = t_ends;
+  march_kernel<true><<<div_up(n_rays, 128), 128, 0, as_stream(stream)>>>(a);
+  return check_launch("march_fill");
+}
+
+int sn_grid_query(int64_t n, const float* samples, const float* roi, const uint8_t* grid_binary,
+                  int rx, int ry, int rz, int contraction_type, uint8_t* out, void* stream) {
+  SN_REQUIRE(n >= 0, "grid_query: n < 0");
+  GridView g;
+  memset(&g, 0, sizeof(g));
+  SN_TRY(make_grid(g, roi, grid_binary, rx, ry, rz, contraction_type));
+  if (n == 0) return SN_OK;
+  grid_query_kernel<<<stride_grid(n, 256, 8), 256, 0, as_stream(stream)>>>(n, samples, g, out);
+  return check_launch("grid_query");
+}
+
+int sn_occ_points(int64_t n, const int64_t* cells, const float* jitter, int rx, int ry, int rz,
+                  const float* roi, int contraction_type, float* x_out, void* stream) {
+  SN_REQUIRE(n >= 0, "occ_points: n < 0");
+  SN_REQUIRE(rx > 0 && ry > 0 && rz > 0, "occ_points: bad resolution");
+  SN_REQUIRE(contraction_type >= 0 && contraction_type <= 2, "occ_points: bad contraction");
+  SN_REQUIRE(roi && jitter && x_out, "occ_points: null buffer");
+  if (n == 0) return SN_OK;
+  occ_points_kernel<<<stride_grid(n, 256, 8), 256, 0, as_stream(stream)>>>(
+      n, cells, jitter, rx, ry, rz, roi, contraction_type, x_out);
+  return check_launch("occ_points");
+}
+
+int sn_occ_ema_update(int64_t n, const int64_t* cells, const float* occ, float ema_decay,
+                      float* occs, void* stream) {
+  SN_REQUIRE(n >= 0, "occ_ema_update: n < 0");
+  SN_REQUIRE(ema_decay >= 0.0f, "occ_ema_update: ema_decay < 0");
+  if (n == 0) return SN_OK;
+  occ_ema_kernel<<<stride_grid(n, 256, 8), 256, 0, as_stream(stream)>>>(n, cells, occ, ema_decay,
+                                                                        occs);
+  return check_launch("occ_ema_update");
+}
+
+size_t sn_occ_binarize_workspace_bytes(int64_t n_cells) {
+  (void)n_cells;
+  return (size_t)(4 * 1024) * sizeof(double);
+}
+
+int sn_occ_binarize(int64_t n_cells, const float* occs, float occ_thre, uint8_t* binary,
+                    float* mean_out, void* workspace, void* stream) {
+  SN_REQUIRE(n_cells > 0, "occ_binarize: n_cells must be > 0");
+  SN_REQUIRE(workspace != nullptr, "occ_binarize: workspace required");
+  cudaStream_t st = as_stream(stream);
+  int nb = (int)stride_grid(n_cells, kReduceThreads, 4);
+  if (nb > 4096) nb = 4096;
+  double* partial = reinterpret_cast<double*>(workspace);
+  occ_partial_sum<<<nb, kReduceThreads, 0, st>>>(n_cells, occs, partial);
+  occ_threshold_kernel<<<stride_grid(n_cells, kReduceThreads, 4), kReduceThreads, 0, st>>>(
+      n_cells, occs, partial, nb, occ_thre, binary, mean_out);
+  return check_launch("occ_binarize", 2);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int sn_occ_points_n(int64_t cap, const int32_t* count, const int64_t* cells, uint64_t seed,
+                    const int32_t* stream_counter, int rx, int ry, int rz, const float* roi,
+                    int contraction_type, float* x_out, void* stream) {
+  SN_REQUIRE(cap >= 0, "occ_points_n: cap < 0");
+  SN_REQUIRE(rx > 0 && ry > 0 && rz > 0, "occ_points_n: bad resolution");
+  SN_REQUIRE(contraction_type >= 0 && contraction_type <= 2, "occ_points_n: bad contraction");
+  SN_REQUIRE(roi && x_out, "occ_points_n: null buffer");
+  if (cap == 0) return SN_OK;
+  occ_points_n_kernel<<<stride_grid(cap, 256, 8), 256, 0, as_stream(stream)>>>(
+      cap, count, cells, seed, stream_counter, rx, ry, rz, roi, contraction_type, x_out);
+  return check_launch("occ_points_n");
+}
+
+int sn_occ_ema_sdf(int64_t cap, const int32_t* count, const int64_t* cells, const float* sdf,
+                   float sigmoid_k, float ema_decay, float* occs, void* stream) {
+  SN_REQUIRE(cap >= 0, "occ_ema_sdf: cap < 0");
+  SN_REQUIRE(sdf && occs, "occ_ema_sdf: null buffer");
+  if (cap == 0) return SN_OK;
+  occ_ema_sdf_kernel<<<stride_grid(cap, 256, 8), 256, 0, as_stream(stream)>>>(
+      cap, count, cells, sdf, sigmoid_k, ema_decay, occs);
+  return check_launch("occ_ema_sdf");
+}
+
+size_t sn_occ_sample_workspace_bytes(int64_t n_cells) {
+  const int64_t n_tiles = (n_cells + sn::kScanTile - 1) / sn::kScanTile;
+  size_t b = (size_t)(n_tiles + 1) * sizeof(int32_t) + 256;   // tile offsets + total
+  b += (size_t)n_cells * sizeof(int32_t);                      // occupied list
+  return (b + 255) & ~(size_t)255;
+}
+
+int sn_occ_sample_cells(int64_t n_cells, const uint8_t* binary, int64_t n_uniform, uint64_t seed,
+                        const int32_t* stream_counter, int64_t* cells, int32_t* count,
+                        void* workspace, void* stream) {
+  SN_REQUIRE(n_cells > 0 && n_uniform >= 0, "occ_sample_cells: bad sizes");
+  SN_REQUIRE(binary && cells && count && workspace, "occ_sample_cells: null buffer");
+  cudaStream_t st = as_stream(stream);
+  const int64_t n_tiles = (n_cells + kScanTile - 1) / kScanTile;
+  int32_t* tiles = reinterpret_cast<int32_t*>(workspace);
+  int32_t* n_occ = tiles + n_tiles;
+  int32_t* list = reinterpret_cast<int32_t*>(
+      (reinterpret_cast<uintptr_t>(tiles + n_tiles + 1) + 255) & ~(uintptr_t)255);
+  u8_tile_count<<<(unsigned)n_tiles, kScanThreads, 0, st>>>(binary, n_cells, tiles);
+  scan_tile_offsets<<<1, kScanThreads, 0, st>>>(tiles, n_tiles, n_occ);
+  u8_tile_compact<<<(unsigned)n_tiles, kScanThreads, 0, st>>>(binary, n_cells, tiles, list);
+  occ_select_kernel<<<stride_grid(n_uniform > 0 ? n_uniform : 1, 256, 8), 256, 0, st>>>(
+      n_cells, n_uniform, list, n_occ, seed, stream_counter, cells, count);
+  return check_launch("occ_sample_cells", 4);
+}
+
+}  // extern "C"

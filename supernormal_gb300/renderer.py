@@ -1,0 +1,182 @@
+"""Patch-based NeuS renderer on the fused kernels: drop-in for models/renderer.py.
+
+``NeuSRenderer.render`` keeps the reference inputs and outputs
+(models/renderer.py:63-276): centre-ray marching with SDF-alpha culling,
+patch expansion through the marching plane, one field evaluation for all
+patch pixels, then NeuS alpha, patch weights, dfd normals and accumulation
+in one fused kernel whose backward is hand-written.  The returned tensors
+are autograd-connected, so the caller's losses (exp_runner.py:191-203)
+back-propagate through the custom kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+from torch import Tensor
+
+from ._lib import call, stream_handle
+from .nerfacc import ContractionType, OccupancyGrid, _pack_counts, ray_marching
+
+__all__ = ["NeuSRenderer", "near_far_from_sphere"]
+
+
+def near_far_from_sphere(rays_o: Tensor, rays_d: Tensor):
+    """Unit-sphere chord (models/dataset_loader.py:279-297)."""
+    a = torch.sum(rays_d ** 2, dim=-1, keepdim=True)
+    b = 2.0 * torch.sum(rays_o * rays_d, dim=-1, keepdim=True)
+    c = torch.sum(rays_o ** 2, dim=-1, keepdim=True) - 1.0
+    mid = 0.5 * (-b) / a
+    near = mid - torch.sqrt(b ** 2 - 4 * a * c) / (2 * a)
+    far = mid + torch.sqrt(b ** 2 - 4 * a * c) / (2 * a)
+    return near[..., 0], far[..., 0]
+
+
+class PatchGeometry:
+    """No-grad per-step geometry shared by the forward and backward kernels."""
+
+    def __init__(self, H, W, packed, S, end_packed, E, t_pix_s, t_pix_e, rays_o, rays_d, vinv):
+        self.H, self.W, self.P = H, W, H * W
+        self.packed, self.S, self.end_packed, self.E = packed, S, end_packed, E
+        self.t_pix_s, self.t_pix_e = t_pix_s, t_pix_e
+        self.rays_o, self.rays_d, self.vinv = rays_o, rays_d, vinv
+        self.n_patches = packed.shape[0]
+
+
+class _PatchRenderFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, sdf: Tensor, variance: Tensor, geo: PatchGeometry):
+        dev = sdf.device
+        B, P, S = geo.n_patches, geo.P, geo.S
+        sdf = sdf.contiguous().float().reshape(-1)
+        var = variance.detach().reshape(1).contiguous().float()
+        comp = torch.empty((B, P, 3), device=dev)
+        wsum = torch.empty((B, P), device=dev)
+        grads = torch.empty((S, P, 3), device=dev)
+        call("sn_patch_render_fwd", B, geo.H, geo.W, geo.packed, None, S, geo.end_packed, sdf,
+             geo.t_pix_s, geo.t_pix_e, geo.rays_o, geo.rays_d, geo.vinv, var, None, None, grads,
+             comp, wsum, stream_handle())
+        ctx.save_for_backward(sdf, var)
+        ctx.geo = geo
+        return comp, wsum, grads
+
+    @staticmethod
+    def backward(ctx, g_comp, g_wsum, g_grads):
+        sdf, var = ctx.saved_tensors
+        geo = ctx.geo
+        dev = sdf.device
+        B, P, S = geo.n_patches, geo.P, geo.S
+        g_comp = torch.zeros((B, P, 3), device=dev) if g_comp is None else g_comp.contiguous().float()
+        g_wsum = torch.zeros((B, P), device=dev) if g_wsum is None else g_wsum.contiguous().float()
+        g_grads = None if g_grads is None else g_grads.contiguous().float()
+        d_sdf = torch.empty_like(sdf)
+        partials = torch.zeros((B, 4), device=dev)
+        carry = torch.empty((B, P), device=dev)
+        st = stream_handle()
+        call("sn_patch_render_bwd", B, geo.H, geo.W, geo.packed, None, S, geo.end_packed, sdf,
+             geo.t_pix_s, geo.t_pix_e, geo.rays_o, geo.rays_d, geo.vinv, var, g_comp, g_wsum,
+             g_grads, d_sdf, partials, carry, st)
+        call("sn_patch_carry_fixup", B, P, geo.packed, None, S, geo.end_packed, carry, d_sdf, st)
+        d_var = torch.zeros((1,), device=dev)
+        call("sn_patch_finalize", B, P, partials, None, S, var, None, 0.0, 0.0, 0.0, None, d_var, st)
+        return d_sdf, d_var.reshape(()), None
+
+
+class NeuSRenderer:
+    def __init__(self, sdf_network, deviation_network, gradient_method="dfd"):
+        self.sdf_network = sdf_network
+        self.deviation_network = deviation_network
+        self.scene_aabb = torch.as_tensor([-1., -1., -1., 1., 1., 1.], dtype=torch.float32)
+        self.contraction_type = ContractionType.AABB
+        self.occupancy_grid = OccupancyGrid(roi_aabb=self.scene_aabb, resolution=128,
+                                            contraction_type=self.contraction_type).to("cuda")
+        self.sampling_step_size = 0.01
+        self.gradient_method = gradient_method
+
+    def occ_eval_fn(self, x):
+        sdf = self.sdf_network.sdf(x)
+        return torch.sigmoid(-sdf * 80)
+
+    def _variance(self) -> Tensor:
+        return self.deviation_network.variance
+
+    def _center_alpha_fn(self, rays_o_c: Tensor, rays_d_c: Tensor):
+        net = self.sdf_network
+
+        def alpha_fn(t_starts, t_ends, ray_indices):
+            n = t_starts.shape[0]
+            dev = t_starts.device
+            st = stream_handle()
+            ts = t_starts.reshape(-1).contiguous()
+            te = t_ends.reshape(-1).contiguous()
+            diff = torch.empty((n,), dtype=torch.int32, device=dev)
+            call("sn_end_diff", n, None, ts, te, diff, st)
+            end_packed, n_ends = _pack_counts(diff)
+            xyz = torch.empty((2 * n, 3), device=dev)
+            q = torch.empty((1,), dtype=torch.int32, device=dev)
+            call("sn_center_points", n, None, ray_indices.contiguous(), ts, te, rays_o_c, rays_d_c,
+                 end_packed, n_ends, xyz, q, st)
+            sdf = net.sdf_raw(xyz, q)
+            alpha = torch.empty((n, 1), device=dev)
+            var = self._variance().detach().reshape(1).contiguous().float()
+            call("sn_center_alpha", n, None, sdf, 1, end_packed, var, alpha, st)
+            return alpha
+
+        return alpha_fn
+
+    def render(self, rays_o_patch_all, rays_d_patch_all, marching_plane_normal, near, far,
+               V_inverse_patch_all, val_gradient_method="dfd", mode="train"):
+        patch_H, patch_W = rays_o_patch_all.shape[1], rays_o_patch_all.shape[2]
+        num_patch = rays_o_patch_all.shape[0]
+        P = patch_H * patch_W
+        dev = rays_o_patch_all.device
+        ro = rays_o_patch_all.contiguous().float()
+        rd = rays_d_patch_all.contiguous().float()
+        ro_c = ro[:, patch_H // 2, patch_W // 2].contiguous()
+        rd_c = rd[:, patch_H // 2, patch_W // 2].contiguous()
+        gradient_method = self.gradient_method if mode == "train" else val_gradient_method
+        if gradient_method != "dfd":
+            raise NotImplementedError(f"gradient_method {gradient_method!r}: the fused renderer "
+                                      "implements 'dfd' (the shipped configuration)")
+        with torch.no_grad():
+            patch_indices, t_s, t_e = ray_marching(
+                ro_c, rd_c, t_min=near, t_max=far, grid=self.occupancy_grid,
+                render_step_size=self.sampling_step_size, stratified=True, cone_angle=0.0,
+                early_stop_eps=1e-8, alpha_fn=self._center_alpha_fn(ro_c, rd_c))
+        S = patch_indices.shape[0]
+        samples_per_ray = S / num_patch
+        self.last_samples = (patch_indices, t_s, t_e)
+        inv_s = self.deviation_network(torch.zeros([1, 3], device=dev))[:, :1].clip(1e-6, 1e6)
+        if S == 0:
+            z = torch.zeros([num_patch, patch_H, patch_W, 3], device=dev)
+            return {"s_val": 1 / inv_s, "weight_sum": torch.zeros([num_patch, patch_H, patch_W, 1],
+                                                                   device=dev),
+                    "gradients": None, "comp_normal": z, "samples_per_ray": 0.0}
+        st = stream_handle()
+        ts = t_s.reshape(-1).contiguous()
+        te = t_e.reshape(-1).contiguous()
+        with torch.no_grad():
+            diff = torch.empty((S,), dtype=torch.int32, device=dev)
+            call("sn_end_diff", S, None, ts, te, diff, st)
+            end_packed, n_ends = _pack_counts(diff)
+            E = int(n_ends.item())
+            xyz = torch.empty(((S + E) * P, 3), device=dev)
+            tps = torch.empty((S, P), device=dev)
+            tpe = torch.empty((S, P), device=dev)
+            call("sn_patch_points", S, None, patch_H, patch_W, patch_indices, ts, te, ro, rd,
+                 marching_plane_normal.contiguous().float(), end_packed, n_ends, xyz, tps, tpe, None,
+                 st)
+            counts = torch.empty((num_patch,), dtype=torch.int32, device=dev)
+            call("sn_count_indices", S, patch_indices, num_patch, counts, st)
+            packed, _ = _pack_counts(counts)
+        geo = PatchGeometry(patch_H, patch_W, packed, S, end_packed, E, tps, tpe, ro, rd,
+                            V_inverse_patch_all.contiguous().float())
+        sdf = self.sdf_network.sdf(xyz)
+        comp, wsum, grads = _PatchRenderFn.apply(sdf, self._variance(), geo)
+        return {
+            "s_val": 1 / inv_s,
+            "weight_sum": wsum.reshape(num_patch, patch_H, patch_W, 1),
+            "gradients": grads.reshape(S, patch_H, patch_W, 3),
+            "comp_normal": comp.reshape(num_patch, patch_H, patch_W, 3),
+            "samples_per_ray": samples_per_ray,
+        }

@@ -1,0 +1,291 @@
+"""Synthetic multi-view normal-map scenes with analytic SDF ground truth.
+
+Stand-in for the DiLiGenT-MV data SuperNormal trains on (models/dataset_loader.py),
+which is not shipped here: an analytic SDF (sphere, displaced torus, unions of
+spheres / tori / boxes) is sphere-traced from pinhole cameras on a ring to give
+world-space normal maps and masks.  Cameras follow the dataset's conventions
+(OpenCV axes: x right, y down, z forward; pose = camera-to-world), rays are
+``pose[:3,:3] @ normalize(K^-1 [x, y, 1])`` at integer pixel coordinates, the
+marching-plane normal is the camera z axis and V^-1 = inv([d; right; down])
+per pixel (models/dataset_loader.py:112-137, :223-277).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import torch
+from torch import Tensor
+
+__all__ = ["SDFScene", "sphere", "displaced_torus", "box", "union", "CameraRig", "ring_cameras",
+           "SyntheticDataset", "random_scene"]
+
+
+# ---------------------------------------------------------------------------
+# analytic SDFs (torch, any device / dtype)
+# ---------------------------------------------------------------------------
+@dataclass
+class SDFScene:
+    """An analytic signed distance (approximate where displaced) with a
+    Lipschitz bound used to keep sphere tracing conservative."""
+
+    fn: callable
+    lipschitz: float = 1.0
+    name: str = "scene"
+
+    def __call__(self, p: Tensor) -> Tensor:
+        return self.fn(p)
+
+    def normal(self, p: Tensor) -> Tensor:
+        with torch.enable_grad():
+            q = p.detach().requires_grad_(True)
+            d = self.fn(q)
+            (g,) = torch.autograd.grad(d.sum(), q)
+        return torch.nn.functional.normalize(g, dim=-1)
+
+
+def sphere(radius: float = 0.5, center=(0.0, 0.0, 0.0)) -> SDFScene:
+    c = torch.tensor(center)
+
+    def f(p):
+        return torch.linalg.vector_norm(p - c.to(p), dim=-1) - radius
+
+    return SDFScene(f, 1.0, f"sphere(r={radius})")
+
+
+def displaced_torus(R: float = 0.5, r: float = 0.2, amp: float = 0.02, freq: float = 20.0,
+                    center=(0.0, 0.0, 0.0)) -> SDFScene:
+    """Torus around the z axis with a radial displacement amp*sin(f*theta)*sin(f*phi)."""
+    c = torch.tensor(center)
+
+    def f(p):
+        q = p - c.to(p)
+        rxy = torch.sqrt(q[..., 0] ** 2 + q[..., 1] ** 2)
+        ring = rxy - R
+        d = torch.sqrt(ring ** 2 + q[..., 2] ** 2) - r
+        if amp != 0.0:
+            theta = torch.atan2(q[..., 1], q[..., 0])
+            phi = torch.atan2(q[..., 2], ring)
+            d = d - amp * torch.sin(freq * theta) * torch.sin(freq * phi)
+        return d
+
+    lip = 1.0 + abs(amp) * freq * (1.0 / max(R - r, 1e-3) + 1.0 / r)
+    return SDFScene(f, lip, f"torus(R={R},r={r},amp={amp},freq={freq})")
+
+
+def box(half=(0.3, 0.3, 0.3), center=(0.0, 0.0, 0.0)) -> SDFScene:
+    h = torch.tensor(half)
+    c = torch.tensor(center)
+
+    def f(p):
+        q = (p - c.to(p)).abs() - h.to(p)
+        outside = torch.linalg.vector_norm(q.clamp_min(0.0), dim=-1)
+        inside = q.amax(dim=-1).clamp_max(0.0)
+        return outside + inside
+
+    return SDFScene(f, 1.0, f"box({tuple(half)})")
+
+
+def union(*scenes: SDFScene, displacement: float = 0.0, freq: float = 20.0) -> SDFScene:
+    def f(p):
+        d = torch.stack([s(p) for s in scenes], dim=0).amin(dim=0)
+        if displacement:
+            d = d - displacement * torch.sin(freq * p[..., 0]) * torch.sin(freq * p[..., 1]) * \
+                torch.sin(freq * p[..., 2])
+        return d
+
+    lip = max(s.lipschitz for s in scenes) + abs(displacement) * freq * math.sqrt(3.0)
+    return SDFScene(f, lip, "union(" + ",".join(s.name for s in scenes) + ")")
+
+
+def random_scene(seed: int) -> SDFScene:
+    """Seeded union of 1-3 spheres / tori / boxes inside the unit sphere with
+    displacement amplitude in [0.005, 0.03]."""
+    g = torch.Generator().manual_seed(seed)
+    parts = []
+    n = int(torch.randint(1, 4, (1,), generator=g))
+    for _ in range(n):
+        kind = int(torch.randint(0, 3, (1,), generator=g))
+        ctr = ((torch.rand(3, generator=g) - 0.5) * 0.5).tolist()
+        if kind == 0:
+            parts.append(sphere(float(0.15 + 0.2 * torch.rand(1, generator=g)), ctr))
+        elif kind == 1:
+            parts.append(displaced_torus(0.3, 0.1, 0.0, 20.0, ctr))
+        else:
+            parts.append(box(tuple((0.1 + 0.15 * torch.rand(3, generator=g)).tolist()), ctr))
+    amp = float(0.005 + 0.025 * torch.rand(1, generator=g))
+    return union(*parts, displacement=amp)
+
+
+# ---------------------------------------------------------------------------
+# cameras
+# ---------------------------------------------------------------------------
+@dataclass
+class CameraRig:
+    poses: Tensor        # (n, 4, 4) camera-to-world
+    intrinsics: Tensor   # (n, 4, 4)
+    H: int
+    W: int
+
+
+def look_at(eye: Tensor, target: Tensor, up: Tensor) -> Tensor:
+    z = torch.nn.functional.normalize(target - eye, dim=-1)          # forward
+    x = torch.nn.functional.normalize(torch.linalg.cross(z, up), dim=-1)  # right
+    y = torch.linalg.cross(z, x)                                      # down
+    pose = torch.eye(4, dtype=eye.dtype)
+    pose[:3, 0], pose[:3, 1], pose[:3, 2], pose[:3, 3] = x, y, z, eye
+    return pose
+
+
+def ring_cameras(n_views: int, H: int, W: int, radius: float = 3.0, elevation_deg: float = 0.0,
+                 fov_deg: float = 40.0, dtype=torch.float64) -> CameraRig:
+    """n_views pinhole cameras evenly spaced on a ring (axis z) looking at the origin."""
+    poses, Ks = [], []
+    f = 0.5 * W / math.tan(0.5 * math.radians(fov_deg))
+    el = math.radians(elevation_deg)
+    for i in range(n_views):
+        az = 2.0 * math.pi * i / n_views
+        eye = torch.tensor([radius * math.cos(el) * math.cos(az), radius * math.cos(el) * math.sin(az),
+                            radius * math.sin(el)], dtype=dtype)
+        poses.append(look_at(eye, torch.zeros(3, dtype=dtype), torch.tensor([0.0, 0.0, 1.0], dtype=dtype)))
+        K = torch.eye(4, dtype=dtype)
+        K[0, 0] = K[1, 1] = f
+        K[0, 2], K[1, 2] = 0.5 * (W - 1), 0.5 * (H - 1)
+        Ks.append(K)
+    return CameraRig(torch.stack(poses), torch.stack(Ks), H, W)
+
+
+# ---------------------------------------------------------------------------
+# ground truth rendering
+# ---------------------------------------------------------------------------
+def pixel_rays(rig: CameraRig, view: int, px: Tensor, py: Tensor) -> Tensor:
+    """World ray directions at integer pixel coordinates (float64)."""
+    Kinv = torch.inverse(rig.intrinsics[view, :3, :3]).to(px.device)
+    p = torch.stack([px, py, torch.ones_like(px)], dim=-1).to(Kinv.dtype)
+    v = p @ Kinv.T
+    v = v / torch.linalg.vector_norm(v, dim=-1, keepdim=True)
+    return v @ rig.poses[view, :3, :3].to(px.device).T
+
+
+def sphere_trace(scene: SDFScene, o: Tensor, d: Tensor, near: Tensor, far: Tensor,
+                 iters: int = 400, eps: float = 1e-6):
+    t = near.clone()
+    alive = torch.ones_like(t, dtype=torch.bool)
+    hit = torch.zeros_like(alive)
+    for _ in range(iters):
+        p = o + d * t[..., None]
+        s = scene(p)
+        newly = alive & (s.abs() < eps)
+        hit |= newly
+        alive &= ~newly
+        t = torch.where(alive, t + s / scene.lipschitz * 0.9, t)
+        alive &= t < far
+        if not alive.any():
+            break
+    return t, hit
+
+
+@dataclass
+class SyntheticDataset:
+    """Views of an analytic scene with GT normals / masks and per-pixel V^-1,
+    resident on `device`; gen_random_patches mirrors the reference sampler."""
+
+    scene: SDFScene
+    rig: CameraRig
+    device: torch.device
+    normals: Tensor = field(init=False)      # (n, H, W, 3) float32
+    masks: Tensor = field(init=False)        # (n, H, W) float32
+    V_inverse_all: Tensor = field(init=False)  # (n, H, W, 3, 3) float32
+    rays_all: Tensor = field(init=False)     # (n, H, W, 3) float32
+
+    def __post_init__(self):
+        n, H, W = self.rig.poses.shape[0], self.rig.H, self.rig.W
+        dev = self.device
+        ys, xs = torch.meshgrid(torch.arange(H, device=dev, dtype=torch.float64),
+                                torch.arange(W, device=dev, dtype=torch.float64), indexing="ij")
+        normals, masks, vinvs, rays = [], [], [], []
+        for v in range(n):
+            d = pixel_rays(self.rig, v, xs, ys)                         # (H, W, 3)
+            o = self.rig.poses[v, :3, 3].to(dev).expand_as(d)
+            near, far = _near_far(o, d)
+            t, hit = sphere_trace(self.scene, o.reshape(-1, 3), d.reshape(-1, 3), near.reshape(-1),
+                                  far.reshape(-1))
+            pts = o.reshape(-1, 3) + d.reshape(-1, 3) * t[:, None]
+            nrm = self.scene.normal(pts) * hit[:, None]
+            normals.append(nrm.reshape(H, W, 3).float())
+            masks.append(hit.reshape(H, W).float())
+            right = self.rig.poses[v, :3, 0].to(dev).expand_as(d)
+            down = self.rig.poses[v, :3, 1].to(dev).expand_as(d)
+            V = torch.stack([d, right, down], dim=-2)                  # rows: d, right, down
+            vinvs.append(torch.inverse(V).float())
+            rays.append(d.float())
+        self.normals = torch.stack(normals)
+        self.masks = torch.stack(masks)
+        self.V_inverse_all = torch.stack(vinvs)
+        self.rays_all = torch.stack(rays)
+        self.pose_all = self.rig.poses.to(dev).float()
+        self.intrinsics_all = self.rig.intrinsics.to(dev).float()
+        self.n_images, self.H, self.W = n, H, W
+
+    def gen_random_patches(self, num_patch: int, patch_H: int = 3, patch_W: int = 3,
+                           generator: Optional[torch.Generator] = None):
+        """Random patches from random views (models/dataset_loader.py:223-277)."""
+        dev = self.device
+        g = generator
+        cx = torch.randint(patch_W // 2, self.W - 1 - patch_W // 2, (num_patch,), device=dev, generator=g)
+        cy = torch.randint(patch_H // 2, self.H - 1 - patch_H // 2, (num_patch,), device=dev, generator=g)
+        img = torch.randint(0, self.n_images, (num_patch,), device=dev, generator=g)
+        ox = torch.arange(-(patch_W // 2), patch_W // 2 + 1, device=dev)
+        oy = torch.arange(-(patch_H // 2), patch_H // 2 + 1, device=dev)
+        px = cx[:, None, None] + ox[None, None, :].expand(1, patch_H, patch_W)
+        py = cy[:, None, None] + oy[None, :, None].expand(1, patch_H, patch_W)
+        iv = img[:, None, None].expand_as(px)
+        normal = self.normals[iv, py, px]
+        vinv = self.V_inverse_all[iv, py, px]
+        mask = self.masks[iv, py, px].unsqueeze(-1)
+        rays_d = self.rays_all[iv, py, px]
+        rays_o = self.pose_all[img, None, None, :3, 3].expand(rays_d.shape)
+        plane_n = self.pose_all[img, :3, 2]
+        return (rays_o.contiguous(), rays_d.contiguous(), plane_n.contiguous(), vinv.contiguous(),
+                normal.contiguous(), mask.contiguous())
+
+
+def sample_patches(scene: SDFScene, rig: CameraRig, num_patch: int, patch_H: int = 3, patch_W: int = 3,
+                   generator: Optional[torch.Generator] = None, device="cpu"):
+    """gen_random_patches for just the sampled pixels (sphere-traced on demand), so a
+    host-only consumer needs no full-view ground truth.  Same outputs and layout."""
+    g = generator
+    H, W, n = rig.H, rig.W, rig.poses.shape[0]
+    cx = torch.randint(patch_W // 2, W - 1 - patch_W // 2, (num_patch,), generator=g)
+    cy = torch.randint(patch_H // 2, H - 1 - patch_H // 2, (num_patch,), generator=g)
+    img = torch.randint(0, n, (num_patch,), generator=g)
+    ox = torch.arange(-(patch_W // 2), patch_W // 2 + 1)
+    oy = torch.arange(-(patch_H // 2), patch_H // 2 + 1)
+    px = (cx[:, None, None] + ox[None, None, :]).expand(num_patch, patch_H, patch_W).double()
+    py = (cy[:, None, None] + oy[None, :, None]).expand(num_patch, patch_H, patch_W).double()
+    rays = torch.empty((num_patch, patch_H, patch_W, 3), dtype=torch.float64)
+    for v in img.unique().tolist():
+        sel = img == v
+        rays[sel] = pixel_rays(rig, v, px[sel], py[sel])
+    o = rig.poses[img, :3, 3][:, None, None, :].expand_as(rays)
+    near, far = _near_far(o, rays)
+    t, hit = sphere_trace(scene, o.reshape(-1, 3), rays.reshape(-1, 3), near.reshape(-1), far.reshape(-1))
+    pts = o.reshape(-1, 3) + rays.reshape(-1, 3) * t[:, None]
+    normal = (scene.normal(pts) * hit[:, None]).reshape(num_patch, patch_H, patch_W, 3)
+    mask = hit.reshape(num_patch, patch_H, patch_W, 1).double()
+    right = rig.poses[img, :3, 0][:, None, None, :].expand_as(rays)
+    down = rig.poses[img, :3, 1][:, None, None, :].expand_as(rays)
+    vinv = torch.inverse(torch.stack([rays, right, down], dim=-2))
+    plane_n = rig.poses[img, :3, 2]
+    f = lambda a: a.float().contiguous().to(device)
+    return f(o), f(rays), f(plane_n), f(vinv), f(normal), f(mask)
+
+
+def _near_far(o: Tensor, d: Tensor):
+    a = (d * d).sum(-1)
+    b = 2.0 * (o * d).sum(-1)
+    c = (o * o).sum(-1) - 1.0
+    disc = (b * b - 4 * a * c).clamp_min(0.0)
+    mid = -0.5 * b / a
+    return mid - disc.sqrt() / (2 * a), mid + disc.sqrt() / (2 * a)

@@ -1,0 +1,363 @@
+"""Fused SuperNormal training step: one iteration of Runner.train() on device.
+
+Reproduces exp_runner.py:147-210 for the 'dfd' gradient method: occupancy
+update every n steps, centre-ray marching with stratified jitter, SDF-alpha
+culling, patch expansion, one field evaluation for every patch pixel, NeuS
+alpha + patch weights + dfd normals + accumulation + losses + adjoint in one
+kernel, the field backward, weight-norm adjoints, the warm-up/cosine learning
+rate and Adam.  Every size that depends on the data (samples marched,
+samples kept, extra end points, field points) lives in device memory, all
+buffers have fixed capacity, and kernels bound their work by those device
+counts, so a step issues no host synchronisation and can be captured in a
+CUDA graph.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+from typing import Optional
+
+import torch
+from torch import Tensor
+
+from ._lib import SN_STATUS_CAPACITY, SN_STATUS_MARCH_LIMIT, call, stream_handle
+from .fields import SDFNetwork, SingleVarianceNetwork
+
+__all__ = ["TrainConfig", "FusedTrainer"]
+
+
+@dataclass
+class TrainConfig:
+    batch_size: int = 2048
+    patch_h: int = 3
+    patch_w: int = 3
+    step_size: float = 2.0 / 1024.0       # fixed marching step (config: <=1024 samples per chord)
+    start_step_size: Optional[float] = None   # log schedule (exp_runner.py:81-83,149) when set
+    end_step_size: Optional[float] = None
+    end_iter: int = 5000
+    learning_rate: float = 5e-4
+    learning_rate_alpha: float = 0.05
+    warm_up_end: int = 50
+    increase_bandwidth_every: int = 300
+    occ_update_freq: int = 8
+    occ_threshold: float = 0.1
+    occ_ema_decay: float = 0.95
+    occ_warmup_steps: int = 256
+    occ_sigmoid_k: float = 80.0
+    early_stop_eps: float = 1e-8
+    loss_type: str = "l2"
+    normal_weight: float = 1.0
+    eikonal_weight: float = 1.0
+    mask_weight: float = 1.0
+    seed: int = 0
+
+
+def _align4(n: int) -> int:
+    return (n + 3) // 4 * 4
+
+
+class FusedTrainer:
+    """Owns flat parameter / gradient / Adam buffers and fixed-capacity step buffers.
+
+    The network's parameters become views into one flat buffer (their
+    ``.data`` and ``.grad`` are re-pointed), so the modules, their
+    state_dicts and this trainer always agree."""
+
+    def __init__(self, sdf_network: SDFNetwork, deviation_network: SingleVarianceNetwork,
+                 cfg: TrainConfig, occupancy_grid=None, device="cuda"):
+        self.net, self.dev_net, self.cfg = sdf_network, deviation_network, cfg
+        self.device = torch.device(device)
+        if not sdf_network._supported:
+            raise NotImplementedError("FusedTrainer needs the fused-field SDFNetwork shape")
+        if cfg.patch_h < 3 or cfg.patch_w < 3 or cfg.patch_h * cfg.patch_w > 32:
+            raise ValueError("patch must be at least 3x3 and at most 32 pixels")
+        dev = self.device
+        self.P = cfg.patch_h * cfg.patch_w
+        self.B = cfg.batch_size
+        # ---- flat parameters (table first: float2 aligned) ----
+        named = [("table", sdf_network.encoding.params)]
+        for l in (0, 1):
+            lin = getattr(sdf_network, f"lin{l}")
+            named += [(f"v{l}", lin.weight_v), (f"g{l}", lin.weight_g), (f"b{l}", lin.bias)]
+        named.append(("variance", deviation_network.variance))
+        offs, o = {}, 0
+        for name, p in named:
+            offs[name] = (o, p.numel(), tuple(p.shape))
+            o += _align4(p.numel())
+        self.n_params = o
+        self.params = torch.zeros(o, device=dev)
+        self.grads = torch.zeros(o, device=dev)
+        self.exp_avg = torch.zeros(o, device=dev)
+        self.exp_avg_sq = torch.zeros(o, device=dev)
+        self.views, self.gviews = {}, {}
+        with torch.no_grad():
+            for name, p in named:
+                a, n, shape = offs[name]
+                self.params[a:a + n].copy_(p.detach().reshape(-1).to(dev))
+                v = self.params[a:a + n].view(shape)
+                gv = self.grads[a:a + n].view(shape)
+                p.data = v
+                p.grad = gv
+                self.views[name], self.gviews[name] = v, gv
+        self.H = sdf_network.d_hidden
+        self.dout = sdf_network.d_out
+        self.din = sdf_network.lin0.in_features
+        self.w0 = torch.empty((self.H, self.din), device=dev)
+        self.w1 = torch.empty((self.dout, self.H), device=dev)
+        self.n0 = torch.empty((self.H,), device=dev)
+        self.n1 = torch.empty((self.dout,), device=dev)
+        self.dw0 = torch.zeros_like(self.w0)
+        self.dw1 = torch.zeros_like(self.w1)
+        # ---- occupancy grid ----
+        from .nerfacc import OccupancyGrid
+        self.grid = occupancy_grid if occupancy_grid is not None else OccupancyGrid(
+            roi_aabb=[-1.0, -1.0, -1.0, 1.0, 1.0, 1.0], resolution=128).to(dev)
+        self.res = tuple(int(r) for r in self.grid.resolution.tolist())
+        self.n_cells = self.res[0] * self.res[1] * self.res[2]
+        self.occ_cells = torch.empty((2 * (self.n_cells // 4),), dtype=torch.int64, device=dev)
+        self.occ_count = torch.zeros((1,), dtype=torch.int32, device=dev)
+        self.occ_xyz = torch.empty((self.n_cells, 3), device=dev)
+        self.occ_sdf = torch.empty((self.n_cells, 1), device=dev)
+        self.occ_ws = torch.empty(int(call("sn_occ_sample_workspace_bytes", self.n_cells)),
+                                  dtype=torch.uint8, device=dev)
+        self.bin_ws = torch.empty(int(call("sn_occ_binarize_workspace_bytes", self.n_cells)),
+                                  dtype=torch.uint8, device=dev)
+        # ---- device scalars ----
+        self.iter_dev = torch.zeros((1,), dtype=torch.int32, device=dev)
+        self.lr_dev = torch.zeros((1,), device=dev)
+        self.adam_step_dev = torch.zeros((1,), dtype=torch.int32, device=dev)
+        self.status = torch.zeros((1,), dtype=torch.int32, device=dev)
+        self.loss_out = torch.zeros((5,), device=dev)
+        self.mask_sum = torch.zeros((1,), device=dev)
+        self.iter_step = 0
+        self.profile = False        # when True, CUDA events mark the stages of each step
+        self.marks: list = []       # [(tag, torch.cuda.Event)] of the steps run while profiling
+        self.q_hist: list = []      # device copies of the training field-point count per step
+        self._alloc_step_buffers(self._max_step_size_for_capacity())
+
+    def _mark(self, tag: str) -> None:
+        if self.profile:
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record(torch.cuda.current_stream())
+            self.marks.append((tag, ev))
+
+    # ------------------------------------------------------------------
+    def _max_step_size_for_capacity(self) -> float:
+        c = self.cfg
+        if c.start_step_size is not None:
+            return min(c.start_step_size, c.end_step_size or c.start_step_size)
+        return c.step_size
+
+    def _alloc_step_buffers(self, min_step: float) -> None:
+        dev, B, P = self.device, self.B, self.P
+        # a unit-sphere chord is at most 2 long: bound on samples per centre ray
+        self.max_steps = int(math.ceil(2.0 / min_step)) + 3
+        C0 = B * self.max_steps
+        self.C0 = C0
+        i32 = dict(dtype=torch.int32, device=dev)
+        self.near = torch.empty((B,), device=dev)
+        self.far = torch.empty((B,), device=dev)
+        self.ro_c = torch.empty((B, 3), device=dev)
+        self.rd_c = torch.empty((B, 3), device=dev)
+        self.jitter = torch.empty((B,), device=dev)
+        self.counts0 = torch.empty((B,), **i32)
+        self.packed0 = torch.empty((B, 2), **i32)
+        self.total0 = torch.zeros((1,), **i32)
+        self.ridx0 = torch.empty((C0,), dtype=torch.int64, device=dev)
+        self.ts0 = torch.empty((C0,), device=dev)
+        self.te0 = torch.empty((C0,), device=dev)
+        self.diff = torch.empty((C0,), **i32)
+        self.endp = torch.empty((C0, 2), **i32)
+        self.n_ends = torch.zeros((1,), **i32)
+        self.q0 = torch.zeros((1,), **i32)
+        self.xyz0 = torch.empty((2 * C0, 3), device=dev)
+        self.sdf0 = torch.empty((2 * C0, 1), device=dev)
+        self.alpha0 = torch.empty((C0,), device=dev)
+        self.vis = torch.empty((C0,), dtype=torch.uint8, device=dev)
+        self.counts1 = torch.empty((B,), **i32)
+        self.packed1 = torch.empty((B, 2), **i32)
+        self.S = torch.zeros((1,), **i32)
+        self.ridx1 = torch.empty((C0,), dtype=torch.int64, device=dev)
+        self.ts1 = torch.empty((C0,), device=dev)
+        self.te1 = torch.empty((C0,), device=dev)
+        self.endp1 = torch.empty((C0, 2), **i32)
+        self.n_ends1 = torch.zeros((1,), **i32)
+        self.q1 = torch.zeros((1,), **i32)
+        self.xyz1 = torch.empty((2 * C0 * P, 3), device=dev)
+        self.tps = torch.empty((C0, P), device=dev)
+        self.tpe = torch.empty((C0, P), device=dev)
+        self.sdf1 = torch.empty((2 * C0 * P, 1), device=dev)
+        self.d_sdf = torch.empty((2 * C0 * P, 1), device=dev)
+        self.partials = torch.zeros((B, 4), device=dev)
+        self.carry = torch.empty((B, P), device=dev)
+        self.mask_bin = torch.empty((B, P), device=dev)
+        ws_n = max(B, C0)
+        self.scan_ws = torch.empty(int(call("sn_scan_workspace_bytes", ws_n)), dtype=torch.uint8,
+                                   device=dev)
+
+    # ------------------------------------------------------------------
+    def _grid_desc(self):
+        return C.byref(self.net.encoding.desc)
+
+    def _mlp(self):
+        d = self.net._mlp_desc(self.w0, self.views["b0"], self.w1, self.views["b1"])
+        return d
+
+    def step_size(self, it: int) -> float:
+        c = self.cfg
+        if c.start_step_size is None:
+            return c.step_size
+        slop = (math.log10(c.start_step_size) - math.log10(c.end_step_size)) / c.end_iter
+        return 10 ** (math.log10(c.start_step_size) - slop * it)
+
+    @torch.no_grad()
+    def weight_norm_forward(self, st) -> None:
+        v = self.views
+        call("sn_weightnorm_fwd", self.H, self.din, v["v0"], v["g0"], self.w0, self.n0, st)
+        call("sn_weightnorm_fwd", self.dout, self.H, v["v1"], v["g1"], self.w1, self.n1, st)
+
+    @torch.no_grad()
+    def occupancy_update(self, it: int) -> None:
+        """OccupancyGrid.every_n_step body (NA/nerfacc/grid.py:196-239), on device."""
+        c, st = self.cfg, stream_handle()
+        g = self.grid
+        roi = g._roi_aabb.contiguous().float()
+        active = self.net.active_levels()
+        self.weight_norm_forward(st)
+        seed = (c.seed * 1000003 + 17) & 0xFFFFFFFF
+        if it < c.occ_warmup_steps:
+            cells, cap, count = None, self.n_cells, None
+        else:
+            n_u = self.n_cells // 4
+            call("sn_occ_sample_cells", self.n_cells, g._binary.view(torch.uint8), n_u, seed,
+                 self.iter_dev, self.occ_cells, self.occ_count, self.occ_ws, st)
+            cells, cap, count = self.occ_cells, 2 * n_u, self.occ_count
+        call("sn_occ_points_n", cap, count, cells, seed ^ 0x9E37, self.iter_dev, *self.res, roi,
+             g._contraction_type.value, self.occ_xyz, st)
+        call("sn_field_fwd", cap, count, self.occ_xyz, self.views["table"], self._grid_desc(), active,
+             C.byref(self._mlp()), 1, self.occ_sdf, st)
+        call("sn_occ_ema_sdf", cap, count, cells, self.occ_sdf, float(c.occ_sigmoid_k),
+             float(c.occ_ema_decay), g.occs, st)
+        call("sn_occ_binarize", self.n_cells, g.occs, float(c.occ_threshold),
+             g._binary.view(torch.uint8), None, self.bin_ws, st)
+
+    @torch.no_grad()
+    def train_step(self, rays_o: Tensor, rays_d: Tensor, plane_n: Tensor, vinv: Tensor,
+                   normal: Tensor, mask: Tensor) -> Tensor:
+        """One iteration on a batch from gen_random_patches; returns the
+        device loss vector {d/d variance, normal, mask BCE, eikonal, total}."""
+        c, st = self.cfg, stream_handle()
+        it = self.iter_step
+        if c.occ_update_freq > 0 and it % c.occ_update_freq == 0:
+            self.occupancy_update(it)
+        if c.increase_bandwidth_every > 0 and it % c.increase_bandwidth_every == 0:
+            self.net.increase_bandwidth()
+        self.run_step(rays_o, rays_d, plane_n, vinv, normal, mask, self.step_size(it),
+                      self.net.active_levels())
+        self.iter_step += 1
+        return self.loss_out
+
+    @torch.no_grad()
+    def run_step(self, rays_o, rays_d, plane_n, vinv, normal, mask, dt: float, active: int) -> None:
+        """The capturable part of an iteration (fixed dt / bandwidth)."""
+        self.forward_backward(rays_o, rays_d, plane_n, vinv, normal, mask, dt, active)
+        self.optimizer_step()
+
+    @torch.no_grad()
+    def optimizer_step(self) -> None:
+        """Learning-rate schedule and Adam over the flat parameters (zeroes grads)."""
+        c, st = self.cfg, stream_handle()
+        call("sn_lr_schedule", self.iter_dev, self.lr_dev, self.adam_step_dev, float(c.learning_rate),
+             int(c.warm_up_end), int(c.end_iter), float(c.learning_rate_alpha), st)
+        self._mark("adam_begin")
+        call("sn_adam_step", self.n_params, self.params, self.grads, self.exp_avg, self.exp_avg_sq,
+             None, self.lr_dev, self.adam_step_dev, 0.0, 1, 0.9, 0.999, 1e-8, 1, st)
+        self._mark("adam_end")
+
+    @torch.no_grad()
+    def forward_backward(self, rays_o, rays_d, plane_n, vinv, normal, mask, dt: float,
+                         active: int) -> None:
+        """Loss and gradients (accumulated into the flat gradient buffer)."""
+        c, st = self.cfg, stream_handle()
+        B, P, H, W, C0 = self.B, self.P, c.patch_h, c.patch_w, self.C0
+        assert rays_o.shape[0] == B and rays_o.is_contiguous() and rays_d.is_contiguous()
+        v = self.views
+        roi = self.grid._roi_aabb
+        binary = self.grid._binary.view(torch.uint8)
+        rx, ry, rz = self.res
+        ctype = self.grid._contraction_type.value
+        gd = self._grid_desc()
+        kc = (H // 2) * W + W // 2
+        seed = (c.seed * 7919 + 1) & 0xFFFFFFFF
+        self._mark("step_begin")
+        self.weight_norm_forward(st)
+        mlp = C.byref(self._mlp())
+        # --- inputs: mask binarisation, near/far and jitter of the centre rays ---
+        call("sn_mask_prep", B * P, mask, self.mask_bin, self.mask_sum, st)
+        call("sn_near_far_sphere", B, _center_ptr(rays_o, kc), _center_ptr(rays_d, kc), 3 * P,
+             self.near, self.far, self.jitter, seed, self.iter_dev, self.ro_c, self.rd_c, st)
+        # --- marching (count, scan, fill) over the centre rays ---
+        margs = (self.ro_c, self.rd_c, self.near, self.far, self.jitter, roi, binary, rx, ry, rz,
+                 ctype, float(dt), 0.0, 0)
+        call("sn_march_count", B, *margs, self.counts0, self.status, st)
+        call("sn_pack_counts", B, self.counts0, self.packed0, self.total0, self.scan_ws, st)
+        call("sn_march_fill", B, *margs, self.packed0, C0, self.ridx0, self.ts0, self.te0,
+             self.status, st)
+        # --- culling: field at centre samples, NeuS alpha, visibility, compaction ---
+        call("sn_end_diff", C0, self.total0, self.ts0, self.te0, self.diff, st)
+        call("sn_pack_counts", C0, self.diff, self.endp, self.n_ends, self.scan_ws, st)
+        call("sn_center_points", C0, self.total0, self.ridx0, self.ts0, self.te0, self.ro_c,
+             self.rd_c, self.endp, self.n_ends, self.xyz0, self.q0, st)
+        call("sn_field_fwd", 2 * C0, self.q0, self.xyz0, v["table"], gd, active, mlp, 1, self.sdf0, st)
+        call("sn_center_alpha", C0, self.total0, self.sdf0, 1, self.endp, v["variance"], self.alpha0, st)
+        call("sn_visibility_from_alpha", B, self.packed0, self.alpha0, float(c.early_stop_eps), 0.0,
+             self.vis, self.counts1, st)
+        call("sn_pack_counts", B, self.counts1, self.packed1, self.S, self.scan_ws, st)
+        call("sn_compact_samples", B, self.packed0, self.vis, self.packed1, self.ridx0, self.ts0,
+             self.te0, self.ridx1, self.ts1, self.te1, st)
+        # --- training points: expansion through the marching plane ---
+        call("sn_end_diff", C0, self.S, self.ts1, self.te1, self.diff, st)
+        call("sn_pack_counts", C0, self.diff, self.endp1, self.n_ends1, self.scan_ws, st)
+        call("sn_patch_points", C0, self.S, H, W, self.ridx1, self.ts1, self.te1, rays_o, rays_d,
+             plane_n, self.endp1, self.n_ends1, self.xyz1, self.tps, self.tpe, self.q1, st)
+        cap1 = 2 * C0 * P
+        self._mark("field_fwd_begin")
+        call("sn_field_fwd", cap1, self.q1, self.xyz1, v["table"], gd, active, mlp, 1, self.sdf1, st)
+        self._mark("field_fwd_end")
+        if self.profile:
+            self.q_hist.append(self.q1.clone())   # field points of this step (device copy)
+        # --- render + loss + adjoint ---
+        call("sn_patch_render_train", B, H, W, self.packed1, self.S, C0, self.endp1, self.sdf1,
+             self.tps, self.tpe, rays_o, rays_d, vinv, v["variance"], normal, self.mask_bin,
+             self.mask_sum, 1 if c.loss_type == "l1" else 0, float(c.normal_weight),
+             float(c.eikonal_weight), float(c.mask_weight), self.d_sdf, self.partials, self.carry, st)
+        call("sn_patch_carry_fixup", B, P, self.packed1, self.S, C0, self.endp1, self.carry,
+             self.d_sdf, st)
+        call("sn_patch_finalize", B, P, self.partials, self.S, C0, v["variance"], self.mask_sum,
+             float(c.normal_weight), float(c.eikonal_weight), float(c.mask_weight), self.loss_out,
+             self.gviews["variance"], st)
+        # --- field backward and weight-norm adjoints ---
+        g = self.gviews
+        self.dw0.zero_()
+        self.dw1.zero_()
+        self._mark("field_bwd_begin")
+        call("sn_field_bwd", cap1, self.q1, self.xyz1, self.d_sdf, 1, v["table"], gd, active, mlp,
+             g["table"], self.dw0, g["b0"], self.dw1, g["b1"], None, st)
+        self._mark("field_bwd_end")
+        call("sn_weightnorm_bwd", self.H, self.din, v["v0"], v["g0"], self.n0, self.dw0, g["v0"],
+             g["g0"], st)
+        call("sn_weightnorm_bwd", self.dout, self.H, v["v1"], v["g1"], self.n1, self.dw1, g["v1"],
+             g["g1"], st)
+
+    def check_status(self) -> None:
+        v = int(self.status.item())
+        if v & SN_STATUS_MARCH_LIMIT:
+            raise RuntimeError("marching iteration limit hit")
+        if v & SN_STATUS_CAPACITY:
+            raise RuntimeError("sample capacity exceeded")
+
+
+def _center_ptr(t: Tensor, kc: int) -> int:
+    """Address of pixel kc of patch 0 in a (B, H, W, 3) tensor."""
+    return t.data_ptr() + kc * 3 * t.element_size()

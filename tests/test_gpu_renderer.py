@@ -1,0 +1,184 @@
+"""GPU parity of the patch renderer and the fused training step vs the float64 oracle.
+
+The oracle re-runs models/renderer.py's patch math and exp_runner.py's losses
+on the samples our marcher/culling kept (the marcher itself is checked bit
+for bit in test_gpu_nerfacc.py).  Tolerances: rendered normals 2e-4 and
+weight sums 2e-5 absolute, losses 1e-4 relative, parameter gradients 2e-3
+relative to each gradient's max-abs (float32 kernels with atomics vs float64)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import field as OF
+from oracle import renderer as OR
+
+pytestmark = pytest.mark.gpu
+
+ENC = dict(otype="HashGrid", n_levels=16, n_features_per_level=2, log2_hashmap_size=15,
+           base_resolution=16, per_level_scale=1.447)
+
+
+def rel_err(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-30)
+
+
+@pytest.fixture(scope="module")
+def scene(built_lib):
+    from supernormal_gb300 import scenes
+
+    return scenes.SyntheticDataset(scenes.sphere(0.5), scenes.ring_cameras(6, 96, 96, elevation_deg=20),
+                                   torch.device("cuda"))
+
+
+def make(seed=0, d_out=16, table_scale=300.0, variance=0.25):
+    from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
+
+    torch.manual_seed(seed)
+    net = SDFNetwork(3, d_out, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=ENC, input_concat=True)
+    with torch.no_grad():
+        net.encoding.params.mul_(table_scale)
+        net.lin0.weight_v[:, 3:].normal_(0.0, 0.05)
+    net.bindwidth = 16
+    return net.cuda(), SingleVarianceNetwork(variance).cuda()
+
+
+def oracle_field(net):
+    prm = OF.params_from_module(net)
+    geom = OF.geometry_from_module(net)
+    act = net.active_levels()
+    return prm, (lambda x: OF.sdf_network(x, **prm, geom=geom, active_levels=act, out_cols=1))
+
+
+def full_grid():
+    from supernormal_gb300.nerfacc import OccupancyGrid
+
+    g = OccupancyGrid(roi_aabb=[-1.0, -1.0, -1.0, 1.0, 1.0, 1.0], resolution=32).cuda()
+    g._binary = torch.ones_like(g._binary)
+    return g
+
+
+def cpu(t):
+    return t.detach().cpu().numpy()
+
+
+def test_renderer_forward_backward_matches_oracle(scene):
+    from supernormal_gb300.renderer import NeuSRenderer, near_far_from_sphere
+
+    net, var = make()
+    r = NeuSRenderer(net, var)
+    r.occupancy_grid = full_grid()
+    r.sampling_step_size = 1.0 / 96
+    g = torch.Generator(device="cuda").manual_seed(3)
+    ro, rd, pn, vinv, nrm, mask = scene.gen_random_patches(96, generator=g)
+    near, far = near_far_from_sphere(ro[:, 1, 1], rd[:, 1, 1])
+    out = r.render(ro, rd, pn, near, far, vinv)
+    pidx, ts, te = (cpu(t) for t in r.last_samples)
+    assert pidx.size > 200
+    prm, fld = oracle_field(net)
+    var_ref = var.variance.detach().cpu().double().clone().requires_grad_(True)
+    ref = OR.patch_forward(fld, pidx, ts, te, cpu(ro), cpu(rd), cpu(pn), cpu(vinv), var_ref)
+    assert np.abs(cpu(out["comp_normal"]) - cpu(ref["comp_normal"])).max() < 2e-4
+    assert np.abs(cpu(out["weight_sum"]) - cpu(ref["weight_sum"])).max() < 2e-5
+    assert np.abs(cpu(out["gradients"]) - cpu(ref["gradients"])).max() < 2e-3
+    # losses of exp_runner.py through autograd on both sides
+    L = OR.losses(out["comp_normal"].double().cpu(), out["weight_sum"].double().cpu(),
+                  out["gradients"].double().cpu(), cpu(nrm), cpu(mask))
+    Lr = OR.losses(ref["comp_normal"], ref["weight_sum"], ref["gradients"], cpu(nrm), cpu(mask))
+    for k in ("normal", "eikonal", "mask", "total"):
+        assert abs(L[k].item() - Lr[k].item()) <= 1e-4 * max(abs(Lr[k].item()), 1e-6), k
+    Lg = OR.losses(out["comp_normal"], out["weight_sum"], out["gradients"],
+                   torch.as_tensor(cpu(nrm)).cuda(), torch.as_tensor(cpu(mask)).cuda())
+    params = [net.encoding.params, net.lin0.weight_v, net.lin0.weight_g, net.lin0.bias,
+              net.lin1.weight_v, net.lin1.weight_g, net.lin1.bias, var.variance]
+    grads = torch.autograd.grad(Lg["total"], params, allow_unused=True)
+    names = ["table", "v0", "g0", "b0", "v1", "g1", "b1"]
+    rgrads = torch.autograd.grad(Lr["total"], [prm[n] for n in names] + [var_ref], allow_unused=True)
+    for n, a, b in zip(names + ["variance"], grads, rgrads):
+        if b is None:
+            continue
+        assert rel_err(cpu(a), b.numpy()) < 2e-3, n
+
+
+def _trainer(scene, B=128, **kw):
+    from supernormal_gb300.trainer import FusedTrainer, TrainConfig
+
+    net, var = make()
+    cfg = TrainConfig(batch_size=B, step_size=1.0 / 96, occ_update_freq=0, increase_bandwidth_every=0,
+                      **kw)
+    tr = FusedTrainer(net, var, cfg, occupancy_grid=full_grid())
+    return tr, net, var
+
+
+def test_trainer_loss_and_grads_match_oracle(scene):
+    tr, net, var = _trainer(scene)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    ro, rd, pn, vinv, nrm, mask = scene.gen_random_patches(128, generator=g)
+    prm, fld = oracle_field(net)
+    var_ref = var.variance.detach().cpu().double().clone().requires_grad_(True)
+    tr.grads.zero_()
+    tr.forward_backward(ro, rd, pn, vinv, nrm, mask, 1.0 / 96, net.active_levels())
+    torch.cuda.synchronize()
+    tr.check_status()
+    S = int(tr.S.item())
+    assert S > 300
+    # culling parity on the pre-cull samples
+    n0 = int(tr.total0.item())
+    ri0, ts0, te0 = cpu(tr.ridx0[:n0]), cpu(tr.ts0[:n0]), cpu(tr.te0[:n0])
+    vis, _ = OR.cull(fld, cpu(tr.packed0), ri0, ts0, te0, cpu(tr.ro_c), cpu(tr.rd_c), var_ref.detach())
+    gpu_vis = cpu(tr.vis[:n0]).astype(bool)
+    assert (vis != gpu_vis).mean() < 2e-3
+    pidx, ts, te = cpu(tr.ridx1[:S]), cpu(tr.ts1[:S]), cpu(tr.te1[:S])
+    ref = OR.patch_forward(fld, pidx, ts, te, cpu(ro), cpu(rd), cpu(pn), cpu(vinv), var_ref)
+    Lr = OR.losses(ref["comp_normal"], ref["weight_sum"], ref["gradients"], cpu(nrm), cpu(mask))
+    lo = cpu(tr.loss_out)
+    for i, k in ((1, "normal"), (2, "mask"), (3, "eikonal"), (4, "total")):
+        assert abs(lo[i] - Lr[k].item()) <= 1e-4 * max(abs(Lr[k].item()), 1e-6), (k, lo[i], Lr[k].item())
+    names = ["table", "v0", "g0", "b0", "v1", "g1", "b1"]
+    rgrads = torch.autograd.grad(Lr["total"], [prm[n] for n in names] + [var_ref])
+    for n, r in zip(names + ["variance"], rgrads):
+        got = cpu(tr.gviews[n])
+        assert rel_err(got, r.numpy().reshape(got.shape)) < 2e-3, n
+
+
+def test_adam_matches_torch(built_lib):
+    from supernormal_gb300._lib import call, stream_handle
+
+    n = 4099
+    p = torch.randn(n, device="cuda")
+    g = torch.randn(n, device="cuda")
+    pt = p.clone().requires_grad_(True)
+    opt = torch.optim.Adam([pt], lr=1e-3)
+    m = torch.zeros(n, device="cuda")
+    v = torch.zeros(n, device="cuda")
+    buf = torch.zeros(4 * ((n + 3) // 4), device="cuda")
+    mine = buf[:n]
+    mine.copy_(p)
+    mb = torch.zeros_like(buf)
+    vb = torch.zeros_like(buf)
+    gbuf = torch.zeros_like(buf)
+    for step in range(1, 4):
+        gg = g * step
+        pt.grad = gg.clone()
+        opt.step()
+        gbuf[:n] = gg
+        call("sn_adam_step", n, mine, gbuf, mb, vb, None, None, None, 1e-3, step, 0.9, 0.999, 1e-8, 1,
+             stream_handle())
+        assert (gbuf == 0).all()
+    torch.testing.assert_close(mine, pt.detach(), rtol=1e-5, atol=1e-7)
+
+
+def test_training_reduces_loss(scene):
+    tr, net, var = _trainer(scene, B=256, learning_rate=5e-3, warm_up_end=2, end_iter=200)
+    g = torch.Generator(device="cuda").manual_seed(9)
+    first = last = None
+    for it in range(60):
+        batch = scene.gen_random_patches(256, generator=g)
+        loss = tr.train_step(*batch)
+        v = float(loss[4].item())
+        if it < 5:
+            first = v if first is None else min(first, v)
+        last = v
+    tr.check_status()
+    assert np.isfinite(last) and last < first
