@@ -143,9 +143,23 @@ class NeuSRenderer:
                 ro_c, rd_c, t_min=near, t_max=far, grid=self.occupancy_grid,
                 render_step_size=self.sampling_step_size, stratified=True, cone_angle=0.0,
                 early_stop_eps=1e-8, alpha_fn=self._center_alpha_fn(ro_c, rd_c))
+        self.last_samples = (patch_indices, t_s, t_e)
+        return self.render_samples(ro, rd, marching_plane_normal, V_inverse_patch_all, patch_indices,
+                                   t_s, t_e)
+
+    def render_samples(self, rays_o_patch_all, rays_d_patch_all, marching_plane_normal,
+                       V_inverse_patch_all, patch_indices, t_s, t_e):
+        """The part of render() after marching and culling (models/renderer.py:142-276),
+        for given culled centre samples (patch_indices, t_starts, t_ends)."""
+        patch_H, patch_W = rays_o_patch_all.shape[1], rays_o_patch_all.shape[2]
+        num_patch = rays_o_patch_all.shape[0]
+        P = patch_H * patch_W
+        dev = rays_o_patch_all.device
+        ro = rays_o_patch_all.contiguous().float()
+        rd = rays_d_patch_all.contiguous().float()
+        patch_indices = patch_indices.contiguous().long()
         S = patch_indices.shape[0]
         samples_per_ray = S / num_patch
-        self.last_samples = (patch_indices, t_s, t_e)
         inv_s = self.deviation_network(torch.zeros([1, 3], device=dev))[:, :1].clip(1e-6, 1e6)
         if S == 0:
             z = torch.zeros([num_patch, patch_H, patch_W, 3], device=dev)

@@ -1,0 +1,86 @@
+"""CUDA path against the fixtures produced by the reference's own Python code.
+
+Same inputs, parameters and culled samples as tests/golden/*.npz; float32
+kernels vs the reference's float64 run: outputs 2e-5 relative, losses 1e-4
+relative, parameter gradients 2e-3 relative (to each gradient's max-abs)."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+G = Path(__file__).parent / "golden"
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-30)
+
+
+def _net(d, d_out):
+    from supernormal_gb300.fields import SDFNetwork
+
+    L, F, T, base, s = d["enc"]
+    enc = dict(otype="HashGrid", n_levels=int(L), n_features_per_level=int(F), log2_hashmap_size=int(T),
+               base_resolution=int(base), per_level_scale=float(s))
+    net = SDFNetwork(3, d_out, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=enc, input_concat=True)
+    sd = {k[len("param/"):]: torch.from_numpy(d[k]).float() for k in d.files if k.startswith("param/")}
+    net.load_state_dict(sd)
+    net.bindwidth = int(d["bindwidth"])
+    return net.cuda()
+
+
+def test_field_matches_reference_fixture(built_lib):
+    d = np.load(G / "reference_field.npz")
+    net = _net(d, 16)
+    x = torch.from_numpy(d["x"]).float().cuda()
+    y = net(x)
+    assert rel(y.detach().cpu().numpy(), d["y"]) < 2e-5
+    names = [str(n) for n in d["param_names"]]
+    params = dict(net.named_parameters())
+    grads = torch.autograd.grad((y * torch.from_numpy(d["g_out"]).float().cuda()).sum(),
+                                [params[n] for n in names])
+    for n, g in zip(names, grads):
+        assert rel(g.cpu().numpy(), d[f"grad/{n}"]) < 2e-3, n
+
+
+def test_renderer_matches_reference_fixture(built_lib):
+    from oracle import renderer as OR
+    from supernormal_gb300.fields import SingleVarianceNetwork
+    from supernormal_gb300.renderer import NeuSRenderer
+
+    d = np.load(G / "reference_render.npz")
+    net = _net(d, 1)
+    var = SingleVarianceNetwork(float(d["variance"])).cuda()
+    r = NeuSRenderer(net, var)
+    c = lambda k, dt=torch.float32: torch.from_numpy(d[k]).to(dt).cuda()
+    out = r.render_samples(c("rays_o"), c("rays_d"), c("plane_n"), c("vinv"),
+                           c("patch_indices", torch.int64), c("t_starts"), c("t_ends"))
+    assert rel(out["comp_normal"].detach().cpu().numpy(), d["comp_normal"]) < 2e-5
+    assert rel(out["weight_sum"].detach().cpu().numpy(), d["weight_sum"]) < 2e-5
+    assert rel(out["gradients"].detach().cpu().numpy(), d["gradients"]) < 2e-5
+    L = OR.losses(out["comp_normal"], out["weight_sum"], out["gradients"], c("normal"), c("mask"))
+    got = np.array([L["normal"].item(), L["eikonal"].item(), L["mask"].item(), L["total"].item()])
+    assert rel(got, d["losses"]) < 1e-4
+    params = dict(net.named_parameters())
+    params["variance"] = var.variance
+    names = [str(n) for n in d["param_names"]]
+    grads = torch.autograd.grad(L["total"], [params[n] for n in names])
+    for n, g in zip(names, grads):
+        assert rel(g.cpu().numpy(), d[f"grad/{n}"]) < 2e-3, n
+
+
+def test_culling_matches_reference_fixture(built_lib):
+    from supernormal_gb300.fields import SingleVarianceNetwork
+    from supernormal_gb300.renderer import NeuSRenderer
+
+    d = np.load(G / "reference_render.npz")
+    net = _net(d, 1)
+    var = SingleVarianceNetwork(float(d["variance"])).cuda()
+    r = NeuSRenderer(net, var)
+    c = lambda k, dt=torch.float32: torch.from_numpy(np.ascontiguousarray(d[k])).to(dt).cuda()
+    alpha_fn = r._center_alpha_fn(c("rays_o")[:, 1, 1].contiguous(), c("rays_d")[:, 1, 1].contiguous())
+    alpha = alpha_fn(c("pre_t_starts")[:, None], c("pre_t_ends")[:, None],
+                     c("pre_ray_indices", torch.int64)).cpu().numpy().ravel()
+    assert np.abs(alpha - d["cull_alpha"]).max() < 2e-5
