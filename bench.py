@@ -271,9 +271,14 @@ def run_ours(args, world, rank, local):
 
 def stage_times(marks):
     """Sum of event intervals per stage over all profiled steps (ms)."""
-    pairs = {"field_fwd": ("field_fwd_begin", "field_fwd_end"),
+    pairs = {"march": ("step_begin", "march_end"),
+             "cull": ("march_end", "cull_end"),
+             "expand": ("cull_end", "field_fwd_begin"),
+             "field_fwd": ("field_fwd_begin", "field_fwd_end"),
+             "render": ("field_fwd_end", "render_end"),
              "field_bwd": ("field_bwd_begin", "field_bwd_end"),
-             "adam": ("adam_begin", "adam_end")}
+             "adam": ("adam_begin", "adam_end"),
+             "occupancy": ("occ_begin", "occ_end")}
     tot = {k: 0.0 for k in pairs}
     open_ev = {}
     for tag, ev in marks:
@@ -297,7 +302,7 @@ def roofline(stages, q, tr, peaks, peak_kind, K):
         # p, g, m, v read; p, m, v, g(=0) written
         "adam": lambda: float(tr.n_params) * 32 * K,
     }
-    top = max(stages, key=lambda k: stages[k])
+    top = max(bytes_per, key=lambda k: stages[k])   # single-kernel stages only
     achieved = bytes_per[top]() / (stages[top] / 1e3) / 1e9
     peak = float(peaks.get("hbm_gbs", 6800.0))
     traffic = None

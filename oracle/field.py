@@ -76,8 +76,11 @@ def encode(x: torch.Tensor, table: torch.Tensor, geom, n_features=2, active_leve
         if l >= active:
             outs.append(torch.zeros((x.shape[0], n_features), dtype=torch.float64))
             continue
-        cell, _, idx = corner_indices(x32, l, offsets, res, scales)
-        frac = xd * float(scales[l]) + 0.5 - torch.from_numpy(cell.astype(np.float64))
+        cell, frac32, idx = corner_indices(x32, l, offsets, res, scales)
+        # value: the float32 fraction tcnn forms (pos rounded to float32 before
+        # floor/subtract); derivative: d frac / dx = scale
+        xs = xd * float(scales[l])
+        frac = torch.from_numpy(frac32.astype(np.float64)) + (xs - xs.detach())
         feat = table.double().reshape(-1, n_features)[torch.from_numpy(idx)]      # (N, 8, F)
         acc = 0.0
         for k in range(8):

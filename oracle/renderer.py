@@ -60,10 +60,15 @@ def cull(field, packed, ridx, ts, te, rays_o_c, rays_d_c, variance, early_stop_e
     return vis, alpha
 
 
-def patch_forward(field, patch_idx, ts, te, rays_o_all, rays_d_all, plane_n, vinv, variance):
+def patch_forward(field, patch_idx, ts, te, rays_o_all, rays_d_all, plane_n, vinv, variance,
+                  points=None):
     """models/renderer.py:142-267 for gradient_method='dfd' (float64).
 
-    patch_idx/ts/te are the culled centre samples; rays_* are (B, H, W, 3)."""
+    patch_idx/ts/te are the culled centre samples; rays_* are (B, H, W, 3).
+    ``points`` (optional, ((S + E) * H * W, 3) float32) are the field query
+    points as a float32 pipeline formed them (the reference computes them in
+    float32); the field is then evaluated exactly there, so hash-grid cell
+    choices match and only arithmetic precision differs."""
     pidx = torch.as_tensor(np.asarray(patch_idx, np.int64))
     ro = torch.as_tensor(np.asarray(rays_o_all, np.float32)).double()
     rd = torch.as_tensor(np.asarray(rays_d_all, np.float32)).double()
@@ -82,7 +87,9 @@ def patch_forward(field, patch_idx, ts, te, rays_o_all, rays_d_all, plane_n, vin
     ps = ro[pidx] + rd[pidx] * t_s
     pe = ro[pidx] + rd[pidx] * t_e
     pts = torch.cat([ps, pe[diff]], 0)
-    sdf = field(pts.reshape(-1, 3)).reshape(*pts.shape[:-1], 1)
+    q = pts.reshape(-1, 3) if points is None else torch.as_tensor(np.asarray(points, np.float32)).double()
+    assert q.shape[0] == pts.reshape(-1, 3).shape[0], "points do not match the sample layout"
+    sdf = field(q).reshape(*pts.shape[:-1], 1)
     s0 = sdf[:S]
     s1 = torch.cat([s0[1:], s0[-1:]], 0)
     s1 = torch.where(diff[:, None, None, None], torch.zeros_like(s1), s1)

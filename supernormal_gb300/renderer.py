@@ -183,6 +183,7 @@ class NeuSRenderer:
             counts = torch.empty((num_patch,), dtype=torch.int32, device=dev)
             call("sn_count_indices", S, patch_indices, num_patch, counts, st)
             packed, _ = _pack_counts(counts)
+        self.last_points = xyz
         geo = PatchGeometry(patch_H, patch_W, packed, S, end_packed, E, tps, tpe, ro, rd,
                             V_inverse_patch_all.contiguous().float())
         sdf = self.sdf_network.sdf(xyz)

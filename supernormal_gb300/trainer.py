@@ -224,6 +224,7 @@ class FusedTrainer:
         g = self.grid
         roi = g._roi_aabb.contiguous().float()
         active = self.net.active_levels()
+        self._mark("occ_begin")
         self.weight_norm_forward(st)
         seed = (c.seed * 1000003 + 17) & 0xFFFFFFFF
         if it < c.occ_warmup_steps:
@@ -241,6 +242,7 @@ class FusedTrainer:
              float(c.occ_ema_decay), g.occs, st)
         call("sn_occ_binarize", self.n_cells, g.occs, float(c.occ_threshold),
              g._binary.view(torch.uint8), None, self.bin_ws, st)
+        self._mark("occ_end")
 
     @torch.no_grad()
     def train_step(self, rays_o: Tensor, rays_d: Tensor, plane_n: Tensor, vinv: Tensor,
@@ -304,6 +306,7 @@ class FusedTrainer:
         call("sn_pack_counts", B, self.counts0, self.packed0, self.total0, self.scan_ws, st)
         call("sn_march_fill", B, *margs, self.packed0, C0, self.ridx0, self.ts0, self.te0,
              self.status, st)
+        self._mark("march_end")
         # --- culling: field at centre samples, NeuS alpha, visibility, compaction ---
         call("sn_end_diff", C0, self.total0, self.ts0, self.te0, self.diff, st)
         call("sn_pack_counts", C0, self.diff, self.endp, self.n_ends, self.scan_ws, st)
@@ -316,6 +319,7 @@ class FusedTrainer:
         call("sn_pack_counts", B, self.counts1, self.packed1, self.S, self.scan_ws, st)
         call("sn_compact_samples", B, self.packed0, self.vis, self.packed1, self.ridx0, self.ts0,
              self.te0, self.ridx1, self.ts1, self.te1, st)
+        self._mark("cull_end")
         # --- training points: expansion through the marching plane ---
         call("sn_end_diff", C0, self.S, self.ts1, self.te1, self.diff, st)
         call("sn_pack_counts", C0, self.diff, self.endp1, self.n_ends1, self.scan_ws, st)
@@ -337,6 +341,7 @@ class FusedTrainer:
         call("sn_patch_finalize", B, P, self.partials, self.S, C0, v["variance"], self.mask_sum,
              float(c.normal_weight), float(c.eikonal_weight), float(c.mask_weight), self.loss_out,
              self.gviews["variance"], st)
+        self._mark("render_end")
         # --- field backward and weight-norm adjoints ---
         g = self.gviews
         self.dw0.zero_()

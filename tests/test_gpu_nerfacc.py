@@ -100,9 +100,17 @@ def test_patch_weights_vs_oracle(nf, P, n_patches):
     an = a.detach().cpu().numpy().reshape(-1, P)
     w_ref = R.weights_fwd(an, packed, P)
     np.testing.assert_allclose(w.detach().cpu().numpy().reshape(-1, P), w_ref, atol=1e-6)
-    ga_ref = R.weights_bwd(an, w.detach().cpu().numpy().reshape(-1, P), gw.cpu().numpy().reshape(-1, P),
-                           packed, P)
-    np.testing.assert_allclose(ga.cpu().numpy().reshape(-1, P), ga_ref, rtol=1e-4, atol=1e-5)
+    wn = w.detach().cpu().numpy().reshape(-1, P)
+    gn = gw.cpu().numpy().reshape(-1, P)
+    ga_ref = R.weights_bwd(an, wn, gn, packed, P)
+    # The reference adjoint (g*T - sum_{i>=j} g_i w_i) / (1 - alpha) is formed in
+    # float32: its rounding error is ~eps32 * (|g T| + sum |g_i w_i|) / (1 - alpha).
+    scale = np.zeros_like(an)
+    for b, c in packed:
+        if c:
+            scale[b:b + c] = np.abs(gn[b:b + c] * wn[b:b + c]).sum(0)
+    tol = 1e-5 + 1e-4 * np.abs(ga_ref) + 8 * 1.2e-7 * (scale + np.abs(gn)) / np.maximum(1 - an, 1e-10)
+    assert (np.abs(ga.cpu().numpy().reshape(-1, P) - ga_ref) <= tol).all()
 
 
 def test_patch_weights_bit_exact_vs_reference_kernel(nf, ref):

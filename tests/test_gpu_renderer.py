@@ -24,6 +24,18 @@ def rel_err(a, b):
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-30)
 
 
+def l2_rel(a, b):
+    """||a - b|| / ||b||: used for the hash-table gradient, a sum of float32
+    atomics over many points (max-abs would be dominated by reordering noise)."""
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+def grad_err(name, a, b):
+    return l2_rel(a, b) if name == "table" else rel_err(a, b)
+
+
 @pytest.fixture(scope="module")
 def scene(built_lib):
     from supernormal_gb300 import scenes
@@ -78,7 +90,8 @@ def test_renderer_forward_backward_matches_oracle(scene):
     assert pidx.size > 200
     prm, fld = oracle_field(net)
     var_ref = var.variance.detach().cpu().double().clone().requires_grad_(True)
-    ref = OR.patch_forward(fld, pidx, ts, te, cpu(ro), cpu(rd), cpu(pn), cpu(vinv), var_ref)
+    ref = OR.patch_forward(fld, pidx, ts, te, cpu(ro), cpu(rd), cpu(pn), cpu(vinv), var_ref,
+                           points=cpu(r.last_points))
     assert np.abs(cpu(out["comp_normal"]) - cpu(ref["comp_normal"])).max() < 2e-4
     assert np.abs(cpu(out["weight_sum"]) - cpu(ref["weight_sum"])).max() < 2e-5
     assert np.abs(cpu(out["gradients"]) - cpu(ref["gradients"])).max() < 2e-3
@@ -98,7 +111,7 @@ def test_renderer_forward_backward_matches_oracle(scene):
     for n, a, b in zip(names + ["variance"], grads, rgrads):
         if b is None:
             continue
-        assert rel_err(cpu(a), b.numpy()) < 2e-3, n
+        assert grad_err(n, cpu(a), b.numpy()) < 2e-3, n
 
 
 def _trainer(scene, B=128, **kw):
@@ -130,7 +143,9 @@ def test_trainer_loss_and_grads_match_oracle(scene):
     gpu_vis = cpu(tr.vis[:n0]).astype(bool)
     assert (vis != gpu_vis).mean() < 2e-3
     pidx, ts, te = cpu(tr.ridx1[:S]), cpu(tr.ts1[:S]), cpu(tr.te1[:S])
-    ref = OR.patch_forward(fld, pidx, ts, te, cpu(ro), cpu(rd), cpu(pn), cpu(vinv), var_ref)
+    q1 = int(tr.q1.item())
+    ref = OR.patch_forward(fld, pidx, ts, te, cpu(ro), cpu(rd), cpu(pn), cpu(vinv), var_ref,
+                           points=cpu(tr.xyz1[:q1]))
     Lr = OR.losses(ref["comp_normal"], ref["weight_sum"], ref["gradients"], cpu(nrm), cpu(mask))
     lo = cpu(tr.loss_out)
     for i, k in ((1, "normal"), (2, "mask"), (3, "eikonal"), (4, "total")):
@@ -139,7 +154,7 @@ def test_trainer_loss_and_grads_match_oracle(scene):
     rgrads = torch.autograd.grad(Lr["total"], [prm[n] for n in names] + [var_ref])
     for n, r in zip(names + ["variance"], rgrads):
         got = cpu(tr.gviews[n])
-        assert rel_err(got, r.numpy().reshape(got.shape)) < 2e-3, n
+        assert grad_err(n, got, r.numpy().reshape(got.shape)) < 2e-3, n
 
 
 def test_adam_matches_torch(built_lib):
