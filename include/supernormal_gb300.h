@@ -245,6 +245,24 @@ int sn_field_bwd(int64_t n, const int32_t* count, const float* x,
                  const sn_mlp_desc* mlp, float* grad_table, float* grad_w0,
                  float* grad_b0, float* grad_w1, float* grad_b1,
                  float* grad_x, void* stream);
+/* sdf (nullable, n) and grad = d sdf / d x (n, 3) in one pass: replaces
+ * SDFNetwork.gradient's autograd.grad (models/fields.py:107-119). */
+int sn_field_grad_fwd(int64_t n, const int32_t* count, const float* x,
+                      const float* table, const sn_grid_desc* grid,
+                      int active_levels, const sn_mlp_desc* mlp, float* sdf,
+                      float* grad, void* stream);
+/* Hand-written adjoint of (sdf, grad) = field_grad_fwd(x): given
+ * grad_grad = dL/dgrad (n, 3) and grad_sdf = dL/dsdf (nullable, n),
+ * accumulates (+=) the parameter gradients including the second-order terms
+ * through the MLP Jacobian and the trilinear weight derivatives (the double
+ * backward that create_graph=True gives the reference; models/fields.py:113-119).
+ * grad_w1 / grad_b1 receive row 0 / entry 0 (the sdf output). */
+int sn_field_grad_bwd(int64_t n, const int32_t* count, const float* x,
+                      const float* grad_grad, const float* grad_sdf,
+                      const float* table, const sn_grid_desc* grid,
+                      int active_levels, const sn_mlp_desc* mlp,
+                      float* grad_table, float* grad_w0, float* grad_b0,
+                      float* grad_w1, float* grad_b1, void* stream);
 /* torch.nn.utils.weight_norm (dim=0): w = g * v / ||v||_row (models/fields.py:66-67). */
 int sn_weightnorm_fwd(int rows, int cols, const float* v, const float* g,
                       float* w, float* norms, void* stream);
@@ -296,7 +314,10 @@ int sn_patch_points(int64_t cap, const int32_t* count, int patch_h,
  * patch weights (:180), dfd gradients (:187-223) and accumulation of
  * normals and mask (:263-267).  One warp per patch, one lane per pixel.
  * alpha / weights / gradients (nullable) are per sample; comp_normal
- * (n_patches, P, 3) and weight_sum (n_patches, P) per patch pixel. */
+ * (n_patches, P, 3) and weight_sum (n_patches, P) per patch pixel.
+ * ext_gradients (nullable, (S, P, 3)) replaces the dfd gradients by given
+ * ones: the 'ad' method, gradients = SDFNetwork.gradient at the start points
+ * (models/renderer.py:225-226). */
 int sn_patch_render_fwd(int64_t n_patches, int patch_h, int patch_w,
                         const int32_t* packed_info, const int32_t* s_count,
                         int64_t s_cap, const int32_t* end_packed,
@@ -305,11 +326,13 @@ int sn_patch_render_fwd(int64_t n_patches, int patch_h, int patch_w,
                         const float* rays_d, const float* v_inverse,
                         const float* variance, float* alpha, float* weights,
                         float* gradients, float* comp_normal,
-                        float* weight_sum, void* stream);
+                        float* weight_sum, const float* ext_gradients,
+                        void* stream);
 /* Adjoint of sn_patch_render_fwd: d_sdf (field-point layout; every live
  * entry written) and per-patch partials[4p] = d loss / d inv_s.  carry
  * (n_patches, P) receives the end adjoint a patch owes the next sample when
- * that sample starts a later patch; sn_patch_carry_fixup adds it. */
+ * that sample starts a later patch; sn_patch_carry_fixup adds it.  With
+ * ext_gradients, d_gradients (S, P, 3) receives dL / d gradients. */
 int sn_patch_render_bwd(int64_t n_patches, int patch_h, int patch_w,
                         const int32_t* packed_info, const int32_t* s_count,
                         int64_t s_cap, const int32_t* end_packed,
@@ -319,7 +342,9 @@ int sn_patch_render_bwd(int64_t n_patches, int patch_h, int patch_w,
                         const float* variance, const float* grad_comp_normal,
                         const float* grad_weight_sum,
                         const float* grad_gradients, float* d_sdf,
-                        float* partials, float* carry, void* stream);
+                        float* partials, float* carry,
+                        const float* ext_gradients, float* d_gradients,
+                        void* stream);
 /* Training form: forward, the losses of exp_runner.py:191-203 (normal L2 or
  * L1 over sum(mask), eikonal mean, mask BCE) and the adjoint in one pass.
  * partials[4p..4p+3] = d/d inv_s, normal-loss sum, BCE sum, eikonal sum. */
@@ -333,7 +358,8 @@ int sn_patch_render_train(int64_t n_patches, int patch_h, int patch_w,
                           const float* gt_mask, const float* mask_sum,
                           int loss_l1, float w_normal, float w_eikonal,
                           float w_mask, float* d_sdf, float* partials,
-                          float* carry, void* stream);
+                          float* carry, const float* ext_gradients,
+                          float* d_gradients, void* stream);
 /* d_sdf[start after the last sample of patch p] += carry[p] where that
  * sample's end was not evaluated separately (run after the render adjoint). */
 int sn_patch_carry_fixup(int64_t n_patches, int patch_size,
@@ -355,6 +381,9 @@ int sn_near_far_sphere(int64_t n, const float* rays_o, const float* rays_d,
                        int64_t stride, float* near, float* far, float* jitter,
                        uint64_t seed, const int32_t* stream_counter,
                        float* rays_o_out, float* rays_d_out, void* stream);
+/* *out = *in * mul + add on the device (counts derived without a host sync). */
+int sn_scale_count(const int32_t* in, int32_t mul, int32_t add, int32_t* out,
+                   void* stream);
 /* mask_out = (mask_in > 0.5), *mask_sum = sum(mask_out) + 1e-5
  * (exp_runner.py:169-175). */
 int sn_mask_prep(int64_t n, const float* mask_in, float* mask_out,

@@ -61,7 +61,7 @@ def cull(field, packed, ridx, ts, te, rays_o_c, rays_d_c, variance, early_stop_e
 
 
 def patch_forward(field, patch_idx, ts, te, rays_o_all, rays_d_all, plane_n, vinv, variance,
-                  points=None):
+                  points=None, gradient_method="dfd"):
     """models/renderer.py:142-267 for gradient_method='dfd' (float64).
 
     patch_idx/ts/te are the culled centre samples; rays_* are (B, H, W, 3).
@@ -122,6 +122,13 @@ def patch_forward(field, patch_idx, ts, te, rays_o_all, rays_d_all, plane_n, vin
     df_dy = torch.cat([dy_t, df_dy, dy_b], dim=1)
     proj = torch.cat([df_dt, df_dx, df_dy], dim=-1)
     gradients = (vi[pidx] @ proj[..., None])[..., 0]                  # (S, H, W, 3)
+    if gradient_method == "ad":
+        # SDFNetwork.gradient at the start points (models/renderer.py:225-226,
+        # models/fields.py:107-119: autograd with create_graph)
+        xs = q[: S * H * W].detach().clone().requires_grad_(True)
+        s_ad = field(xs)
+        (g_ad,) = torch.autograd.grad(s_ad.sum(), xs, create_graph=True)
+        gradients = g_ad.reshape(S, H, W, 3)
     # accumulation (models/renderer.py:263-267)
     wsum = torch.zeros((B, H * W, 1), dtype=torch.float64).index_add(0, pidx, weights.reshape(S, H * W, 1))
     comp = torch.zeros((B, H * W, 3), dtype=torch.float64).index_add(

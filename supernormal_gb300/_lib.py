@@ -90,6 +90,8 @@ SIGNATURES: dict[str, tuple] = {
     "sn_hashgrid_bwd": (_I, [_I64, _P, _P, _GD, _I, _P, _P]),
     "sn_field_fwd": (_I, [_I64, _P, _P, _P, _GD, _I, _MD, _I, _P, _P]),
     "sn_field_bwd": (_I, [_I64, _P, _P, _P, _I, _P, _GD, _I, _MD, _P, _P, _P, _P, _P, _P, _P]),
+    "sn_field_grad_fwd": (_I, [_I64, _P, _P, _P, _GD, _I, _MD, _P, _P, _P]),
+    "sn_field_grad_bwd": (_I, [_I64, _P, _P, _P, _P, _P, _GD, _I, _MD, _P, _P, _P, _P, _P, _P]),
     "sn_weightnorm_fwd": (_I, [_I, _I, _P, _P, _P, _P, _P]),
     "sn_weightnorm_bwd": (_I, [_I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "sn_end_diff": (_I, [_I64, _P, _P, _P, _P, _P]),
@@ -98,13 +100,14 @@ SIGNATURES: dict[str, tuple] = {
     "sn_compact_samples": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sn_patch_points": (_I, [_I64, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sn_patch_render_fwd": (_I, [_I64, _I, _I, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
-                                 _P, _P, _P, _P]),
-    "sn_patch_render_bwd": (_I, [_I64, _I, _I, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                  _P, _P, _P, _P, _P]),
+    "sn_patch_render_bwd": (_I, [_I64, _I, _I, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                 _P, _P, _P, _P, _P, _P, _P]),
     "sn_patch_render_train": (_I, [_I64, _I, _I, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P,
-                                   _P, _P, _I, _F, _F, _F, _P, _P, _P, _P]),
+                                   _P, _P, _I, _F, _F, _F, _P, _P, _P, _P, _P, _P]),
     "sn_patch_carry_fixup": (_I, [_I64, _I, _P, _P, _I64, _P, _P, _P, _P]),
     "sn_patch_finalize": (_I, [_I64, _I, _P, _P, _I64, _P, _P, _F, _F, _F, _P, _P, _P]),
+    "sn_scale_count": (_I, [_P, C.c_int32, C.c_int32, _P, _P]),
     "sn_mask_prep": (_I, [_I64, _P, _P, _P, _P]),
     "sn_lr_schedule": (_I, [_P, _P, _P, _F, _I, _I, _F, _P]),
     "sn_adam_step": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _F, _I, _F, _F, _F, _I, _P]),

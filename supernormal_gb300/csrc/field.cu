@@ -57,6 +57,7 @@ struct LevelCorners {
   uint32_t idx[8];
   float w[8];
   float frac[3];
+  uint32_t cell[3];  // integer cell coordinates (the 8 indices are a function of these)
 };
 
 __device__ __forceinline__ void level_corners(const GridDev& g, int l, const float x[3],
@@ -68,6 +69,7 @@ __device__ __forceinline__ void level_corners(const GridDev& g, int l, const flo
     const float p = __fmaf_rn(s, x[d], 0.5f);
     const float f = floorf(p);
     cell[d] = (uint32_t)(int)f;
+    c.cell[d] = cell[d];
     c.frac[d] = __fsub_rn(p, f);
   }
   const uint32_t res = g.res[l];
@@ -255,16 +257,22 @@ __global__ void __launch_bounds__(kBwdThreads) field_bwd_kernel(FieldArgs a) {
   const int n_in4 = (3 + 2 * a.active + 3) / 4;
   const int din_used = 3 + 2 * a.active;
   const int t = threadIdx.x;
-  const int own_j = t >> 1, half = t & 1;
-
-  // thread-owned weight-gradient accumulators
-  float acc_w0[(kDinPad + 1) / 2];
-  float acc_w1[kDoutMax / 2];
-  float acc_b0 = 0.0f, acc_b1 = 0.0f;
+  const int lane = t & 31;
+  // register tile of the weight-gradient reduction: rows 4*rg..4*rg+3 of the
+  // hidden layer, input columns cg + 8m (m < 5) and outputs cg + 8m (m < 2)
+  const int rg = t >> 3, cg = t & 7;
+  float acc_w0[4][5];
+  float acc_w1[4][2];
+  float acc_b0[4];
+  float acc_b1 = 0.0f;
 #pragma unroll
-  for (int q = 0; q < (kDinPad + 1) / 2; ++q) acc_w0[q] = 0.0f;
+  for (int r = 0; r < 4; ++r) {
+    acc_b0[r] = 0.0f;
 #pragma unroll
-  for (int q = 0; q < kDoutMax / 2; ++q) acc_w1[q] = 0.0f;
+    for (int m = 0; m < 5; ++m) acc_w0[r][m] = 0.0f;
+#pragma unroll
+    for (int m = 0; m < 2; ++m) acc_w1[r][m] = 0.0f;
+  }
 
   const int64_t stride = (int64_t)gridDim.x * kBwdThreads;
   for (int64_t b0 = (int64_t)blockIdx.x * kBwdThreads; b0 < n; b0 += stride) {
@@ -315,7 +323,11 @@ __global__ void __launch_bounds__(kBwdThreads) field_bwd_kernel(FieldArgs a) {
     for (int o = 0; o < kDoutMax; ++o) s_g[t * kDoutMax + o] = g[o];
 
     // ---- phase 2: table gradient scatter (and optional dL/dx) ----
-    if (live && (a.grad_table || a.grad_x)) {
+    // All 32 lanes of a warp take part (dead lanes carry zero gradient at
+    // x = 0) so a level whose cell is the same for the whole warp -- most
+    // coarse levels, since a warp holds neighbouring pixels of consecutive
+    // samples -- is reduced with shuffles into 8 atomics instead of 256.
+    if (a.grad_table || a.grad_x) {
       const float x[3] = {in[0], in[1], in[2]};
       float dx[3] = {denc[0], denc[1], denc[2]};
       float2* gt2 = reinterpret_cast<float2*>(a.grad_table);
@@ -324,13 +336,29 @@ __global__ void __launch_bounds__(kBwdThreads) field_bwd_kernel(FieldArgs a) {
         if (l < a.active) {
           LevelCorners c;
           level_corners(a.g, l, x, c);
-          const float d0 = denc[3 + 2 * l], d1 = denc[4 + 2 * l];
+          const float d0 = live ? denc[3 + 2 * l] : 0.0f, d1 = live ? denc[4 + 2 * l] : 0.0f;
           if (a.grad_table) {
+            const bool same = (c.cell[0] == __shfl_sync(0xffffffffu, c.cell[0], 0)) &&
+                              (c.cell[1] == __shfl_sync(0xffffffffu, c.cell[1], 0)) &&
+                              (c.cell[2] == __shfl_sync(0xffffffffu, c.cell[2], 0));
+            if (__all_sync(0xffffffffu, same)) {
 #pragma unroll
-            for (int k = 0; k < 8; ++k)
-              atomicAdd(gt2 + c.idx[k], make_float2(c.w[k] * d0, c.w[k] * d1));
+              for (int k = 0; k < 8; ++k) {
+                float v0 = c.w[k] * d0, v1 = c.w[k] * d1;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                  v0 += __shfl_xor_sync(0xffffffffu, v0, o);
+                  v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+                }
+                if (lane == k) atomicAdd(gt2 + c.idx[k], make_float2(v0, v1));
+              }
+            } else if (live) {
+#pragma unroll
+              for (int k = 0; k < 8; ++k)
+                atomicAdd(gt2 + c.idx[k], make_float2(c.w[k] * d0, c.w[k] * d1));
+            }
           }
-          if (a.grad_x) {
+          if (a.grad_x && live) {
             const float2* t2 = reinterpret_cast<const float2*>(a.table);
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
@@ -342,7 +370,7 @@ __global__ void __launch_bounds__(kBwdThreads) field_bwd_kernel(FieldArgs a) {
           }
         }
       }
-      if (a.grad_x) {
+      if (a.grad_x && live) {
         a.grad_x[3 * p] = dx[0];
         a.grad_x[3 * p + 1] = dx[1];
         a.grad_x[3 * p + 2] = dx[2];
@@ -350,44 +378,61 @@ __global__ void __launch_bounds__(kBwdThreads) field_bwd_kernel(FieldArgs a) {
     }
     __syncthreads();
 
-    // ---- phase 3: weight gradients over the batch ----
+    // ---- phase 3: weight gradients over the batch (register-tiled) ----
     const int batch = (int)((n - b0) < kBwdThreads ? (n - b0) : kBwdThreads);
     for (int q = 0; q < batch; ++q) {
-      const float dh = s_dh[q * kH + own_j];
-      const float act = s_act[q * kH + own_j];
+      const float4 dh = reinterpret_cast<const float4*>(s_dh + q * kH)[rg];
+      const float4 ac = reinterpret_cast<const float4*>(s_act + q * kH)[rg];
       const float* iq = s_in + q * kDinPad;
       const float* gq = s_g + q * kDoutMax;
+      const float dhr[4] = {dh.x, dh.y, dh.z, dh.w};
+      const float acr[4] = {ac.x, ac.y, ac.z, ac.w};
 #pragma unroll
-      for (int c = 0; c < (kDinPad + 1) / 2; ++c) {
-        const int i = half + 2 * c;
-        if (i < din_used) acc_w0[c] = fmaf(dh, iq[i], acc_w0[c]);
+      for (int m = 0; m < 5; ++m) {
+        const int i = cg + 8 * m;
+        if (i < din_used) {
+          const float v = iq[i];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) acc_w0[r][m] = fmaf(dhr[r], v, acc_w0[r][m]);
+        }
       }
 #pragma unroll
-      for (int c = 0; c < kDoutMax / 2; ++c) {
-        const int o = half + 2 * c;
-        if (o < a.out_cols) acc_w1[c] = fmaf(gq[o], act, acc_w1[c]);
+      for (int m = 0; m < 2; ++m) {
+        const int o = cg + 8 * m;
+        if (o < a.out_cols) {
+          const float gv = gq[o];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) acc_w1[r][m] = fmaf(gv, acr[r], acc_w1[r][m]);
+        }
       }
-      if (half == 0) acc_b0 += dh;
+      if (cg == 0) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) acc_b0[r] += dhr[r];
+      }
       if (t < a.out_cols) acc_b1 += gq[t];
     }
     __syncthreads();
   }
 
-  // ---- flush ----
-  if (a.grad_w0) {
+  // ---- flush (one atomic per owned entry and block) ----
 #pragma unroll
-    for (int c = 0; c < (kDinPad + 1) / 2; ++c) {
-      const int i = half + 2 * c;
-      if (i < din_used && acc_w0[c] != 0.0f) atomicAdd(a.grad_w0 + own_j * a.din + i, acc_w0[c]);
-    }
-  }
-  if (a.grad_b0 && half == 0 && acc_b0 != 0.0f) atomicAdd(a.grad_b0 + own_j, acc_b0);
-  if (a.grad_w1) {
+  for (int r = 0; r < 4; ++r) {
+    const int j = 4 * rg + r;
+    if (a.grad_w0) {
 #pragma unroll
-    for (int c = 0; c < kDoutMax / 2; ++c) {
-      const int o = half + 2 * c;
-      if (o < a.out_cols && acc_w1[c] != 0.0f) atomicAdd(a.grad_w1 + o * kH + own_j, acc_w1[c]);
+      for (int m = 0; m < 5; ++m) {
+        const int i = cg + 8 * m;
+        if (i < din_used && acc_w0[r][m] != 0.0f) atomicAdd(a.grad_w0 + j * a.din + i, acc_w0[r][m]);
+      }
     }
+    if (a.grad_w1) {
+#pragma unroll
+      for (int m = 0; m < 2; ++m) {
+        const int o = cg + 8 * m;
+        if (o < a.out_cols && acc_w1[r][m] != 0.0f) atomicAdd(a.grad_w1 + o * kH + j, acc_w1[r][m]);
+      }
+    }
+    if (a.grad_b0 && cg == 0 && acc_b0[r] != 0.0f) atomicAdd(a.grad_b0 + j, acc_b0[r]);
   }
   if (a.grad_b1 && t < a.out_cols && acc_b1 != 0.0f) atomicAdd(a.grad_b1 + t, acc_b1);
 }
@@ -395,6 +440,306 @@ __global__ void __launch_bounds__(kBwdThreads) field_bwd_kernel(FieldArgs a) {
 constexpr size_t kFwdSmem = kSmemMlpFloats * sizeof(float);
 constexpr size_t kBwdSmem =
     (kSmemMlpFloats + kBwdThreads * (kDinPad + 2 * kH + kDoutMax)) * sizeof(float);
+
+// ---------------------------------------------------------------------------
+// d sdf / d x (SDFNetwork.gradient, models/fields.py:107-119) and its adjoint
+// ---------------------------------------------------------------------------
+// With in = [x, e(x)], h = W0 in + b0, s = w1 . softplus(h) + b1 (w1 = row 0 of W1):
+//   u = w1 * softplus'(h),  grad = W0x^T u + E^T (W0e^T u),  E = d e / d x,
+// where e_{l,f} = sum_c w_c T_{c,f} and E_{l,f,d} = sum_c T_{c,f} d w_c / d x_d.
+// The adjoint of a loss L(grad, s) with gamma = dL/dgrad, rho = dL/ds:
+//   eta = E gamma,  zeta = [gamma, eta],  mu = W0 zeta,
+//   delta = mu * w1 * softplus''(h) + rho * w1 * softplus'(h)      (= dL/dh)
+//   dW0 += delta in^T + u zeta^T,  db0 += delta,
+//   dw1 += mu * softplus'(h) + rho * softplus(h),  db1 += rho,
+//   dT_{c,f} += (W0e^T delta)_{l,f} w_c + (W0e^T u)_{l,f} (gamma . d w_c / d x).
+__device__ __forceinline__ float softplus_grad2(float x, float beta, float threshold) {
+  const float bx = x * beta;
+  if (bx > threshold) return 0.0f;
+  const float s = 1.0f / (1.0f + expf(-bx));
+  return beta * s * (1.0f - s);
+}
+
+__global__ void __launch_bounds__(128) field_grad_fwd_kernel(FieldArgs a, float* __restrict__ out_sdf,
+                                                             float* __restrict__ out_grad) {
+  extern __shared__ float4 smem4[];
+  float* s_w0 = reinterpret_cast<float*>(smem4);
+  float* s_b0 = s_w0 + kH * kDinPad;
+  float* s_w1 = s_b0 + kH;
+  float* s_b1 = s_w1 + kDoutMax * kH;
+  load_mlp(a, s_w0, s_b0, s_w1, s_b1);
+  __syncthreads();
+  const int64_t n = effective_n(a);
+  const int n_in4 = (3 + 2 * a.active + 3) / 4;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    float in[kDinPad];
+    build_input(a, p, in);
+    float v[kDinPad];  // W0^T u: [0..2] linear part of the gradient, [3..] per-feature weights
+#pragma unroll
+    for (int i = 0; i < kDinPad; ++i) v[i] = 0.0f;
+    float s = s_b1[0];
+#pragma unroll 2
+    for (int j = 0; j < kH; ++j) {
+      const float h = hidden_pre(s_w0, s_b0, j, in, n_in4);
+      const float w1 = s_w1[j];
+      s = fmaf(w1, softplus_fwd(h, a.beta, a.thresh), s);
+      const float u = w1 * softplus_grad(h, a.beta, a.thresh);
+      const float4* wr = reinterpret_cast<const float4*>(s_w0 + j * kDinPad);
+#pragma unroll
+      for (int q = 0; q < kDinPad / 4; ++q) {
+        if (q < n_in4) {
+          const float4 w = wr[q];
+          v[4 * q + 0] = fmaf(w.x, u, v[4 * q + 0]);
+          v[4 * q + 1] = fmaf(w.y, u, v[4 * q + 1]);
+          v[4 * q + 2] = fmaf(w.z, u, v[4 * q + 2]);
+          v[4 * q + 3] = fmaf(w.w, u, v[4 * q + 3]);
+        }
+      }
+    }
+    float gx[3] = {v[0], v[1], v[2]};
+    const float x[3] = {in[0], in[1], in[2]};
+    const float2* t2 = reinterpret_cast<const float2*>(a.table);
+#pragma unroll
+    for (int l = 0; l < kMaxL; ++l) {
+      if (l < a.active) {
+        LevelCorners c;
+        level_corners(a.g, l, x, c);
+        const float v0 = v[3 + 2 * l], v1 = v[4 + 2 * l];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const float2 tv = __ldg(t2 + c.idx[k]);
+          const float gk = v0 * tv.x + v1 * tv.y;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) gx[d] = fmaf(gk, corner_dw(c, k, d, a.g.scale[l]), gx[d]);
+        }
+      }
+    }
+    if (out_sdf) out_sdf[p] = s;
+    out_grad[3 * p + 0] = gx[0];
+    out_grad[3 * p + 1] = gx[1];
+    out_grad[3 * p + 2] = gx[2];
+  }
+}
+
+struct GradBwdArgs {
+  const float* gamma;  // (n, 3) dL / d grad
+  const float* rho;    // (n) dL / d sdf, nullable
+};
+
+__global__ void __launch_bounds__(kBwdThreads) field_grad_bwd_kernel(FieldArgs a, GradBwdArgs b) {
+  extern __shared__ float4 smem4[];
+  float* s_w0 = reinterpret_cast<float*>(smem4);
+  float* s_b0 = s_w0 + kH * kDinPad;
+  float* s_w1 = s_b0 + kH;
+  float* s_b1 = s_w1 + kDoutMax * kH;
+  float* s_in = s_b1 + kDoutMax;                 // [128][kDinPad]
+  float* s_z = s_in + kBwdThreads * kDinPad;     // [128][kDinPad]  zeta = [gamma, eta]
+  float* s_u = s_z + kBwdThreads * kDinPad;      // [128][64]
+  float* s_d = s_u + kBwdThreads * kH;           // [128][64]      delta
+  float* s_dw1 = s_d + kBwdThreads * kH;         // [128][64]
+  float* s_rho = s_dw1 + kBwdThreads * kH;       // [128]
+  load_mlp(a, s_w0, s_b0, s_w1, s_b1);
+  __syncthreads();
+  const int64_t n = effective_n(a);
+  const int n_in4 = (3 + 2 * a.active + 3) / 4;
+  const int din_used = 3 + 2 * a.active;
+  const int t = threadIdx.x, lane = t & 31;
+  const int rg = t >> 3, cg = t & 7;
+  float acc_w0[4][5], acc_b0[4], acc_w1[4];
+  float acc_b1 = 0.0f;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    acc_b0[r] = 0.0f;
+    acc_w1[r] = 0.0f;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) acc_w0[r][m] = 0.0f;
+  }
+  const float2* t2 = reinterpret_cast<const float2*>(a.table);
+  float2* gt2 = reinterpret_cast<float2*>(a.grad_table);
+  const int64_t stride = (int64_t)gridDim.x * kBwdThreads;
+  for (int64_t base = (int64_t)blockIdx.x * kBwdThreads; base < n; base += stride) {
+    const int64_t p = base + t;
+    const bool live = p < n;
+    float in[kDinPad], z[kDinPad];
+#pragma unroll
+    for (int i = 0; i < kDinPad; ++i) {
+      in[i] = 0.0f;
+      z[i] = 0.0f;
+    }
+    float rho = 0.0f;
+    if (live) {
+      in[0] = a.x[3 * p];
+      in[1] = a.x[3 * p + 1];
+      in[2] = a.x[3 * p + 2];
+      z[0] = b.gamma[3 * p];
+      z[1] = b.gamma[3 * p + 1];
+      z[2] = b.gamma[3 * p + 2];
+      rho = b.rho ? b.rho[p] : 0.0f;
+    }
+    // phase 0: encoding e and eta = E gamma
+    {
+      const float x[3] = {in[0], in[1], in[2]};
+#pragma unroll
+      for (int l = 0; l < kMaxL; ++l) {
+        if (l < a.active && live) {
+          LevelCorners c;
+          level_corners(a.g, l, x, c);
+          float e0 = 0.0f, e1 = 0.0f, h0 = 0.0f, h1 = 0.0f;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const float2 tv = __ldg(t2 + c.idx[k]);
+            const float sc = a.g.scale[l];
+            const float wg = z[0] * corner_dw(c, k, 0, sc) + z[1] * corner_dw(c, k, 1, sc) +
+                             z[2] * corner_dw(c, k, 2, sc);
+            e0 = fmaf(c.w[k], tv.x, e0);
+            e1 = fmaf(c.w[k], tv.y, e1);
+            h0 = fmaf(wg, tv.x, h0);
+            h1 = fmaf(wg, tv.y, h1);
+          }
+          in[3 + 2 * l] = e0;
+          in[4 + 2 * l] = e1;
+          z[3 + 2 * l] = h0;
+          z[4 + 2 * l] = h1;
+        }
+      }
+    }
+    // phase 1: hidden layer; delta, u, dw1; de = W0e^T delta, v = W0e^T u
+    float de[2 * kMaxL], vv[2 * kMaxL];
+#pragma unroll
+    for (int k = 0; k < 2 * kMaxL; ++k) {
+      de[k] = 0.0f;
+      vv[k] = 0.0f;
+    }
+#pragma unroll 1
+    for (int j = 0; j < kH; ++j) {
+      const float h = hidden_pre(s_w0, s_b0, j, in, n_in4);
+      const float w1 = s_w1[j];
+      const float g1 = softplus_grad(h, a.beta, a.thresh);
+      const float u = w1 * g1;
+      const float4* wr = reinterpret_cast<const float4*>(s_w0 + j * kDinPad);
+      float mu = 0.0f;
+#pragma unroll
+      for (int q = 0; q < kDinPad / 4; ++q) {
+        if (q < n_in4) {
+          const float4 w = wr[q];
+          mu = fmaf(w.x, z[4 * q], mu);
+          mu = fmaf(w.y, z[4 * q + 1], mu);
+          mu = fmaf(w.z, z[4 * q + 2], mu);
+          mu = fmaf(w.w, z[4 * q + 3], mu);
+        }
+      }
+      const float delta = mu * w1 * softplus_grad2(h, a.beta, a.thresh) + rho * w1 * g1;
+      s_u[t * kH + j] = u;
+      s_d[t * kH + j] = delta;
+      s_dw1[t * kH + j] = mu * g1 + rho * softplus_fwd(h, a.beta, a.thresh);
+#pragma unroll
+      for (int q = 0; q < kDinPad / 4; ++q) {
+        if (q < n_in4) {
+          const float4 w4 = wr[q];
+          const float wc[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int k = 4 * q + e - 3;  // encoding feature of input column 4q+e
+            if (k >= 0 && k < 2 * kMaxL) {
+              de[k] = fmaf(wc[e], delta, de[k]);
+              vv[k] = fmaf(wc[e], u, vv[k]);
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < kDinPad; ++i) {
+      s_in[t * kDinPad + i] = in[i];
+      s_z[t * kDinPad + i] = z[i];
+    }
+    s_rho[t] = rho;
+    // phase 2: table gradient (first- and second-order terms)
+    if (gt2) {
+      const float x[3] = {in[0], in[1], in[2]};
+#pragma unroll
+      for (int l = 0; l < kMaxL; ++l) {
+        if (l < a.active) {
+          LevelCorners c;
+          level_corners(a.g, l, x, c);
+          const float sc = a.g.scale[l];
+          const bool same = (c.cell[0] == __shfl_sync(0xffffffffu, c.cell[0], 0)) &&
+                            (c.cell[1] == __shfl_sync(0xffffffffu, c.cell[1], 0)) &&
+                            (c.cell[2] == __shfl_sync(0xffffffffu, c.cell[2], 0));
+          const bool uni = __all_sync(0xffffffffu, same);
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const float wg = z[0] * corner_dw(c, k, 0, sc) + z[1] * corner_dw(c, k, 1, sc) +
+                             z[2] * corner_dw(c, k, 2, sc);
+            float g0 = live ? de[2 * l] * c.w[k] + vv[2 * l] * wg : 0.0f;
+            float g1 = live ? de[2 * l + 1] * c.w[k] + vv[2 * l + 1] * wg : 0.0f;
+            if (uni) {
+#pragma unroll
+              for (int o = 16; o > 0; o >>= 1) {
+                g0 += __shfl_xor_sync(0xffffffffu, g0, o);
+                g1 += __shfl_xor_sync(0xffffffffu, g1, o);
+              }
+              if (lane == k) atomicAdd(gt2 + c.idx[k], make_float2(g0, g1));
+            } else if (live) {
+              atomicAdd(gt2 + c.idx[k], make_float2(g0, g1));
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // phase 3: weight gradients over the batch
+    const int batch = (int)((n - base) < kBwdThreads ? (n - base) : kBwdThreads);
+    for (int q = 0; q < batch; ++q) {
+      const float4 dq = reinterpret_cast<const float4*>(s_d + q * kH)[rg];
+      const float4 uq = reinterpret_cast<const float4*>(s_u + q * kH)[rg];
+      const float4 wq = reinterpret_cast<const float4*>(s_dw1 + q * kH)[rg];
+      const float dr[4] = {dq.x, dq.y, dq.z, dq.w};
+      const float ur[4] = {uq.x, uq.y, uq.z, uq.w};
+      const float wr1[4] = {wq.x, wq.y, wq.z, wq.w};
+      const float* iq = s_in + q * kDinPad;
+      const float* zq = s_z + q * kDinPad;
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const int i = cg + 8 * m;
+        if (i < din_used) {
+          const float iv = iq[i], zv = zq[i];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) acc_w0[r][m] = fmaf(dr[r], iv, fmaf(ur[r], zv, acc_w0[r][m]));
+        }
+      }
+      if (cg == 0) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          acc_b0[r] += dr[r];
+          acc_w1[r] += wr1[r];
+        }
+      }
+      if (t == 0) acc_b1 += s_rho[q];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int j = 4 * rg + r;
+    if (a.grad_w0) {
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const int i = cg + 8 * m;
+        if (i < din_used && acc_w0[r][m] != 0.0f) atomicAdd(a.grad_w0 + j * a.din + i, acc_w0[r][m]);
+      }
+    }
+    if (cg == 0) {
+      if (a.grad_b0 && acc_b0[r] != 0.0f) atomicAdd(a.grad_b0 + j, acc_b0[r]);
+      if (a.grad_w1 && acc_w1[r] != 0.0f) atomicAdd(a.grad_w1 + j, acc_w1[r]);
+    }
+  }
+  if (a.grad_b1 && t == 0 && acc_b1 != 0.0f) atomicAdd(a.grad_b1, acc_b1);
+}
+
+constexpr size_t kGradBwdSmem =
+    (kSmemMlpFloats + kBwdThreads * (2 * kDinPad + 3 * kH + 1)) * sizeof(float);
 
 // --- standalone encoding (tcnn.Encoding forward / backward) -----------------
 __global__ void hashgrid_fwd_kernel(int64_t n, const float* __restrict__ x,
@@ -636,6 +981,48 @@ int sn_field_bwd(int64_t n, const int32_t* count, const float* x, const float* g
   }
   field_bwd_kernel<<<stride_grid(n, kBwdThreads, 2), kBwdThreads, kBwdSmem, as_stream(stream)>>>(a);
   return check_launch("field_bwd");
+}
+
+int sn_field_grad_fwd(int64_t n, const int32_t* count, const float* x, const float* table,
+                      const sn_grid_desc* grid, int active_levels, const sn_mlp_desc* mlp,
+                      float* sdf, float* grad, void* stream) {
+  FieldArgs a;
+  SN_TRY(fill_field_args(a, n, count, x, table, grid, active_levels, mlp, 1));
+  SN_REQUIRE(grad != nullptr, "field_grad_fwd: grad is null");
+  if (n == 0) return SN_OK;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(field_grad_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kFwdSmem);
+    attr = true;
+  }
+  field_grad_fwd_kernel<<<stride_grid(n, 128, 8), 128, kFwdSmem, as_stream(stream)>>>(a, sdf, grad);
+  return check_launch("field_grad_fwd");
+}
+
+int sn_field_grad_bwd(int64_t n, const int32_t* count, const float* x, const float* grad_grad,
+                      const float* grad_sdf, const float* table, const sn_grid_desc* grid,
+                      int active_levels, const sn_mlp_desc* mlp, float* grad_table, float* grad_w0,
+                      float* grad_b0, float* grad_w1, float* grad_b1, void* stream) {
+  FieldArgs a;
+  SN_TRY(fill_field_args(a, n, count, x, table, grid, active_levels, mlp, 1));
+  SN_REQUIRE(grad_grad != nullptr, "field_grad_bwd: grad_grad is null");
+  a.grad_table = grad_table;
+  a.grad_w0 = grad_w0;
+  a.grad_b0 = grad_b0;
+  a.grad_w1 = grad_w1;
+  a.grad_b1 = grad_b1;
+  if (n == 0) return SN_OK;
+  GradBwdArgs b{grad_grad, grad_sdf};
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(field_grad_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kGradBwdSmem);
+    attr = true;
+  }
+  field_grad_bwd_kernel<<<stride_grid(n, kBwdThreads, 1), kBwdThreads, kGradBwdSmem,
+                          as_stream(stream)>>>(a, b);
+  return check_launch("field_grad_bwd");
 }
 
 int sn_weightnorm_fwd(int rows, int cols, const float* v, const float* g, float* w, float* norms,

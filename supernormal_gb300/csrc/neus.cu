@@ -195,6 +195,10 @@ struct PatchArgs {
   float* d_sdf;             // same layout as sdf; every live entry is written once
   float* partials;          // (n_patches, 4): d_inv_s, normal, bce, eikonal
   float* carry;             // (n_patches, P): end adjoint owed to the next patch's first start
+  // 'ad' gradient method: gradients come from the field (d sdf / dx at the
+  // start points, models/renderer.py:225-226) instead of dfd
+  const float* ext_grads;   // (S, P, 3) nullable
+  float* d_grads;           // (S, P, 3): dL / d gradients when ext_grads is given
 };
 
 struct Lane {
@@ -235,6 +239,13 @@ __device__ __forceinline__ void sample_fwd(const PatchArgs& a, const Lane& L, in
   st.ts = a.tps[i * P + L.k];
   st.te = a.tpe[i * P + L.k];
   st.alpha = neus_alpha(st.s0, st.s1, inv_s, &st.cdf0, &st.cdf1, &st.q);
+  if (a.ext_grads) {
+#pragma unroll
+    for (int e = 0; e < 3; ++e) st.g[e] = a.ext_grads[(i * P + L.k) * 3 + e];
+    st.dt = __fsub_rn(st.te, st.ts);
+    st.dxl = st.dxr = st.dyu = st.dyd = 0.0f;
+    return;
+  }
 
   float pos[3];
 #pragma unroll
@@ -432,6 +443,11 @@ __global__ void __launch_bounds__(128) patch_render_kernel(PatchArgs a) {
 #pragma unroll
       for (int e = 0; e < 3; ++e) dg[e] += a.g_grads[(i * P + L.k) * 3 + e];
     }
+    if (a.ext_grads) {
+      // 'ad': the gradients are field outputs; their adjoint goes to the field
+#pragma unroll
+      for (int e = 0; e < 3; ++e) a.d_grads[(i * P + L.k) * 3 + e] = dg[e];
+    } else {
     float dpj[3];
 #pragma unroll
     for (int b = 0; b < 3; ++b) dpj[b] = L.V[b] * dg[0] + L.V[3 + b] * dg[1] + L.V[6 + b] * dg[2];
@@ -477,6 +493,7 @@ __global__ void __launch_bounds__(128) patch_render_kernel(PatchArgs a) {
     if (L.c < W - 1) ds0 += from_r;
     if (L.r > 0) ds0 += from_u;
     if (L.r < H - 1) ds0 += from_d;
+    }
     ds0 += carry;
     carry = 0.0f;
     // route the end adjoint
@@ -590,6 +607,11 @@ __global__ void near_far_kernel(int64_t n, const float* __restrict__ ro, const f
     far[i] = __fadd_rn(mid, h);
     if (jitter) jitter[i] = uniform01(seed, sid, (uint64_t)i);
   }
+}
+
+__global__ void scale_count_kernel(const int32_t* __restrict__ in, int32_t mul, int32_t add,
+                                   int32_t* __restrict__ out) {
+  *out = *in * mul + add;
 }
 
 // mask := (mask > 0.5) as float, out = sum(mask) + 1e-5 (exp_runner.py:169-175).
@@ -710,11 +732,13 @@ int sn_patch_render_fwd(int64_t n_patches, int patch_h, int patch_w, const int32
                         const float* sdf, const float* t_pix_starts, const float* t_pix_ends,
                         const float* rays_o, const float* rays_d, const float* v_inverse,
                         const float* variance, float* alpha, float* weights, float* gradients,
-                        float* comp_normal, float* weight_sum, void* stream) {
+                        float* comp_normal, float* weight_sum, const float* ext_gradients,
+                        void* stream) {
   PatchArgs a;
   SN_TRY(patch_common(a, n_patches, patch_h, patch_w, packed_info, s_count, s_cap, end_packed, sdf,
                       t_pix_starts, t_pix_ends, rays_o, rays_d, v_inverse, variance));
   SN_REQUIRE(comp_normal && weight_sum, "patch_render_fwd: null output");
+  a.ext_grads = ext_gradients;
   a.alpha = alpha;
   a.weights = weights;
   a.grads = gradients;
@@ -731,12 +755,17 @@ int sn_patch_render_bwd(int64_t n_patches, int patch_h, int patch_w, const int32
                         const float* rays_o, const float* rays_d, const float* v_inverse,
                         const float* variance, const float* grad_comp_normal,
                         const float* grad_weight_sum, const float* grad_gradients, float* d_sdf,
-                        float* partials, float* carry, void* stream) {
+                        float* partials, float* carry, const float* ext_gradients,
+                        float* d_gradients, void* stream) {
   PatchArgs a;
   SN_TRY(patch_common(a, n_patches, patch_h, patch_w, packed_info, s_count, s_cap, end_packed, sdf,
                       t_pix_starts, t_pix_ends, rays_o, rays_d, v_inverse, variance));
   SN_REQUIRE(grad_comp_normal && grad_weight_sum && d_sdf && partials && carry,
              "patch_render_bwd: null buffer");
+  SN_REQUIRE(ext_gradients == nullptr || d_gradients != nullptr,
+             "patch_render_bwd: d_gradients required with ext_gradients");
+  a.ext_grads = ext_gradients;
+  a.d_grads = d_gradients;
   a.carry = carry;
   a.g_comp = grad_comp_normal;
   a.g_wsum = grad_weight_sum;
@@ -755,12 +784,16 @@ int sn_patch_render_train(int64_t n_patches, int patch_h, int patch_w, const int
                           const float* variance, const float* gt_normal, const float* gt_mask,
                           const float* mask_sum, int loss_l1, float w_normal, float w_eikonal,
                           float w_mask, float* d_sdf, float* partials, float* carry,
-                          void* stream) {
+                          const float* ext_gradients, float* d_gradients, void* stream) {
   PatchArgs a;
   SN_TRY(patch_common(a, n_patches, patch_h, patch_w, packed_info, s_count, s_cap, end_packed, sdf,
                       t_pix_starts, t_pix_ends, rays_o, rays_d, v_inverse, variance));
   SN_REQUIRE(gt_normal && gt_mask && mask_sum && d_sdf && partials && carry,
              "patch_render_train: null buffer");
+  SN_REQUIRE(ext_gradients == nullptr || d_gradients != nullptr,
+             "patch_render_train: d_gradients required with ext_gradients");
+  a.ext_grads = ext_gradients;
+  a.d_grads = d_gradients;
   a.carry = carry;
   a.gt_normal = gt_normal;
   a.gt_mask = gt_mask;
@@ -810,6 +843,12 @@ int sn_near_far_sphere(int64_t n, const float* rays_o, const float* rays_d, int6
   near_far_kernel<<<stride_grid(n, 256, 8), 256, 0, as_stream(stream)>>>(
       n, rays_o, rays_d, stride, near, far, jitter, seed, stream_counter, rays_o_out, rays_d_out);
   return check_launch("near_far_sphere");
+}
+
+int sn_scale_count(const int32_t* in, int32_t mul, int32_t add, int32_t* out, void* stream) {
+  SN_REQUIRE(in && out, "scale_count: null buffer");
+  scale_count_kernel<<<1, 1, 0, as_stream(stream)>>>(in, mul, add, out);
+  return check_launch("scale_count");
 }
 
 int sn_mask_prep(int64_t n, const float* mask_in, float* mask_out, float* mask_sum, void* stream) {

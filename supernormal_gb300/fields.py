@@ -194,6 +194,43 @@ class _FieldFn(torch.autograd.Function):
         return g_x, g_table, g_w0, g_b0, g_w1, g_b1, None, None
 
 
+class _FieldGradFn(torch.autograd.Function):
+    """(sdf, d sdf/dx) in one kernel; backward is the hand-written second-order
+    adjoint (the double backward of models/fields.py:107-119 with create_graph)."""
+
+    @staticmethod
+    def forward(ctx, x, table, w0, b0, w1, b1, net: "SDFNetwork"):
+        x = x.contiguous().float()
+        active = net.active_levels()
+        desc = net._mlp_desc(w0, b0, w1, b1)
+        sdf = torch.empty((x.shape[0], 1), device=x.device, dtype=torch.float32)
+        grad = torch.empty((x.shape[0], 3), device=x.device, dtype=torch.float32)
+        call("sn_field_grad_fwd", x.shape[0], None, x, table, C.byref(net.encoding.desc), active,
+             C.byref(desc), sdf, grad, stream_handle())
+        ctx.save_for_backward(x, table, w0, b0, w1, b1)
+        ctx.net, ctx.active = net, active
+        return sdf, grad
+
+    @staticmethod
+    def backward(ctx, g_sdf, g_grad):
+        x, table, w0, b0, w1, b1 = ctx.saved_tensors
+        if ctx.needs_input_grad[0]:
+            raise NotImplementedError("d^2 sdf / dx^2 (the Hessian) is not implemented")
+        need = ctx.needs_input_grad
+        g_table = torch.zeros_like(table) if need[1] else None
+        g_w0 = torch.zeros_like(w0) if need[2] else None
+        g_b0 = torch.zeros_like(b0) if need[3] else None
+        g_w1 = torch.zeros_like(w1) if need[4] else None
+        g_b1 = torch.zeros_like(b1) if need[5] else None
+        g_grad = torch.zeros((x.shape[0], 3), device=x.device) if g_grad is None else g_grad.contiguous().float()
+        g_sdf = None if g_sdf is None else g_sdf.contiguous().float().reshape(-1)
+        desc = ctx.net._mlp_desc(w0, b0, w1, b1)
+        call("sn_field_grad_bwd", x.shape[0], None, x, g_grad, g_sdf, table,
+             C.byref(ctx.net.encoding.desc), ctx.active, C.byref(desc), g_table, g_w0, g_b0, g_w1,
+             g_b1, stream_handle())
+        return None, g_table, g_w0, g_b0, g_w1, g_b1, None
+
+
 class SDFNetwork(nn.Module):
     """SDF MLP over a hash-grid encoding (models/fields.py:7-130)."""
 
@@ -298,14 +335,21 @@ class SDFNetwork(nn.Module):
     def sdf_hidden_appearance(self, x: Tensor) -> Tensor:
         return self.forward(x)
 
+    def sdf_and_gradient(self, x: Tensor):
+        """(sdf (N, 1), d sdf / d x (N, 3)), both differentiable w.r.t. the parameters."""
+        self._check(x)
+        w0, b0, w1, b1 = self.mlp_tensors()
+        return _FieldGradFn.apply(x.detach(), self.encoding.params, w0.contiguous(), b0.contiguous(),
+                                  w1.contiguous(), b1.contiguous(), self)
+
     @torch.enable_grad()
     def gradient(self, x: Tensor) -> Tensor:
-        """d sdf / d x, (N, 1, 3) (models/fields.py:107-119)."""
+        """d sdf / d x, (N, 1, 3) (models/fields.py:107-119).  As with the
+        reference's create_graph=True, the result is differentiable w.r.t. the
+        parameters (second-order adjoint in sn_field_grad_bwd); like the
+        reference, x is marked requires_grad."""
         x.requires_grad_(True)
-        y = self.sdf(x)
-        d_output = torch.ones_like(y, requires_grad=False, device=y.device)
-        g = torch.autograd.grad(outputs=y, inputs=x, grad_outputs=d_output, create_graph=False,
-                                retain_graph=True, only_inputs=True)[0]
+        _, g = self.sdf_and_gradient(x)
         return g.unsqueeze(1)
 
 

@@ -44,25 +44,33 @@ class PatchGeometry:
 
 
 class _PatchRenderFn(torch.autograd.Function):
+    """Fused NeuS alpha + patch weights + gradients + accumulation; ``ext``
+    (optional, (S, P, 3)) gives the gradients ('ad'), else dfd is used."""
+
     @staticmethod
-    def forward(ctx, sdf: Tensor, variance: Tensor, geo: PatchGeometry):
+    def forward(ctx, sdf: Tensor, variance: Tensor, ext, geo: PatchGeometry):
         dev = sdf.device
         B, P, S = geo.n_patches, geo.P, geo.S
+        ctx.sdf_shape = sdf.shape
+        ctx.ext_shape = None if ext is None else ext.shape
         sdf = sdf.contiguous().float().reshape(-1)
         var = variance.detach().reshape(1).contiguous().float()
+        ext = None if ext is None else ext.detach().contiguous().float()
         comp = torch.empty((B, P, 3), device=dev)
         wsum = torch.empty((B, P), device=dev)
-        grads = torch.empty((S, P, 3), device=dev)
+        grads = torch.empty((S, P, 3), device=dev) if ext is None else ext.reshape(S, P, 3).clone()
         call("sn_patch_render_fwd", B, geo.H, geo.W, geo.packed, None, S, geo.end_packed, sdf,
-             geo.t_pix_s, geo.t_pix_e, geo.rays_o, geo.rays_d, geo.vinv, var, None, None, grads,
-             comp, wsum, stream_handle())
-        ctx.save_for_backward(sdf, var)
+             geo.t_pix_s, geo.t_pix_e, geo.rays_o, geo.rays_d, geo.vinv, var, None, None,
+             grads if ext is None else None, comp, wsum, ext, stream_handle())
+        ctx.save_for_backward(sdf, var, ext if ext is not None else torch.empty(0, device=dev))
+        ctx.has_ext = ext is not None
         ctx.geo = geo
         return comp, wsum, grads
 
     @staticmethod
     def backward(ctx, g_comp, g_wsum, g_grads):
-        sdf, var = ctx.saved_tensors
+        sdf, var, ext = ctx.saved_tensors
+        ext = ext if ctx.has_ext else None
         geo = ctx.geo
         dev = sdf.device
         B, P, S = geo.n_patches, geo.P, geo.S
@@ -70,16 +78,19 @@ class _PatchRenderFn(torch.autograd.Function):
         g_wsum = torch.zeros((B, P), device=dev) if g_wsum is None else g_wsum.contiguous().float()
         g_grads = None if g_grads is None else g_grads.contiguous().float()
         d_sdf = torch.empty_like(sdf)
+        d_ext = torch.empty((S, P, 3), device=dev) if ext is not None else None
         partials = torch.zeros((B, 4), device=dev)
         carry = torch.empty((B, P), device=dev)
         st = stream_handle()
         call("sn_patch_render_bwd", B, geo.H, geo.W, geo.packed, None, S, geo.end_packed, sdf,
              geo.t_pix_s, geo.t_pix_e, geo.rays_o, geo.rays_d, geo.vinv, var, g_comp, g_wsum,
-             g_grads, d_sdf, partials, carry, st)
+             g_grads, d_sdf, partials, carry, ext, d_ext, st)
         call("sn_patch_carry_fixup", B, P, geo.packed, None, S, geo.end_packed, carry, d_sdf, st)
         d_var = torch.zeros((1,), device=dev)
         call("sn_patch_finalize", B, P, partials, None, S, var, None, 0.0, 0.0, 0.0, None, d_var, st)
-        return d_sdf, d_var.reshape(()), None
+        if d_ext is not None:
+            d_ext = d_ext.reshape(ctx.ext_shape)
+        return d_sdf.reshape(ctx.sdf_shape), d_var.reshape(()), d_ext, None
 
 
 class NeuSRenderer:
@@ -135,9 +146,9 @@ class NeuSRenderer:
         ro_c = ro[:, patch_H // 2, patch_W // 2].contiguous()
         rd_c = rd[:, patch_H // 2, patch_W // 2].contiguous()
         gradient_method = self.gradient_method if mode == "train" else val_gradient_method
-        if gradient_method != "dfd":
+        if gradient_method not in ("dfd", "ad"):
             raise NotImplementedError(f"gradient_method {gradient_method!r}: the fused renderer "
-                                      "implements 'dfd' (the shipped configuration)")
+                                      "implements 'dfd' (the shipped configuration) and 'ad'")
         with torch.no_grad():
             patch_indices, t_s, t_e = ray_marching(
                 ro_c, rd_c, t_min=near, t_max=far, grid=self.occupancy_grid,
@@ -145,12 +156,14 @@ class NeuSRenderer:
                 early_stop_eps=1e-8, alpha_fn=self._center_alpha_fn(ro_c, rd_c))
         self.last_samples = (patch_indices, t_s, t_e)
         return self.render_samples(ro, rd, marching_plane_normal, V_inverse_patch_all, patch_indices,
-                                   t_s, t_e)
+                                   t_s, t_e, gradient_method)
 
     def render_samples(self, rays_o_patch_all, rays_d_patch_all, marching_plane_normal,
-                       V_inverse_patch_all, patch_indices, t_s, t_e):
+                       V_inverse_patch_all, patch_indices, t_s, t_e, gradient_method="dfd"):
         """The part of render() after marching and culling (models/renderer.py:142-276),
-        for given culled centre samples (patch_indices, t_starts, t_ends)."""
+        for given culled centre samples (patch_indices, t_starts, t_ends).
+        'ad' takes the gradients from SDFNetwork.gradient at the start points
+        (models/renderer.py:225-226) with the second-order adjoint."""
         patch_H, patch_W = rays_o_patch_all.shape[1], rays_o_patch_all.shape[2]
         num_patch = rays_o_patch_all.shape[0]
         P = patch_H * patch_W
@@ -187,7 +200,10 @@ class NeuSRenderer:
         geo = PatchGeometry(patch_H, patch_W, packed, S, end_packed, E, tps, tpe, ro, rd,
                             V_inverse_patch_all.contiguous().float())
         sdf = self.sdf_network.sdf(xyz)
-        comp, wsum, grads = _PatchRenderFn.apply(sdf, self._variance(), geo)
+        ext = None
+        if gradient_method == "ad":
+            _, ext = self.sdf_network.sdf_and_gradient(xyz[: S * P])
+        comp, wsum, grads = _PatchRenderFn.apply(sdf, self._variance(), ext, geo)
         return {
             "s_val": 1 / inv_s,
             "weight_sum": wsum.reshape(num_patch, patch_H, patch_W, 1),

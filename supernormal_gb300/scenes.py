@@ -161,7 +161,7 @@ def ring_cameras(n_views: int, H: int, W: int, radius: float = 3.0, elevation_de
 # ---------------------------------------------------------------------------
 def pixel_rays(rig: CameraRig, view: int, px: Tensor, py: Tensor) -> Tensor:
     """World ray directions at integer pixel coordinates (float64)."""
-    Kinv = torch.inverse(rig.intrinsics[view, :3, :3]).to(px.device)
+    Kinv = inv3x3(rig.intrinsics[view, :3, :3]).to(px.device)
     p = torch.stack([px, py, torch.ones_like(px)], dim=-1).to(Kinv.dtype)
     v = p @ Kinv.T
     v = v / torch.linalg.vector_norm(v, dim=-1, keepdim=True)
@@ -218,7 +218,7 @@ class SyntheticDataset:
             right = self.rig.poses[v, :3, 0].to(dev).expand_as(d)
             down = self.rig.poses[v, :3, 1].to(dev).expand_as(d)
             V = torch.stack([d, right, down], dim=-2)                  # rows: d, right, down
-            vinvs.append(torch.inverse(V).float())
+            vinvs.append(inv3x3(V).float())
             rays.append(d.float())
         self.normals = torch.stack(normals)
         self.masks = torch.stack(masks)
@@ -276,10 +276,21 @@ def sample_patches(scene: SDFScene, rig: CameraRig, num_patch: int, patch_H: int
     mask = hit.reshape(num_patch, patch_H, patch_W, 1).double()
     right = rig.poses[img, :3, 0][:, None, None, :].expand_as(rays)
     down = rig.poses[img, :3, 1][:, None, None, :].expand_as(rays)
-    vinv = torch.inverse(torch.stack([rays, right, down], dim=-2))
+    vinv = inv3x3(torch.stack([rays, right, down], dim=-2))
     plane_n = rig.poses[img, :3, 2]
     f = lambda a: a.float().contiguous().to(device)
     return f(o), f(rays), f(plane_n), f(vinv), f(normal), f(mask)
+
+
+def inv3x3(M: Tensor) -> Tensor:
+    """Inverse of (..., 3, 3) matrices by the adjugate (rows r0, r1, r2:
+    inverse columns are r1 x r2, r2 x r0, r0 x r1 over the determinant)."""
+    r0, r1, r2 = M[..., 0, :], M[..., 1, :], M[..., 2, :]
+    c0 = torch.linalg.cross(r1, r2)
+    c1 = torch.linalg.cross(r2, r0)
+    c2 = torch.linalg.cross(r0, r1)
+    det = (r0 * c0).sum(-1, keepdim=True)
+    return torch.stack([c0 / det, c1 / det, c2 / det], dim=-1)
 
 
 def _near_far(o: Tensor, d: Tensor):

@@ -47,6 +47,7 @@ class TrainConfig:
     occ_sigmoid_k: float = 80.0
     early_stop_eps: float = 1e-8
     loss_type: str = "l2"
+    gradient_method: str = "dfd"            # 'dfd' (shipped) or 'ad' (second-order adjoint)
     normal_weight: float = 1.0
     eikonal_weight: float = 1.0
     mask_weight: float = 1.0
@@ -191,6 +192,10 @@ class FusedTrainer:
         self.d_sdf = torch.empty((2 * C0 * P, 1), device=dev)
         self.partials = torch.zeros((B, 4), device=dev)
         self.carry = torch.empty((B, P), device=dev)
+        if self.cfg.gradient_method == "ad":
+            self.sp_count = torch.zeros((1,), **i32)
+            self.ext_g = torch.empty((C0 * P, 3), device=dev)
+            self.d_ext = torch.empty((C0 * P, 3), device=dev)
         self.mask_bin = torch.empty((B, P), device=dev)
         ws_n = max(B, C0)
         self.scan_ws = torch.empty(int(call("sn_scan_workspace_bytes", ws_n)), dtype=torch.uint8,
@@ -331,11 +336,17 @@ class FusedTrainer:
         self._mark("field_fwd_end")
         if self.profile:
             self.q_hist.append(self.q1.clone())   # field points of this step (device copy)
+        ad = c.gradient_method == "ad"
+        if ad:  # gradients = d sdf / dx at the start points (models/renderer.py:225-226)
+            call("sn_scale_count", self.S, P, 0, self.sp_count, st)
+            call("sn_field_grad_fwd", C0 * P, self.sp_count, self.xyz1, v["table"], gd, active, mlp,
+                 None, self.ext_g, st)
         # --- render + loss + adjoint ---
         call("sn_patch_render_train", B, H, W, self.packed1, self.S, C0, self.endp1, self.sdf1,
              self.tps, self.tpe, rays_o, rays_d, vinv, v["variance"], normal, self.mask_bin,
              self.mask_sum, 1 if c.loss_type == "l1" else 0, float(c.normal_weight),
-             float(c.eikonal_weight), float(c.mask_weight), self.d_sdf, self.partials, self.carry, st)
+             float(c.eikonal_weight), float(c.mask_weight), self.d_sdf, self.partials, self.carry,
+             self.ext_g if ad else None, self.d_ext if ad else None, st)
         call("sn_patch_carry_fixup", B, P, self.packed1, self.S, C0, self.endp1, self.carry,
              self.d_sdf, st)
         call("sn_patch_finalize", B, P, self.partials, self.S, C0, v["variance"], self.mask_sum,
@@ -349,6 +360,9 @@ class FusedTrainer:
         self._mark("field_bwd_begin")
         call("sn_field_bwd", cap1, self.q1, self.xyz1, self.d_sdf, 1, v["table"], gd, active, mlp,
              g["table"], self.dw0, g["b0"], self.dw1, g["b1"], None, st)
+        if ad:  # second-order adjoint of the gradients
+            call("sn_field_grad_bwd", C0 * P, self.sp_count, self.xyz1, self.d_ext, None, v["table"],
+                 gd, active, mlp, g["table"], self.dw0, g["b0"], self.dw1, g["b1"], st)
         self._mark("field_bwd_end")
         call("sn_weightnorm_bwd", self.H, self.din, v["v0"], v["g0"], self.n0, self.dw0, g["v0"],
              g["g0"], st)

@@ -87,6 +87,119 @@ def test_field_backward_matches_oracle(built_lib, enc, d_out, active, cols):
         assert rel_err(g.cpu().numpy(), r.numpy()) < 1e-3, n
 
 
+@pytest.mark.parametrize("enc,active", [(ENC1, 16), (ENC_SHIPPED, 9)])
+def test_gradient_and_second_order_adjoint_match_oracle(built_lib, enc, active):
+    net = make_net(enc, d_out=16, table_scale=1e3)
+    net.bindwidth = active
+    x = torch.rand((1500, 3), device="cuda") * 2 - 1
+    sdf, grad = net.sdf_and_gradient(x)
+    prm = OF.params_from_module(net)
+    xr = x.cpu().double().requires_grad_(True)
+    s_ref = OF.sdf_network(xr, **prm, geom=OF.geometry_from_module(net), active_levels=active, out_cols=1)
+    (g_ref,) = torch.autograd.grad(s_ref.sum(), xr, create_graph=True)
+    np.testing.assert_allclose(sdf.detach().cpu().numpy(), s_ref.detach().numpy(), atol=2e-5)
+    assert rel_err(grad.detach().cpu().numpy(), g_ref.detach().numpy()) < 1e-4
+    gg = torch.randn_like(grad)
+    gs = torch.randn_like(sdf)
+    params = [net.encoding.params, net.lin0.weight_v, net.lin0.weight_g, net.lin0.bias,
+              net.lin1.weight_v, net.lin1.weight_g, net.lin1.bias]
+    grads = torch.autograd.grad((grad * gg).sum() + (sdf * gs).sum(), params, allow_unused=True)
+    names = ["table", "v0", "g0", "b0", "v1", "g1", "b1"]
+    obj = (g_ref * gg.cpu().double()).sum() + (s_ref * gs.cpu().double()).sum()
+    rgrads = torch.autograd.grad(obj, [prm[n] for n in names], allow_unused=True)
+    for n, g, r in zip(names, grads, rgrads):
+        g = np.zeros(prm[n].shape) if g is None else g.cpu().numpy()
+        r = np.zeros(prm[n].shape) if r is None else r.numpy()
+        err = (np.linalg.norm(g - r) / max(np.linalg.norm(r), 1e-30)) if n == "table" else rel_err(g, r)
+        assert err < 2e-3, (n, err)
+
+
+def test_second_order_adjoint_vs_central_differences(built_lib):
+    """Config-4 style check: d/dtheta of L = <gamma, grad_x sdf> against float64
+    central differences (h = 1e-4) of the oracle on 512 random parameters."""
+    enc = dict(ENC1, log2_hashmap_size=17)
+    net = make_net(enc, d_out=16, table_scale=1e3)
+    net.bindwidth = 16
+    x = torch.rand((64 * 9, 3), device="cuda") * 2 - 1
+    gamma = torch.randn((x.shape[0], 3), device="cuda")
+    _, grad = net.sdf_and_gradient(x)
+    names = ["table", "v0", "g0", "b0", "v1", "g1", "b1"]
+    params = [net.encoding.params, net.lin0.weight_v, net.lin0.weight_g, net.lin0.bias,
+              net.lin1.weight_v, net.lin1.weight_g, net.lin1.bias]
+    grads = torch.autograd.grad((grad * gamma).sum(), params, allow_unused=True)
+    prm = {k: v.detach() for k, v in OF.params_from_module(net).items()}
+    geom = OF.geometry_from_module(net)
+    xr = x.cpu().double()
+    gam = gamma.cpu().double()
+
+    def objective(p):
+        xx = xr.clone().requires_grad_(True)
+        s = OF.sdf_network(xx, **p, geom=geom, active_levels=16, out_cols=1)
+        (gx,) = torch.autograd.grad(s.sum(), xx)
+        return float((gx * gam).sum())
+
+    rng = np.random.default_rng(0)
+    # parameters that matter: table entries touched by the points + all MLP weights
+    touched = np.unique(np.concatenate([OF.corner_indices(x.cpu().numpy(), l, *geom)[2].ravel()
+                                        for l in range(16)]))
+    picks = []
+    for _ in range(512):
+        n = names[rng.integers(0, 6)] if rng.random() < 0.5 else "table"
+        if n == "table":
+            e = int(rng.choice(touched))
+            picks.append((n, 2 * e + int(rng.integers(0, 2))))
+        else:
+            picks.append((n, int(rng.integers(0, prm[n].numel()))))
+    h = 1e-4
+    errs = []
+    for n, i in picks:
+        p_plus = dict(prm)
+        p_minus = dict(prm)
+        t = prm[n].clone().reshape(-1)
+        t[i] += h
+        p_plus[n] = t.reshape(prm[n].shape)
+        t2 = prm[n].clone().reshape(-1)
+        t2[i] -= h
+        p_minus[n] = t2.reshape(prm[n].shape)
+        fd = (objective(p_plus) - objective(p_minus)) / (2 * h)
+        g = grads[names.index(n)]
+        got = 0.0 if g is None else float(g.reshape(-1)[i])
+        errs.append((abs(got - fd), abs(fd)))
+    errs = np.array(errs)
+    scale = max(errs[:, 1].max(), 1e-12)
+    assert (errs[:, 0] <= 2e-3 * scale + 1e-3 * errs[:, 1]).all(), errs[:, 0].max() / scale
+
+
+def test_gradient_matches_reference_fixture(built_lib):
+    from pathlib import Path
+
+    d = np.load(Path(__file__).parent / "golden" / "reference_field.npz")
+    from supernormal_gb300.fields import SDFNetwork
+
+    L, F, T, base, s = d["enc"]
+    enc = dict(otype="HashGrid", n_levels=int(L), n_features_per_level=int(F),
+               log2_hashmap_size=int(T), base_resolution=int(base), per_level_scale=float(s))
+    net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=enc, input_concat=True)
+    net.load_state_dict({k[6:]: torch.from_numpy(d[k]).float() for k in d.files if k.startswith("param/")})
+    net.bindwidth = int(d["bindwidth"])
+    net = net.cuda()
+    x = torch.from_numpy(d["x"]).float().cuda()
+    g = net.gradient(x)
+    assert rel_err(g.detach().cpu().numpy(), d["gradient"]) < 1e-4
+    names = [str(n) for n in d["param_names"]]
+    params = dict(net.named_parameters())
+    grads = torch.autograd.grad((g * torch.from_numpy(d["g_grad"]).float().cuda()).sum(),
+                                [params[n] for n in names], allow_unused=True)
+    for n, gr in zip(names, grads):
+        ref = d[f"grad2/{n}"]
+        got = np.zeros_like(ref) if gr is None else gr.cpu().numpy()
+        if np.abs(ref).max() == 0:
+            assert np.abs(got).max() == 0, n
+            continue
+        err = (np.linalg.norm(got - ref) / np.linalg.norm(ref)) if n == "encoding.params" else rel_err(got, ref)
+        assert err < 2e-3, (n, err)
+
+
 def test_weightnorm_matches_torch(built_lib):
     from supernormal_gb300.fields import _WeightNorm
 

@@ -1,8 +1,10 @@
 """CUDA path against the fixtures produced by the reference's own Python code.
 
 Same inputs, parameters and culled samples as tests/golden/*.npz; float32
-kernels vs the reference's float64 run: outputs 2e-5 relative, losses 1e-4
-relative, parameter gradients 2e-3 relative (to each gradient's max-abs)."""
+kernels vs the reference's float64 run: field outputs, rendered normals and
+mask 2e-5 relative, dfd gradients 2e-4 relative, culling alpha 1e-4 absolute,
+losses 1e-4 relative, parameter gradients 2e-3 relative (to each gradient's
+max-abs)."""
 from pathlib import Path
 
 import numpy as np
@@ -59,7 +61,9 @@ def test_renderer_matches_reference_fixture(built_lib):
                            c("patch_indices", torch.int64), c("t_starts"), c("t_ends"))
     assert rel(out["comp_normal"].detach().cpu().numpy(), d["comp_normal"]) < 2e-5
     assert rel(out["weight_sum"].detach().cpu().numpy(), d["weight_sum"]) < 2e-5
-    assert rel(out["gradients"].detach().cpu().numpy(), d["gradients"]) < 2e-5
+    # dfd gradients are sdf differences over ~1e-2 distances: float32 rounding of
+    # the sdf (~1e-7) is amplified ~100x
+    assert rel(out["gradients"].detach().cpu().numpy(), d["gradients"]) < 2e-4
     L = OR.losses(out["comp_normal"], out["weight_sum"], out["gradients"], c("normal"), c("mask"))
     got = np.array([L["normal"].item(), L["eikonal"].item(), L["mask"].item(), L["total"].item()])
     assert rel(got, d["losses"]) < 1e-4
@@ -83,4 +87,5 @@ def test_culling_matches_reference_fixture(built_lib):
     alpha_fn = r._center_alpha_fn(c("rays_o")[:, 1, 1].contiguous(), c("rays_d")[:, 1, 1].contiguous())
     alpha = alpha_fn(c("pre_t_starts")[:, None], c("pre_t_ends")[:, None],
                      c("pre_ray_indices", torch.int64)).cpu().numpy().ravel()
-    assert np.abs(alpha - d["cull_alpha"]).max() < 2e-5
+    # sigmoid(sdf * inv_s) with inv_s = e^6 ~ 403 scales the float32 sdf error
+    assert np.abs(alpha - d["cull_alpha"]).max() < 1e-4

@@ -75,11 +75,12 @@ def cpu(t):
     return t.detach().cpu().numpy()
 
 
-def test_renderer_forward_backward_matches_oracle(scene):
+@pytest.mark.parametrize("method", ["dfd", "ad"])
+def test_renderer_forward_backward_matches_oracle(scene, method):
     from supernormal_gb300.renderer import NeuSRenderer, near_far_from_sphere
 
     net, var = make()
-    r = NeuSRenderer(net, var)
+    r = NeuSRenderer(net, var, gradient_method=method)
     r.occupancy_grid = full_grid()
     r.sampling_step_size = 1.0 / 96
     g = torch.Generator(device="cuda").manual_seed(3)
@@ -91,7 +92,7 @@ def test_renderer_forward_backward_matches_oracle(scene):
     prm, fld = oracle_field(net)
     var_ref = var.variance.detach().cpu().double().clone().requires_grad_(True)
     ref = OR.patch_forward(fld, pidx, ts, te, cpu(ro), cpu(rd), cpu(pn), cpu(vinv), var_ref,
-                           points=cpu(r.last_points))
+                           points=cpu(r.last_points), gradient_method=method)
     assert np.abs(cpu(out["comp_normal"]) - cpu(ref["comp_normal"])).max() < 2e-4
     assert np.abs(cpu(out["weight_sum"]) - cpu(ref["weight_sum"])).max() < 2e-5
     assert np.abs(cpu(out["gradients"]) - cpu(ref["gradients"])).max() < 2e-3
@@ -124,8 +125,9 @@ def _trainer(scene, B=128, **kw):
     return tr, net, var
 
 
-def test_trainer_loss_and_grads_match_oracle(scene):
-    tr, net, var = _trainer(scene)
+@pytest.mark.parametrize("method", ["dfd", "ad"])
+def test_trainer_loss_and_grads_match_oracle(scene, method):
+    tr, net, var = _trainer(scene, gradient_method=method)
     g = torch.Generator(device="cuda").manual_seed(5)
     ro, rd, pn, vinv, nrm, mask = scene.gen_random_patches(128, generator=g)
     prm, fld = oracle_field(net)
@@ -145,7 +147,7 @@ def test_trainer_loss_and_grads_match_oracle(scene):
     pidx, ts, te = cpu(tr.ridx1[:S]), cpu(tr.ts1[:S]), cpu(tr.te1[:S])
     q1 = int(tr.q1.item())
     ref = OR.patch_forward(fld, pidx, ts, te, cpu(ro), cpu(rd), cpu(pn), cpu(vinv), var_ref,
-                           points=cpu(tr.xyz1[:q1]))
+                           points=cpu(tr.xyz1[:q1]), gradient_method=method)
     Lr = OR.losses(ref["comp_normal"], ref["weight_sum"], ref["gradients"], cpu(nrm), cpu(mask))
     lo = cpu(tr.loss_out)
     for i, k in ((1, "normal"), (2, "mask"), (3, "eikonal"), (4, "total")):
