@@ -97,6 +97,23 @@ int sn_march_fill(int64_t n_rays, const float* rays_o, const float* rays_d,
                   const int32_t* packed_info, int64_t capacity,
                   int64_t* ray_indices, float* t_starts, float* t_ends,
                   int32_t* status, void* stream);
+/* Single-pass marcher: ray i writes its samples to slots
+ * [i*slot_stride, i*slot_stride + num_steps[i]) (num_steps written too;
+ * SN_STATUS_CAPACITY if a ray has more than slot_stride samples).  Same
+ * samples as count + fill; used with sn_pack_counts + sn_compact_padded. */
+int sn_march_padded(int64_t n_rays, const float* rays_o, const float* rays_d,
+                    const float* t_min, const float* t_max, const float* jitter,
+                    const float* roi, const uint8_t* grid_binary, int rx, int ry,
+                    int rz, int contraction_type, float step_size,
+                    float cone_angle, int64_t max_iters, int64_t slot_stride,
+                    int32_t* num_steps, int64_t* ray_indices, float* t_starts,
+                    float* t_ends, int32_t* status, void* stream);
+/* Copies padded per-ray samples to their packed_info offsets. */
+int sn_compact_padded(int64_t n_rays, int64_t slot_stride,
+                      const int32_t* packed_info, const int64_t* ray_indices_in,
+                      const float* t_starts_in, const float* t_ends_in,
+                      int64_t* ray_indices_out, float* t_starts_out,
+                      float* t_ends_out, void* stream);
 /* out[i] = grid_binary at samples[i] (0 outside the AABB roi).
  * Replaces query_occ_kernel (NA/nerfacc/cuda/csrc/ray_marching.cu:295-358). */
 int sn_grid_query(int64_t n, const float* samples, const float* roi,

@@ -69,6 +69,9 @@ SIGNATURES: dict[str, tuple] = {
     "sn_march_count": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _F, _F, _I64, _P, _P, _P]),
     "sn_march_fill": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _F, _F, _I64, _P, _I64,
                            _P, _P, _P, _P, _P]),
+    "sn_march_padded": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _F, _F, _I64, _I64,
+                             _P, _P, _P, _P, _P, _P]),
+    "sn_compact_padded": (_I, [_I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sn_grid_query": (_I, [_I64, _P, _P, _P, _I, _I, _I, _I, _P, _P]),
     "sn_occ_points": (_I, [_I64, _P, _P, _I, _I, _I, _P, _I, _P, _P]),
     "sn_occ_ema_update": (_I, [_I64, _P, _P, _F, _P, _P]),

@@ -320,70 +320,137 @@ struct MarchArgs {
   int32_t* status;
 };
 
-template <bool FILL>
-__global__ void __launch_bounds__(128) march_kernel(MarchArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= a.n_rays) return;
+// Warp-per-ray marcher with speculative occupied runs.  The reference marcher
+// (NA/nerfacc/cuda/csrc/ray_marching.cu:135-185) walks one ray sequentially:
+//   while t_mid < far: if occupied(origin + t_mid*dir): emit [t0, t1], t0 = t1,
+//   t1 = t0 + dt, t_mid = (t0 + t1)/2; else t_mid = DDA skip, t0/t1 = t_mid -/+ dt/2.
+// Here the same samples come out bit for bit.  From a state (t0, t1), lane l forms the state
+// after l consecutive occupied steps with exactly the sequential additions
+// (t0' = t1, t1' = t0' + dt, at most 31 of them), all 32 lanes look up the grid
+// at their t_mid in one round trip, and a ballot finds the first lane that is
+// empty or past `far`.  Lanes before it are samples; that lane's state is the
+// sequential marcher's state at the same point, from which it takes the DDA
+// skip (or the marcher stops), and the warp restarts from the broadcast state.
+// Modes: count only (num_steps), fill at packed_info offsets, or fill into
+// fixed slots ray*slot_stride (padded; num_steps written too).
+template <int MODE>  // 0 count, 1 fill packed, 2 fill padded
+__global__ void __launch_bounds__(128) march_warp_kernel(MarchArgs a, int64_t slot_stride) {
+  const int lane = threadIdx.x & 31;
+  const int64_t ray = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (ray >= a.n_rays) return;  // whole warp exits together
   GridView g = a.grid;
   load_roi(g);
   float o[3], d[3], inv[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    o[k] = a.rays_o[3 * i + k];
-    d[k] = a.rays_d[3 * i + k];
+    o[k] = a.rays_o[3 * ray + k];
+    d[k] = a.rays_d[3 * ray + k];
     inv[k] = __fdiv_rn(1.0f, d[k]);
   }
-  float near = a.t_min[i];
-  const float far = a.t_max[i];
-  if (a.jitter) near = __fadd_rn(near, __fmul_rn(a.jitter[i], a.step));
-
+  float near = a.t_min[ray];
+  const float far = a.t_max[ray];
+  if (a.jitter) near = __fadd_rn(near, __fmul_rn(a.jitter[ray], a.step));
   int64_t base = 0, room = 0;
-  if (FILL) {
-    base = a.packed[2 * i];
-    room = a.packed[2 * i + 1];
+  if (MODE == 1) {
+    base = a.packed[2 * ray];
+    room = a.packed[2 * ray + 1];
+  } else if (MODE == 2) {
+    base = ray * slot_stride;
+    room = slot_stride;
   }
   const float dt_min = a.step, dt_max = 1e10f;
   int64_t j = 0, iters = 0;
   float t0 = near;
   float dt = calc_dt(t0, a.cone, dt_min, dt_max);
   float t1 = __fadd_rn(t0, dt);
-  float tm = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
-  bool overflow = false;
-  while (tm < far) {
-    if (++iters > a.max_iters) {
-      atomicOr(a.status, SN_STATUS_MARCH_LIMIT);
-      break;
+  // t_mid of the current state: (t0 + t1) / 2 after an occupied step, but the
+  // skip's own result after a DDA skip (the sequential loop tests that value)
+  float tm0 = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
+  bool overflow = false, limit = false;
+  while (true) {
+    // state after `lane` occupied steps, formed with the sequential additions
+    float l0 = t0, l1 = t1;
+    for (int s = 0; s < lane; ++s) {
+      l0 = l1;
+      l1 = __fadd_rn(l0, calc_dt(l0, a.cone, dt_min, dt_max));
     }
+    const float tm = lane == 0 ? tm0 : __fmul_rn(__fadd_rn(l0, l1), 0.5f);
     float p[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) p[k] = __fmaf_rn(tm, d[k], o[k]);
-    if (occupied_at(g, p)) {
-      if (FILL) {
-        if (j < room && base + j < a.capacity) {
-          a.t_starts[base + j] = t0;
-          a.t_ends[base + j] = t1;
-          a.ray_indices[base + j] = i;
+    const bool inside = tm < far;
+    const bool occ = inside && occupied_at(g, p);
+    const unsigned empty = __ballot_sync(0xffffffffu, !occ);
+    const int m = empty ? __ffs(empty) - 1 : 32;  // occupied run length
+    if (lane < m && MODE != 0) {
+      const int64_t jj = j + lane;
+      if (jj < room && base + jj < a.capacity) {
+        a.t_starts[base + jj] = l0;
+        a.t_ends[base + jj] = l1;
+        a.ray_indices[base + jj] = ray;
+      } else {
+        overflow = true;
+      }
+    }
+    j += m;
+    iters += m + 1;
+    if (m == 32) {  // the whole warp was occupied: continue after lane 31
+      t0 = __shfl_sync(0xffffffffu, l1, 31);
+      t1 = __fadd_rn(t0, calc_dt(t0, a.cone, dt_min, dt_max));
+      tm0 = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
+    } else {
+      // lane m holds the sequential state at the first non-occupied position
+      const bool done = !__shfl_sync(0xffffffffu, inside, m);
+      if (done) break;
+      float ntm = 0.0f, n0 = 0.0f, n1 = 0.0f;
+      if (lane == m) {
+        if (g.ctype == SN_CONTRACTION_AABB) {
+          ntm = advance_voxel(g, tm, dt_min, p, d, inv, far);
+          const float ndt = calc_dt(ntm, a.cone, dt_min, dt_max);
+          n0 = __fsub_rn(ntm, __fmul_rn(ndt, 0.5f));
+          n1 = __fadd_rn(ntm, __fmul_rn(ndt, 0.5f));
         } else {
-          overflow = true;
+          n0 = l1;
+          n1 = __fadd_rn(n0, calc_dt(n0, a.cone, dt_min, dt_max));
+          ntm = __fmul_rn(__fadd_rn(n0, n1), 0.5f);
         }
       }
-      ++j;
-      t0 = t1;
-      t1 = __fadd_rn(t0, calc_dt(t0, a.cone, dt_min, dt_max));
-      tm = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
-    } else if (g.ctype == SN_CONTRACTION_AABB) {
-      tm = advance_voxel(g, tm, dt_min, p, d, inv, far);
-      dt = calc_dt(tm, a.cone, dt_min, dt_max);
-      t0 = __fsub_rn(tm, __fmul_rn(dt, 0.5f));
-      t1 = __fadd_rn(tm, __fmul_rn(dt, 0.5f));
-    } else {
-      t0 = t1;
-      t1 = __fadd_rn(t0, calc_dt(t0, a.cone, dt_min, dt_max));
-      tm = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
+      t0 = __shfl_sync(0xffffffffu, n0, m);
+      t1 = __shfl_sync(0xffffffffu, n1, m);
+      ntm = __shfl_sync(0xffffffffu, ntm, m);
+      tm0 = ntm;
+      if (!(ntm < far)) break;
+      // the sequential loop re-tests occupancy at ntm from state (t0, t1):
+      // the next speculation round starts there (its lane 0 is that test)
+    }
+    if (iters > a.max_iters) {
+      limit = true;
+      break;
     }
   }
-  if (!FILL) a.num_steps[i] = (int32_t)j;
-  if (FILL && overflow && a.status) atomicOr(a.status, SN_STATUS_CAPACITY);
+  if (lane == 0) {
+    if (MODE != 1) a.num_steps[ray] = (int32_t)j;
+    if (limit) atomicOr(a.status, SN_STATUS_MARCH_LIMIT);
+  }
+  if (MODE != 0 && __any_sync(0xffffffffu, overflow) && lane == 0) atomicOr(a.status, SN_STATUS_CAPACITY);
+}
+
+// Copy padded per-ray samples (ray*stride + j, j < count) to packed offsets.
+__global__ void compact_padded_kernel(int64_t n_rays, int64_t stride, const int32_t* __restrict__ packed,
+                                      const int64_t* __restrict__ ri_in, const float* __restrict__ ts_in,
+                                      const float* __restrict__ te_in, int64_t* __restrict__ ri_out,
+                                      float* __restrict__ ts_out, float* __restrict__ te_out) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < n_rays;
+       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t b = packed[2 * r];
+    const int c = packed[2 * r + 1];
+    for (int j = lane; j < c; j += 32) {
+      ri_out[b + j] = ri_in[r * stride + j];
+      ts_out[b + j] = ts_in[r * stride + j];
+      te_out[b + j] = te_in[r * stride + j];
+    }
+  }
 }
 
 __global__ void grid_query_kernel(int64_t n, const float* __restrict__ x, GridView g,
@@ -707,8 +774,41 @@ int sn_march_count(int64_t n_rays, const float* rays_o, const float* rays_d, con
                       contraction_type, step_size, cone_angle, max_iters, status));
   if (n_rays == 0) return SN_OK;
   a.num_steps = num_steps;
-  march_kernel<false><<<div_up(n_rays, 128), 128, 0, as_stream(stream)>>>(a);
+  march_warp_kernel<0><<<div_up(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(a, 0);
   return check_launch("march_count");
+}
+
+int sn_march_padded(int64_t n_rays, const float* rays_o, const float* rays_d, const float* t_min,
+                    const float* t_max, const float* jitter, const float* roi,
+                    const uint8_t* grid_binary, int rx, int ry, int rz, int contraction_type,
+                    float step_size, float cone_angle, int64_t max_iters, int64_t slot_stride,
+                    int32_t* num_steps, int64_t* ray_indices, float* t_starts, float* t_ends,
+                    int32_t* status, void* stream) {
+  MarchArgs a;
+  SN_TRY(march_common(a, n_rays, rays_o, rays_d, t_min, t_max, jitter, roi, grid_binary, rx, ry, rz,
+                      contraction_type, step_size, cone_angle, max_iters, status));
+  SN_REQUIRE(slot_stride > 0, "march_padded: slot_stride must be positive");
+  SN_REQUIRE(num_steps && ray_indices && t_starts && t_ends, "march_padded: null output");
+  if (n_rays == 0) return SN_OK;
+  a.num_steps = num_steps;
+  a.capacity = n_rays * slot_stride;
+  a.ray_indices = ray_indices;
+  a.t_starts = t_starts;
+  a.t_ends = t_ends;
+  march_warp_kernel<2><<<div_up(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(a, slot_stride);
+  return check_launch("march_padded");
+}
+
+int sn_compact_padded(int64_t n_rays, int64_t slot_stride, const int32_t* packed_info,
+                      const int64_t* ray_indices_in, const float* t_starts_in,
+                      const float* t_ends_in, int64_t* ray_indices_out, float* t_starts_out,
+                      float* t_ends_out, void* stream) {
+  SN_REQUIRE(n_rays >= 0 && slot_stride > 0, "compact_padded: bad sizes");
+  if (n_rays == 0) return SN_OK;
+  compact_padded_kernel<<<stride_grid(n_rays * 32, 256, 8), 256, 0, as_stream(stream)>>>(
+      n_rays, slot_stride, packed_info, ray_indices_in, t_starts_in, t_ends_in, ray_indices_out,
+      t_starts_out, t_ends_out);
+  return check_launch("compact_padded");
 }
 
 int sn_march_fill(int64_t n_rays, const float* rays_o, const float* rays_d, const float* t_min,
@@ -728,7 +828,7 @@ int sn_march_fill(int64_t n_rays, const float* rays_o, const float* rays_d, cons
   a.ray_indices = ray_indices;
   a.t_starts = t_starts;
   a.t_ends = t_ends;
-  march_kernel<true><<<div_up(n_rays, 128), 128, 0, as_stream(stream)>>>(a);
+  march_warp_kernel<1><<<div_up(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(a, 0);
   return check_launch("march_fill");
 }
 

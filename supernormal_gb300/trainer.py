@@ -168,6 +168,9 @@ class FusedTrainer:
         self.ridx0 = torch.empty((C0,), dtype=torch.int64, device=dev)
         self.ts0 = torch.empty((C0,), device=dev)
         self.te0 = torch.empty((C0,), device=dev)
+        self.ridx_pad = torch.empty((C0,), dtype=torch.int64, device=dev)
+        self.ts_pad = torch.empty((C0,), device=dev)
+        self.te_pad = torch.empty((C0,), device=dev)
         self.diff = torch.empty((C0,), **i32)
         self.endp = torch.empty((C0, 2), **i32)
         self.n_ends = torch.zeros((1,), **i32)
@@ -304,13 +307,13 @@ class FusedTrainer:
         call("sn_mask_prep", B * P, mask, self.mask_bin, self.mask_sum, st)
         call("sn_near_far_sphere", B, _center_ptr(rays_o, kc), _center_ptr(rays_d, kc), 3 * P,
              self.near, self.far, self.jitter, seed, self.iter_dev, self.ro_c, self.rd_c, st)
-        # --- marching (count, scan, fill) over the centre rays ---
-        margs = (self.ro_c, self.rd_c, self.near, self.far, self.jitter, roi, binary, rx, ry, rz,
-                 ctype, float(dt), 0.0, 0)
-        call("sn_march_count", B, *margs, self.counts0, self.status, st)
+        # --- marching over the centre rays: one pass into per-ray slots, scan, pack ---
+        call("sn_march_padded", B, self.ro_c, self.rd_c, self.near, self.far, self.jitter, roi, binary,
+             rx, ry, rz, ctype, float(dt), 0.0, 0, self.max_steps, self.counts0, self.ridx_pad,
+             self.ts_pad, self.te_pad, self.status, st)
         call("sn_pack_counts", B, self.counts0, self.packed0, self.total0, self.scan_ws, st)
-        call("sn_march_fill", B, *margs, self.packed0, C0, self.ridx0, self.ts0, self.te0,
-             self.status, st)
+        call("sn_compact_padded", B, self.max_steps, self.packed0, self.ridx_pad, self.ts_pad,
+             self.te_pad, self.ridx0, self.ts0, self.te0, st)
         self._mark("march_end")
         # --- culling: field at centre samples, NeuS alpha, visibility, compaction ---
         call("sn_end_diff", C0, self.total0, self.ts0, self.te0, self.diff, st)

@@ -181,6 +181,35 @@ def test_marcher_bit_exact_vs_reference_kernel(nf, ref):
     assert torch.equal(ts, ts_r) and torch.equal(te, te_r)
 
 
+def test_padded_single_pass_marcher_matches(nf):
+    from supernormal_gb300._lib import call, stream_handle
+
+    o, d, near, far, grid, jitter = _march_case(21)
+    step = 2.0 / 1024
+    g = _grid(nf, grid)
+    packed, ri, ts, te = nf.march_packed(T(o), T(d), T(near), T(far), g, step, 0.0, jitter=T(jitter))
+    n = o.shape[0]
+    stride = int(np.ceil(2.0 / step)) + 3
+    st = stream_handle()
+    counts = torch.empty(n, dtype=torch.int32, device="cuda")
+    rp = torch.empty(n * stride, dtype=torch.int64, device="cuda")
+    tsp = torch.empty(n * stride, device="cuda")
+    tep = torch.empty(n * stride, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    roi, binary, rx, ry, rz, ct = nf._grid_args(g, "cuda")
+    call("sn_march_padded", n, T(o), T(d), T(near), T(far), T(jitter), roi, binary, rx, ry, rz, ct, step,
+         0.0, 0, stride, counts, rp, tsp, tep, status, st)
+    packed2, total = nf._pack_counts(counts)
+    m = int(total.item())
+    ri2 = torch.empty(m, dtype=torch.int64, device="cuda")
+    ts2 = torch.empty(m, device="cuda")
+    te2 = torch.empty(m, device="cuda")
+    call("sn_compact_padded", n, stride, packed2, rp, tsp, tep, ri2, ts2, te2, st)
+    assert int(status.item()) == 0
+    assert torch.equal(packed2, packed) and torch.equal(ri2, ri)
+    assert torch.equal(ts2, ts.ravel()) and torch.equal(te2, te.ravel())
+
+
 def test_marcher_edge_cases(nf):
     # no rays; rays that miss the sphere (NaN near/far) give no samples; empty grid
     g = _grid(nf, np.ones((8, 8, 8), np.uint8))
