@@ -64,19 +64,28 @@ def corner_indices(x32: np.ndarray, level: int, offsets, res, scales):
     return cell, frac, idx
 
 
-def encode(x: torch.Tensor, table: torch.Tensor, geom, n_features=2, active_levels=None):
-    """(N, L*F) float64 encoding, differentiable w.r.t. table and x."""
+def encode(x: torch.Tensor, table: torch.Tensor, geom, n_features=2, active_levels=None,
+           cache: dict | None = None):
+    """(N, L*F) float64 encoding, differentiable w.r.t. table and x.  ``cache``
+    (optional dict) keeps the per-level cell data of a fixed x across calls."""
     offsets, res, scales = geom
     L = len(res)
     active = L if active_levels is None else active_levels
-    x32 = x.detach().cpu().numpy().astype(np.float32)
+    x32 = x.detach().cpu().numpy().astype(np.float32) if cache is None or not cache else None
     xd = x.double()
     outs = []
     for l in range(L):
         if l >= active:
             outs.append(torch.zeros((x.shape[0], n_features), dtype=torch.float64))
             continue
-        cell, frac32, idx = corner_indices(x32, l, offsets, res, scales)
+        if cache is not None and l in cache:
+            cell, frac32, idx = cache[l]
+        else:
+            if x32 is None:
+                x32 = x.detach().cpu().numpy().astype(np.float32)
+            cell, frac32, idx = corner_indices(x32, l, offsets, res, scales)
+            if cache is not None:
+                cache[l] = (cell, frac32, idx)
         # value: the float32 fraction tcnn forms (pos rounded to float32 before
         # floor/subtract); derivative: d frac / dx = scale
         xs = xd * float(scales[l])
@@ -100,9 +109,10 @@ def softplus(h, beta=100.0, threshold=20.0):
     return torch.where(h * beta > threshold, h, torch.log1p(torch.exp(h * beta)) / beta)
 
 
-def sdf_network(x, table, v0, g0, b0, v1, g1, b1, geom, active_levels=None, out_cols=None):
+def sdf_network(x, table, v0, g0, b0, v1, g1, b1, geom, active_levels=None, out_cols=None,
+                cache=None):
     """SDFNetwork.forward with n_layers=1, input_concat=True (float64)."""
-    enc = encode(x, table, geom, active_levels=active_levels)
+    enc = encode(x, table, geom, active_levels=active_levels, cache=cache)
     inp = torch.cat([x.double(), enc], dim=1)
     h = inp @ weight_norm(v0.double(), g0.double()).T + b0.double()
     a = softplus(h)

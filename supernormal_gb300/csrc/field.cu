@@ -93,6 +93,18 @@ __device__ __forceinline__ void level_corners(const GridDev& g, int l, const flo
   }
 }
 
+// True on every lane when all 32 lanes of the warp are in the same cell.  Must
+// be reached by all 32 lanes; the three shuffles are issued unconditionally
+// (a short-circuit && around them would leave some lanes out of a full-mask
+// shuffle and deadlock the warp).
+__device__ __forceinline__ bool warp_same_cell(const LevelCorners& c) {
+  const uint32_t c0 = __shfl_sync(0xffffffffu, c.cell[0], 0);
+  const uint32_t c1 = __shfl_sync(0xffffffffu, c.cell[1], 0);
+  const uint32_t c2 = __shfl_sync(0xffffffffu, c.cell[2], 0);
+  const bool same = (c.cell[0] == c0) & (c.cell[1] == c1) & (c.cell[2] == c2);
+  return __all_sync(0xffffffffu, same);
+}
+
 // d w_k / d x_d for linear interpolation (scale * +-1 * product of the other two factors).
 __device__ __forceinline__ float corner_dw(const LevelCorners& c, int k, int d, float s) {
   float w = 1.0f;
@@ -338,10 +350,7 @@ __global__ void __launch_bounds__(kBwdThreads) field_bwd_kernel(FieldArgs a) {
           level_corners(a.g, l, x, c);
           const float d0 = live ? denc[3 + 2 * l] : 0.0f, d1 = live ? denc[4 + 2 * l] : 0.0f;
           if (a.grad_table) {
-            const bool same = (c.cell[0] == __shfl_sync(0xffffffffu, c.cell[0], 0)) &&
-                              (c.cell[1] == __shfl_sync(0xffffffffu, c.cell[1], 0)) &&
-                              (c.cell[2] == __shfl_sync(0xffffffffu, c.cell[2], 0));
-            if (__all_sync(0xffffffffu, same)) {
+            if (warp_same_cell(c)) {
 #pragma unroll
               for (int k = 0; k < 8; ++k) {
                 float v0 = c.w[k] * d0, v1 = c.w[k] * d1;
@@ -664,10 +673,7 @@ __global__ void __launch_bounds__(kBwdThreads) field_grad_bwd_kernel(FieldArgs a
           LevelCorners c;
           level_corners(a.g, l, x, c);
           const float sc = a.g.scale[l];
-          const bool same = (c.cell[0] == __shfl_sync(0xffffffffu, c.cell[0], 0)) &&
-                            (c.cell[1] == __shfl_sync(0xffffffffu, c.cell[1], 0)) &&
-                            (c.cell[2] == __shfl_sync(0xffffffffu, c.cell[2], 0));
-          const bool uni = __all_sync(0xffffffffu, same);
+          const bool uni = warp_same_cell(c);
 #pragma unroll
           for (int k = 0; k < 8; ++k) {
             const float wg = z[0] * corner_dw(c, k, 0, sc) + z[1] * corner_dw(c, k, 1, sc) +

@@ -131,10 +131,11 @@ def test_second_order_adjoint_vs_central_differences(built_lib):
     geom = OF.geometry_from_module(net)
     xr = x.cpu().double()
     gam = gamma.cpu().double()
+    cache = {}
 
     def objective(p):
         xx = xr.clone().requires_grad_(True)
-        s = OF.sdf_network(xx, **p, geom=geom, active_levels=16, out_cols=1)
+        s = OF.sdf_network(xx, **p, geom=geom, active_levels=16, out_cols=1, cache=cache)
         (gx,) = torch.autograd.grad(s.sum(), xx)
         return float((gx * gam).sum())
 
