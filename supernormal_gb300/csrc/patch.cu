@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(MAXT) patch_block_kernel(PatchArgs a) {
   if (MODE != kBwd) {
     for (int j0 = 0; j0 < steps; j0 += 32) {
       const int j = j0 + lane;
-      const bool ok = j < steps;
+      const bool ok = j < steps && base + j < S;  // S clamps a packed table past capacity
       const int64_t i = base + j;
       Sample s;
       chunk_sample(a, R, i, S, inv_s, ok, lane, sm_s0, sm_pos, s);
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(MAXT) patch_block_kernel(PatchArgs a) {
   Tc = 1.0f;
   for (int j0 = 0; j0 < steps; j0 += 32) {
     const int j = j0 + lane;
-    const bool ok = j < steps;
+    const bool ok = j < steps && base + j < S;  // S clamps a packed table past capacity
     Sample s;
     chunk_sample(a, R, base + j, S, inv_s, ok, lane, sm_s0, sm_pos, s);
     const float T = transmittance(ok ? __fsub_rn(1.0f, s.alpha) : 1.0f, Tc, lane);
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(MAXT) patch_block_kernel(PatchArgs a) {
   Tc = 1.0f;
   for (int j0 = 0; j0 < steps; j0 += 32) {
     const int j = j0 + lane;
-    const bool ok = j < steps;
+    const bool ok = j < steps && base + j < S;  // S clamps a packed table past capacity
     const int64_t i = base + j;
     Sample s;
     chunk_sample(a, R, i, S, inv_s, ok, lane, sm_s0, sm_pos, s);
