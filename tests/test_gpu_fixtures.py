@@ -1,8 +1,8 @@
 """CUDA path against the fixtures produced by the reference's own Python code.
 
 Same inputs, parameters and culled samples as tests/golden/*.npz; float32
-kernels vs the reference's float64 run: field outputs, rendered normals and
-mask 2e-5 relative, dfd gradients 2e-4 relative, culling alpha 1e-4 absolute,
+kernels vs the reference's float64 run: field outputs and mask 2e-5 relative,
+dfd gradients and rendered normals 2e-4 relative, culling alpha 1e-4 absolute,
 losses 1e-4 relative, parameter gradients 2e-3 relative (to each gradient's
 max-abs)."""
 from pathlib import Path
@@ -59,11 +59,14 @@ def test_renderer_matches_reference_fixture(built_lib):
     c = lambda k, dt=torch.float32: torch.from_numpy(d[k]).to(dt).cuda()
     out = r.render_samples(c("rays_o"), c("rays_d"), c("plane_n"), c("vinv"),
                            c("patch_indices", torch.int64), c("t_starts"), c("t_ends"))
-    assert rel(out["comp_normal"].detach().cpu().numpy(), d["comp_normal"]) < 2e-5
     assert rel(out["weight_sum"].detach().cpu().numpy(), d["weight_sum"]) < 2e-5
     # dfd gradients are sdf differences over ~1e-2 distances: float32 rounding of
     # the sdf (~1e-7) is amplified ~100x
     assert rel(out["gradients"].detach().cpu().numpy(), d["gradients"]) < 2e-4
+    # the rendered normal is sum_i w_i g_i with sum_i w_i <= 1: it carries the
+    # gradients' error, so it gets their bound (relative to the largest gradient)
+    err = np.abs(out["comp_normal"].detach().cpu().numpy().astype(np.float64) - d["comp_normal"]).max()
+    assert err < 2e-4 * np.abs(d["gradients"]).max()
     L = OR.losses(out["comp_normal"], out["weight_sum"], out["gradients"], c("normal"), c("mask"))
     got = np.array([L["normal"].item(), L["eikonal"].item(), L["mask"].item(), L["total"].item()])
     assert rel(got, d["losses"]) < 1e-4
