@@ -61,7 +61,7 @@ def cull(field, packed, ridx, ts, te, rays_o_c, rays_d_c, variance, early_stop_e
 
 
 def patch_forward(field, patch_idx, ts, te, rays_o_all, rays_d_all, plane_n, vinv, variance,
-                  points=None, gradient_method="dfd"):
+                  points=None, gradient_method="dfd", ext_gradients=None):
     """models/renderer.py:142-267 for gradient_method='dfd' (float64).
 
     patch_idx/ts/te are the culled centre samples; rays_* are (B, H, W, 3).
@@ -122,7 +122,10 @@ def patch_forward(field, patch_idx, ts, te, rays_o_all, rays_d_all, plane_n, vin
     df_dy = torch.cat([dy_t, df_dy, dy_b], dim=1)
     proj = torch.cat([df_dt, df_dx, df_dy], dim=-1)
     gradients = (vi[pidx] @ proj[..., None])[..., 0]                  # (S, H, W, 3)
-    if gradient_method == "ad":
+    if gradient_method == "ad" and ext_gradients is not None:
+        # given start-point gradients (S * H * W, 3): isolates the patch math
+        gradients = ext_gradients.reshape(S, H, W, 3)
+    elif gradient_method == "ad":
         # SDFNetwork.gradient at the start points (models/renderer.py:225-226,
         # models/fields.py:107-119: autograd with create_graph)
         xs = q[: S * H * W].detach().clone().requires_grad_(True)

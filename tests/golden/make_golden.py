@@ -217,12 +217,18 @@ def main(ref_root: str):
     RECORD["jitter"] = torch.rand(B, generator=gp).float().numpy()
     r = NeuSRenderer(net, var, "dfd")
     r.sampling_step_size = 1.0 / 40
+    # the last SDFNetwork call of render() evaluates every patch point at once
+    # (models/renderer.py:160): keep its points, values and, below, dL/dsdf
+    calls = []
+    hook = net.register_forward_hook(lambda m, inp, outp: calls.append((inp[0].detach(), outp)))
     out = r.render(ro.double(), rd.double(), pn.double(), near.double(), far.double(), vinv.double())
+    hook.remove()
+    patch_x, patch_sdf = calls[-1]
     nl, el, ml, total = exp_runner_losses(out, nrm.double(), mask.double())
     all_params = dict(net.named_parameters())
     all_params["variance"] = var.variance
     pn_names = sorted(all_params)
-    rgrads = torch.autograd.grad(total, [all_params[n] for n in pn_names])
+    *rgrads, patch_dsdf = torch.autograd.grad(total, [all_params[n] for n in pn_names] + [patch_sdf])
     packed0, ri0, ts0, te0 = RECORD["pre_cull"]
     vis = RECORD["vis"]
     np.savez_compressed(
@@ -235,6 +241,8 @@ def main(ref_root: str):
         patch_indices=ri0[vis], t_starts=ts0[vis], t_ends=te0[vis],
         comp_normal=out["comp_normal"].detach().numpy(), weight_sum=out["weight_sum"].detach().numpy(),
         gradients=out["gradients"].detach().numpy(),
+        patch_points=patch_x.numpy(), patch_sdf=patch_sdf.detach().numpy(),
+        patch_dsdf=patch_dsdf.numpy(),
         losses=np.array([nl.item(), el.item(), ml.item(), total.item()]),
         enc=np.array([ENC[k] for k in ("n_levels", "n_features_per_level", "log2_hashmap_size",
                                        "base_resolution")] + [ENC["per_level_scale"]]),

@@ -87,6 +87,30 @@ def test_field_backward_matches_oracle(built_lib, enc, d_out, active, cols):
         assert rel_err(g.cpu().numpy(), r.numpy()) < 1e-3, n
 
 
+@pytest.mark.parametrize("spread", [1e-3, 3e-2])
+def test_field_backward_clustered_points(built_lib, spread):
+    """Warps of 32 neighbouring points (as a patch's samples are): coarse levels
+    put a whole warp in one cell, which takes the shuffle-reduced scatter."""
+    net = make_net(ENC1, d_out=16, table_scale=1e3)
+    net.bindwidth = 16
+    g = torch.Generator(device="cuda").manual_seed(5)
+    centres = torch.rand((70, 1, 3), device="cuda", generator=g) * 1.6 - 0.8
+    x = (centres + spread * torch.randn((70, 32, 3), device="cuda", generator=g)).reshape(-1, 3)
+    x = x[:2221].contiguous().requires_grad_(True)       # ragged last warp
+    y = net(x)
+    gy = torch.randn_like(y)
+    params = [net.encoding.params, net.lin0.weight_v, net.lin0.weight_g, net.lin0.bias,
+              net.lin1.weight_v, net.lin1.weight_g, net.lin1.bias]
+    grads = torch.autograd.grad(y, params + [x], gy)
+    prm = OF.params_from_module(net)
+    xr = x.detach().cpu().double().requires_grad_(True)
+    ref = OF.sdf_network(xr, **prm, geom=OF.geometry_from_module(net), active_levels=16)
+    names = ["table", "v0", "g0", "b0", "v1", "g1", "b1"]
+    rgrads = torch.autograd.grad(ref, [prm[n] for n in names] + [xr], gy.cpu().double())
+    for n, gd, r in zip(names + ["x"], grads, rgrads):
+        assert rel_err(gd.cpu().numpy(), r.numpy()) < 1e-3, n
+
+
 @pytest.mark.parametrize("enc,active", [(ENC1, 16), (ENC_SHIPPED, 9)])
 def test_gradient_and_second_order_adjoint_match_oracle(built_lib, enc, active):
     net = make_net(enc, d_out=16, table_scale=1e3)

@@ -47,7 +47,27 @@ def test_field_matches_reference_fixture(built_lib):
         assert rel(g.cpu().numpy(), d[f"grad/{n}"]) < 2e-3, n
 
 
+class _FixedSdf:
+    """sdf_network stand-in returning given values at the patch points."""
+
+    def __init__(self, values):
+        self.values = values
+
+    def sdf(self, x):
+        assert x.shape[0] == self.values.shape[0]
+        return self.values
+
+
 def test_renderer_matches_reference_fixture(built_lib):
+    """Three parts, each free of the other's float32 error (alpha's clip and the
+    mask loss's clip make the adjoint branch on the sdf values, and inv_s = e^6
+    turns a 1e-7 sdf difference into ~1e-5 in alpha):
+    (a) the field at the reference's own patch points;
+    (b) the fused patch kernel on the reference's sdf values: outputs, losses,
+        d loss / d sdf at every start and end point, d loss / d variance;
+    (c) parameter gradients: the field's backward of the reference's d loss / d sdf.
+    The whole chain (our field into our kernel) is then held to the forward
+    bound that (a)'s error allows."""
     from oracle import renderer as OR
     from supernormal_gb300.fields import SingleVarianceNetwork
     from supernormal_gb300.renderer import NeuSRenderer
@@ -55,27 +75,42 @@ def test_renderer_matches_reference_fixture(built_lib):
     d = np.load(G / "reference_render.npz")
     net = _net(d, 1)
     var = SingleVarianceNetwork(float(d["variance"])).cuda()
-    r = NeuSRenderer(net, var)
     c = lambda k, dt=torch.float32: torch.from_numpy(d[k]).to(dt).cuda()
-    out = r.render_samples(c("rays_o"), c("rays_d"), c("plane_n"), c("vinv"),
-                           c("patch_indices", torch.int64), c("t_starts"), c("t_ends"))
-    assert rel(out["weight_sum"].detach().cpu().numpy(), d["weight_sum"]) < 2e-5
-    # dfd gradients are sdf differences over ~1e-2 distances: float32 rounding of
-    # the sdf (~1e-7) is amplified ~100x
-    assert rel(out["gradients"].detach().cpu().numpy(), d["gradients"]) < 2e-4
-    # the rendered normal is sum_i w_i g_i with sum_i w_i <= 1: it carries the
-    # gradients' error, so it gets their bound (relative to the largest gradient)
-    err = np.abs(out["comp_normal"].detach().cpu().numpy().astype(np.float64) - d["comp_normal"]).max()
-    assert err < 2e-4 * np.abs(d["gradients"]).max()
+    cpu = lambda t: t.detach().cpu().numpy()
+    samples = (c("patch_indices", torch.int64), c("t_starts"), c("t_ends"))
+    # (b)
+    vals = c("patch_sdf").requires_grad_(True)
+    rf = NeuSRenderer(_FixedSdf(vals), var)
+    out = rf.render_samples(c("rays_o"), c("rays_d"), c("plane_n"), c("vinv"), *samples)
+    assert rf.last_points.shape == d["patch_points"].shape
+    assert np.abs(cpu(rf.last_points) - d["patch_points"]).max() < 2e-6
+    assert rel(cpu(out["weight_sum"]), d["weight_sum"]) < 2e-5
+    # dfd gradients are sdf differences over ~1e-2 distances: the float32
+    # rounding of the sdf (~3e-8) is amplified ~100x
+    assert rel(cpu(out["gradients"]), d["gradients"]) < 2e-4
+    # the rendered normal is sum_i w_i g_i with sum_i w_i <= 1: the gradients' bound
+    assert np.abs(cpu(out["comp_normal"]).astype(np.float64) - d["comp_normal"]).max() < \
+        2e-4 * np.abs(d["gradients"]).max()
     L = OR.losses(out["comp_normal"], out["weight_sum"], out["gradients"], c("normal"), c("mask"))
     got = np.array([L["normal"].item(), L["eikonal"].item(), L["mask"].item(), L["total"].item()])
     assert rel(got, d["losses"]) < 1e-4
+    dsdf, dvar = torch.autograd.grad(L["total"], [vals, var.variance])
+    assert rel(cpu(dsdf), d["patch_dsdf"]) < 1e-4
+    assert rel(cpu(dvar), d["grad/variance"]) < 1e-4
+    # (a)
+    x = c("patch_points")
+    s = net.sdf(x)
+    assert rel(cpu(s), d["patch_sdf"]) < 2e-5
+    # (c)
     params = dict(net.named_parameters())
-    params["variance"] = var.variance
-    names = [str(n) for n in d["param_names"]]
-    grads = torch.autograd.grad(L["total"], [params[n] for n in names])
+    names = [str(n) for n in d["param_names"] if str(n) != "variance"]
+    grads = torch.autograd.grad(s, [params[n] for n in names], c("patch_dsdf"))
     for n, g in zip(names, grads):
-        assert rel(g.cpu().numpy(), d[f"grad/{n}"]) < 2e-3, n
+        assert rel(cpu(g), d[f"grad/{n}"]) < 2e-3, n
+    # whole chain, forward: our field's error (a) through alpha (x inv_s / 4 ~ 100)
+    r = NeuSRenderer(net, var)
+    full = r.render_samples(c("rays_o"), c("rays_d"), c("plane_n"), c("vinv"), *samples)
+    assert rel(cpu(full["weight_sum"]), d["weight_sum"]) < 1e-4
 
 
 def test_culling_matches_reference_fixture(built_lib):

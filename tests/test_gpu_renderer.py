@@ -2,7 +2,8 @@
 
 The oracle re-runs models/renderer.py's patch math and exp_runner.py's losses
 on the samples our marcher/culling kept (the marcher itself is checked bit
-for bit in test_gpu_nerfacc.py).  Tolerances: rendered normals 2e-4 and
+for bit in test_gpu_nerfacc.py), with the device field's sdf values at the
+device's query points (``device_valued``).  Tolerances: rendered normals 2e-4 and
 weight sums 2e-5 absolute, losses 1e-4 relative, parameter gradients 2e-3
 relative to each gradient's max-abs (float32 kernels with atomics vs float64)."""
 import numpy as np
@@ -63,6 +64,24 @@ def oracle_field(net):
     return prm, (lambda x: OF.sdf_network(x, **prm, geom=geom, active_levels=act, out_cols=1))
 
 
+def device_valued(fld, net, points):
+    """The oracle field with the device field's float32 values at ``points`` and
+    the float64 field's derivatives (straight through).  alpha's clip and the
+    mask loss's clip branch on the sdf values, and inv_s amplifies a 1e-7 sdf
+    difference, so the patch math is compared at the device's own values while
+    the field's value parity is asserted here and its derivatives flow through
+    the oracle.  ('ad' evaluates the start points, a prefix of ``points``.)"""
+    dev = net.sdf(points).detach().cpu().double()
+    ref = fld(torch.as_tensor(cpu(points)).double()).detach()
+    assert np.abs(dev.numpy() - ref.numpy()).max() < 2e-5 * max(np.abs(ref.numpy()).max(), 1.0)
+
+    def field(q):
+        s = fld(q)
+        return s + (dev[: s.shape[0]].reshape(s.shape) - s).detach()
+
+    return field
+
+
 def full_grid():
     from supernormal_gb300.nerfacc import OccupancyGrid
 
@@ -91,8 +110,9 @@ def test_renderer_forward_backward_matches_oracle(scene, method):
     assert pidx.size > 200
     prm, fld = oracle_field(net)
     var_ref = var.variance.detach().cpu().double().clone().requires_grad_(True)
-    ref = OR.patch_forward(fld, pidx, ts, te, cpu(ro), cpu(rd), cpu(pn), cpu(vinv), var_ref,
-                           points=cpu(r.last_points), gradient_method=method)
+    ref = OR.patch_forward(device_valued(fld, net, r.last_points), pidx, ts, te, cpu(ro), cpu(rd),
+                           cpu(pn), cpu(vinv), var_ref, points=cpu(r.last_points),
+                           gradient_method=method)
     assert np.abs(cpu(out["comp_normal"]) - cpu(ref["comp_normal"])).max() < 2e-4
     assert np.abs(cpu(out["weight_sum"]) - cpu(ref["weight_sum"])).max() < 2e-5
     assert np.abs(cpu(out["gradients"]) - cpu(ref["gradients"])).max() < 2e-3
@@ -113,6 +133,67 @@ def test_renderer_forward_backward_matches_oracle(scene, method):
         if b is None:
             continue
         assert grad_err(n, cpu(a), b.numpy()) < 2e-3, n
+
+
+class _FixedSdf:
+    """sdf_network stand-in returning given values (a leaf) at the query points."""
+
+    def __init__(self, values, ext=None):
+        self.values, self.ext = values, ext
+
+    def sdf(self, x):
+        assert x.shape[0] == self.values.shape[0]
+        return self.values
+
+    def sdf_and_gradient(self, x):
+        return self.values[: x.shape[0]], self.ext
+
+
+@pytest.mark.parametrize("method", ["dfd", "ad"])
+def test_patch_adjoint_matches_oracle_on_fixed_sdf(scene, method):
+    """The fused patch kernel alone: d loss / d sdf (every start and end point),
+    d / d variance and, for 'ad', d / d gradients, for a linear loss on all three
+    outputs, against float64 autograd of the oracle's patch math on the same
+    float32 sdf values."""
+    from supernormal_gb300.renderer import NeuSRenderer, near_far_from_sphere
+
+    net, var = make()
+    r = NeuSRenderer(net, var, gradient_method=method)
+    r.occupancy_grid = full_grid()
+    r.sampling_step_size = 1.0 / 96
+    g = torch.Generator(device="cuda").manual_seed(11)
+    ro, rd, pn, vinv, _, _ = scene.gen_random_patches(64, generator=g)
+    near, far = near_far_from_sphere(ro[:, 1, 1], rd[:, 1, 1])
+    r.render(ro, rd, pn, near, far, vinv)
+    pidx, ts, te = r.last_samples
+    pts = r.last_points
+    S, P = pidx.shape[0], 9
+    assert S > 100
+    vals = net.sdf(pts).detach().clone().requires_grad_(True)
+    ext = None
+    if method == "ad":
+        ext = (torch.randn((S * P, 3), device="cuda", generator=g) * 0.3 + torch.tensor(
+            [0.0, 0.0, 1.0], device="cuda")).requires_grad_(True)
+    rf = NeuSRenderer(_FixedSdf(vals, ext), var, gradient_method=method)
+    out = rf.render_samples(ro, rd, pn, vinv, pidx, ts, te, method)
+    gc = torch.randn(out["comp_normal"].shape, device="cuda", generator=g)
+    gw = torch.randn(out["weight_sum"].shape, device="cuda", generator=g)
+    gg = torch.randn(out["gradients"].shape, device="cuda", generator=g)
+    L = (out["comp_normal"] * gc).sum() + (out["weight_sum"] * gw).sum() + (out["gradients"] * gg).sum()
+    leaves = [vals, var.variance] + ([ext] if ext is not None else [])
+    got = torch.autograd.grad(L, leaves)
+
+    v64 = vals.detach().cpu().double().requires_grad_(True)
+    var64 = var.variance.detach().cpu().double().clone().requires_grad_(True)
+    e64 = None if ext is None else ext.detach().cpu().double().requires_grad_(True)
+    ref = OR.patch_forward(lambda q: v64, cpu(pidx), cpu(ts), cpu(te), cpu(ro), cpu(rd), cpu(pn),
+                           cpu(vinv), var64, points=cpu(pts), gradient_method=method,
+                           ext_gradients=e64)
+    Lr = ((ref["comp_normal"] * gc.cpu().double()).sum() + (ref["weight_sum"] * gw.cpu().double()).sum()
+          + (ref["gradients"] * gg.cpu().double()).sum())
+    refg = torch.autograd.grad(Lr, [v64, var64] + ([e64] if e64 is not None else []))
+    for name, a, b in zip(["sdf", "variance", "gradients"], got, refg):
+        assert rel_err(cpu(a).ravel(), b.numpy().ravel()) < 1e-4, name
 
 
 def _trainer(scene, B=128, **kw):
@@ -146,8 +227,9 @@ def test_trainer_loss_and_grads_match_oracle(scene, method):
     assert (vis != gpu_vis).mean() < 2e-3
     pidx, ts, te = cpu(tr.ridx1[:S]), cpu(tr.ts1[:S]), cpu(tr.te1[:S])
     q1 = int(tr.q1.item())
-    ref = OR.patch_forward(fld, pidx, ts, te, cpu(ro), cpu(rd), cpu(pn), cpu(vinv), var_ref,
-                           points=cpu(tr.xyz1[:q1]), gradient_method=method)
+    ref = OR.patch_forward(device_valued(fld, net, tr.xyz1[:q1]), pidx, ts, te, cpu(ro), cpu(rd),
+                           cpu(pn), cpu(vinv), var_ref, points=cpu(tr.xyz1[:q1]),
+                           gradient_method=method)
     Lr = OR.losses(ref["comp_normal"], ref["weight_sum"], ref["gradients"], cpu(nrm), cpu(mask))
     lo = cpu(tr.loss_out)
     for i, k in ((1, "normal"), (2, "mask"), (3, "eikonal"), (4, "total")):

@@ -101,3 +101,20 @@ def test_patch_render_losses_and_grads_match_reference_code():
     for n, g in zip(names, grads):
         key = "variance" if n == "variance" else inv[n]
         assert rel(g.numpy(), d[f"grad/{key}"]) < 2e-5, n
+
+
+def test_patch_math_on_reference_sdf_values():
+    """The oracle's patch math alone, fed the sdf values the reference's own
+    SDFNetwork call produced at the patch points: same outputs, and the same
+    d loss / d sdf at every start and end point."""
+    d = np.load(G / "reference_render.npz")
+    var = torch.tensor(float(d["variance"]), dtype=torch.float64, requires_grad=True)
+    sdf = torch.from_numpy(d["patch_sdf"]).requires_grad_(True)
+    out = OR.patch_forward(lambda q: sdf, d["patch_indices"], d["t_starts"], d["t_ends"], d["rays_o"],
+                           d["rays_d"], d["plane_n"], d["vinv"], var)
+    assert rel(out["comp_normal"].detach().numpy(), d["comp_normal"]) < 1e-12
+    assert rel(out["weight_sum"].detach().numpy(), d["weight_sum"]) < 1e-12
+    L = OR.losses(out["comp_normal"], out["weight_sum"], out["gradients"], d["normal"], d["mask"])
+    dsdf, dvar = torch.autograd.grad(L["total"], [sdf, var])
+    assert rel(dsdf.numpy(), d["patch_dsdf"]) < 1e-10
+    assert rel(dvar.numpy(), d["grad/variance"]) < 1e-10
