@@ -61,6 +61,17 @@ size_t sn_scan_workspace_bytes(int64_t n);
  * and NA/nerfacc/pack.py:73-75, without a host synchronisation. */
 int sn_pack_counts(int64_t n, const int32_t* counts, int32_t* packed_info,
                    int32_t* total, void* workspace, void* stream);
+/* sn_pack_counts that allocates nothing and takes no workspace: the tile sums
+ * of the multi-tile scan live in a static device array.  No reference
+ * counterpart (the reference's cumsum allocates through torch); it serves
+ * callers that hold only borrowed device pointers and have no device
+ * allocator of their own (a C or FFI binding handed tensors by its framework).
+ * Limit: n <= 16,777,216 entries (larger n -> SN_ERR_INVALID with a message).
+ * The first call on each device looks up the scratch address with that device
+ * current; make it before any stream capture.  The scratch is one per device:
+ * calls that overlap on a device (other streams or threads) race. */
+int sn_pack_counts_static(int64_t n, const int32_t* counts, int32_t* packed_info,
+                          int32_t* total, void* stream);
 /* counts[r] = number of samples with ray_indices == r (counts zeroed here).
  * Replaces the scatter_add_ in NA/nerfacc/pack.py:70-72. */
 int sn_count_indices(int64_t n_samples, const int64_t* ray_indices,

@@ -13,6 +13,8 @@
 
 #include <string.h>
 
+#include <mutex>
+
 namespace sn {
 
 static thread_local char g_err[512];
@@ -170,6 +172,38 @@ int pack_counts(int64_t n, const int32_t* counts, int32_t* packed, int32_t* tota
   scan_tile_offsets<<<1, kScanThreads, 0, st>>>(tiles, n_tiles, total);
   scan_tile_apply<<<(unsigned)n_tiles, kScanThreads, 0, st>>>(counts, n, tiles, packed, nullptr);
   return check_launch("pack_counts", 3);
+}
+
+// Static scratch of sn_pack_counts_static: tile sums of up to kPackStaticMaxTiles
+// tiles.  Its device address is looked up once per device (with that device
+// current) and cached.
+constexpr int64_t kPackStaticMaxTiles = 4096;
+constexpr int64_t kPackStaticMaxEntries = kPackStaticMaxTiles * kScanTile;
+static __device__ __align__(256) int32_t g_pack_scratch[kPackStaticMaxTiles];
+constexpr int kPackScratchDevices = 64;
+static std::mutex g_pack_scratch_mu;
+static int32_t* g_pack_scratch_ptr[kPackScratchDevices];
+
+int pack_scratch_for_current_device(int32_t** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_error("pack_counts_static: cudaGetDevice failed: %s", cudaGetErrorString(e));
+    return SN_ERR_CUDA;
+  }
+  SN_REQUIRE(dev >= 0 && dev < kPackScratchDevices, "pack_counts_static: device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_pack_scratch_mu);
+  if (!g_pack_scratch_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_pack_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      set_error("pack_counts_static: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return SN_ERR_CUDA;
+    }
+    g_pack_scratch_ptr[dev] = static_cast<int32_t*>(p);
+  }
+  *out = g_pack_scratch_ptr[dev];
+  return SN_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -713,6 +747,25 @@ int sn_pack_counts(int64_t n, const int32_t* counts, int32_t* packed_info, int32
   SN_REQUIRE(n <= ((int64_t)1 << 31) - 1, "pack_counts: n too large");
   SN_REQUIRE(n == 0 || (counts && packed_info), "pack_counts: null buffer");
   return sn::pack_counts(n, counts, packed_info, total, workspace, as_stream(stream));
+}
+
+// sn_pack_counts without a caller workspace: the multi-tile scan's tile sums
+// live in a file-scope device array, so the call allocates nothing.  Limit:
+// kPackStaticMaxTiles tiles of kScanTile entries (16,777,216 entries, 16 KiB of
+// scratch).  Nothing in the scratch has to start at zero (every tile sum is
+// written by scan_tile_reduce before scan_tile_offsets reads it).  The scratch
+// is one per device, so calls that overlap on the device (other streams or
+// host threads) race on it.
+int sn_pack_counts_static(int64_t n, const int32_t* counts, int32_t* packed_info, int32_t* total,
+                          void* stream) {
+  SN_REQUIRE(n >= 0, "pack_counts_static: n < 0");
+  SN_REQUIRE(n <= sn::kPackStaticMaxEntries,
+             "pack_counts_static: n = %lld exceeds the static scratch limit of %lld entries",
+             (long long)n, (long long)sn::kPackStaticMaxEntries);
+  SN_REQUIRE(n == 0 || (counts && packed_info), "pack_counts_static: null buffer");
+  int32_t* scratch = nullptr;
+  SN_TRY(sn::pack_scratch_for_current_device(&scratch));
+  return sn::pack_counts(n, counts, packed_info, total, scratch, as_stream(stream));
 }
 
 int sn_count_indices(int64_t n_samples, const int64_t* ray_indices, int64_t n_rays, int32_t* counts,
