@@ -38,6 +38,7 @@ extern "C" {
 /* device status word bits (OR-ed by kernels into an int32 device word) */
 #define SN_STATUS_MARCH_LIMIT 1   /* a ray exceeded the marching iteration cap */
 #define SN_STATUS_CAPACITY 2      /* a sample buffer overflowed its capacity   */
+#define SN_STATUS_TIMEOUT 4       /* a tensor-core kernel's bounded wait ran out */
 
 /* contraction types; same values as nerfacc's ContractionType
  * (NA/nerfacc/cuda/csrc/include/helpers_contraction.h:9-14) */
@@ -429,6 +430,14 @@ int sn_adam_step(int64_t n, float* param, float* grad, float* exp_avg,
                  float* exp_avg_sq, void* param_half, const float* lr_dev,
                  const int32_t* step_dev, float lr, int step, float beta1,
                  float beta2, float eps, int zero_grad, void* stream);
+
+/* ---- tensor-core MLP pieces (tcgen05, sm_103a) ------------------------------ */
+/* y = x W^T + b with W (64, k), k <= 64: the first Linear of SDFNetwork
+ * (models/fields.py:90-99, nn.Linear in fp32), fp32-accurate via 3xTF32 on
+ * the tensor cores with TMEM accumulators.  b may be null.  A bounded wait
+ * that runs out ORs SN_STATUS_TIMEOUT into *status. */
+int sn_linear_tc(int64_t n, int k, const float* x, const float* w, const float* b, float* y,
+                 int32_t* status, void* stream);
 
 #ifdef __cplusplus
 }
