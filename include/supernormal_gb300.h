@@ -239,6 +239,7 @@ typedef struct sn_mlp_desc {
   const float* b0;
   const float* w1;
   const float* b1;
+  int32_t* status;   /* nullable device word: SN_STATUS_TIMEOUT is OR-ed here */
 } sn_mlp_desc;
 
 /* Level offsets, resolutions and scales of tcnn's GridEncoding for

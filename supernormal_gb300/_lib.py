@@ -21,6 +21,7 @@ SN_ERR_LIMIT = 4
 SN_ERR_UNSUPPORTED = 5
 SN_STATUS_MARCH_LIMIT = 1
 SN_STATUS_CAPACITY = 2
+SN_STATUS_TIMEOUT = 4
 SN_MAX_LEVELS = 32
 
 
@@ -51,6 +52,7 @@ class MlpDesc(C.Structure):
         ("b0", C.c_void_p),
         ("w1", C.c_void_p),
         ("b1", C.c_void_p),
+        ("status", C.c_void_p),
     ]
 
 

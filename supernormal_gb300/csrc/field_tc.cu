@@ -1,0 +1,579 @@
+// Tensor-core (tcgen05) fused SDF field: hash-grid encoding + SDFNetwork MLP
+// (models/fields.py:76-99) forward and backward, fp32-accurate (3xTF32).
+//
+// A CTA owns 128-point tiles (persistent over tiles) with 16 warps: warp w
+// serves TMEM lane quadrant q = w % 4 (points 32q..32q+31 of the tile) as
+// member g = w / 4 of that quadrant's group of four.  The four members split
+// the per-point work -- hash-grid levels 4g..4g+3, hidden units 16g..16g+15 --
+// and write their parts of each point's row straight into the point's TMEM
+// lane, where the tensor core reads it as the A operand.  One thread issues
+// the MMAs; everyone else waits on an mbarrier (bounded).
+//
+// MLP input order inside the kernels (K = 40): encoding features first
+// (level l, feature f -> column 2l + f), then x (columns 32..34), then zeros;
+// W0 is permuted to match when it is staged, and the weight gradient is
+// permuted back when it is flushed.
+//
+// Forward:  H = IN W0^T (TMEM), act = softplus(H + b0), out = W1 act + b1.
+// Backward: recompute H, dH = (W1^T g) * softplus'(H + b0),
+//           dIN = dH W0 (TMEM) -> table-gradient scatter (+ dL/dx),
+//           dW0 += dH^T IN over the CTA's points (TMEM, A = [dH_hi; dH_lo]
+//           stacked as 128 rows so two MMAs per K step give all four
+//           hi/lo products), db0 from a row of ones in IN^T,
+//           dW1, db1 by warp reductions.
+#include "field_common.cuh"
+#include "tc.cuh"
+
+namespace sn {
+namespace {
+
+constexpr int kTile = 128;
+constexpr int kWarps = 16;
+constexpr int kThreads = 32 * kWarps;
+constexpr int kK1 = 40;        // MLP input width inside the kernels (35 used)
+constexpr int kN2 = 48;        // dIN columns (N of the second MMA; 35 used)
+constexpr int kXCol = 32;      // first column of x in the permuted input
+constexpr int kOnesRow = 35;   // row of ones in IN^T (gives db0)
+constexpr uint32_t kCols = 256;
+
+// TMEM column map (both kernels): H / dIN share [0, 64); the input rows
+// (hi, lo) and later dH (hi, lo) share [64, 192); dW0 accumulates in [192, 240).
+constexpr uint32_t kColH = 0, kColInHi = 64, kColInLo = 64 + kK1;
+constexpr uint32_t kColDhHi = 64, kColDhLo = 128, kColDw0 = 192;
+
+// Permuted input column -> column of W0 (or -1 for a zero column).
+__device__ __forceinline__ int w0_col(int c, int L) {
+  if (c < 2 * L) return 3 + c;
+  if (c >= kXCol && c < kXCol + 3) return c - kXCol;
+  return -1;
+}
+
+// W0 (64, din) -> B1 (N = 64 hidden, K = 40 inputs, K-major) hi/lo, and, when
+// b2 is given, W0^T -> B2 (N = 48 inputs, K = 64 hidden, K-major) hi/lo.
+__device__ void stage_w0(const FieldArgs& a, uint8_t* b1_hi, uint8_t* b1_lo, uint8_t* b2_hi,
+                         uint8_t* b2_lo) {
+  for (int e = threadIdx.x; e < kH * kN2; e += blockDim.x) {
+    const int j = e / kN2, c = e - j * kN2;
+    const int src = c < kK1 ? w0_col(c, a.g.L) : -1;
+    const float v = src >= 0 ? a.w0[j * a.din + src] : 0.0f;
+    uint32_t hi, lo;
+    tc::tf32_split(v, hi, lo);
+    if (c < kK1) {
+      const uint32_t o1 = tc::kmajor_offset(j, c, kK1);
+      *reinterpret_cast<uint32_t*>(b1_hi + o1) = hi;
+      *reinterpret_cast<uint32_t*>(b1_lo + o1) = lo;
+    }
+    if (b2_hi) {
+      const uint32_t o2 = tc::kmajor_offset(c, j, kH);
+      *reinterpret_cast<uint32_t*>(b2_hi + o2) = hi;
+      *reinterpret_cast<uint32_t*>(b2_lo + o2) = lo;
+    }
+  }
+}
+
+// Encoding of levels 4g..4g+3 of point x: e[2i + f] for level 4g + i.
+__device__ __forceinline__ void encode_group(const FieldArgs& a, int g, bool live, const float x[3],
+                                             float e[8]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int l = 4 * g + i;
+    float e0 = 0.0f, e1 = 0.0f;
+    if (live && l < a.active) encode_level(a.table, a.g, l, x, e0, e1);
+    e[2 * i] = e0;
+    e[2 * i + 1] = e1;
+  }
+}
+
+__device__ __forceinline__ void st_split8(uint32_t ta_hi, uint32_t ta_lo, const float v[8]) {
+  uint32_t hi[8], lo[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) tc::tf32_split(v[i], hi[i], lo[i]);
+  tc::tmem_st8(ta_hi, hi);
+  tc::tmem_st8(ta_lo, lo);
+}
+
+// Issues H = IN W0^T (3xTF32: in_hi w_hi + in_lo w_hi + in_hi w_lo), M=128, N=64, K=40.
+__device__ __forceinline__ void issue_mma1(uint32_t tbase, uint32_t s_b1_hi, uint32_t s_b1_lo) {
+  const uint32_t idesc = tc::idesc_tf32(kTile, kH);
+  const uint32_t sbo = (kK1 / 4) * 128u;
+  const uint32_t d = tc::taddr(tbase, 0, kColH);
+  for (int ks = 0; ks < kK1 / 8; ++ks)
+    tc::mma_ts(d, tc::taddr(tbase, 0, kColInHi + 8 * ks), tc::smem_desc(s_b1_hi + 256u * ks, 128u, sbo),
+               idesc, ks > 0);
+  for (int ks = 0; ks < kK1 / 8; ++ks)
+    tc::mma_ts(d, tc::taddr(tbase, 0, kColInLo + 8 * ks), tc::smem_desc(s_b1_hi + 256u * ks, 128u, sbo),
+               idesc, 1);
+  for (int ks = 0; ks < kK1 / 8; ++ks)
+    tc::mma_ts(d, tc::taddr(tbase, 0, kColInHi + 8 * ks), tc::smem_desc(s_b1_lo + 256u * ks, 128u, sbo),
+               idesc, 1);
+}
+
+// ---------------------------------------------------------------------------
+// forward
+// ---------------------------------------------------------------------------
+struct FwdSmem {
+  static constexpr uint32_t b1_hi = 0, b1_lo = 10240, w1 = 20480, b0 = 24576, b1 = 24832,
+                            part = 24896, bar = part + 4 * kTile * kDoutMax * 4, slot = bar + 8,
+                            end = slot + 8;
+};
+constexpr size_t kFwdSmemBytes = 80 * 1024;  // > 228/3 KB: at most two CTAs (2 x 256 TMEM columns) per SM
+static_assert(FwdSmem::end <= kFwdSmemBytes, "forward shared memory map");
+
+__global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) {
+  extern __shared__ __align__(1024) uint8_t sm[];
+  float* s_w1 = reinterpret_cast<float*>(sm + FwdSmem::w1);
+  float* s_b0 = reinterpret_cast<float*>(sm + FwdSmem::b0);
+  float* s_b1 = reinterpret_cast<float*>(sm + FwdSmem::b1);
+  float* s_part = reinterpret_cast<float*>(sm + FwdSmem::part);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + FwdSmem::bar);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + FwdSmem::slot);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int q = warp & 3, g = warp >> 2;
+  const int pt = 32 * q + lane;  // point within the tile == TMEM lane
+  const int oc = a.out_cols;
+
+  stage_w0(a, sm + FwdSmem::b1_hi, sm + FwdSmem::b1_lo, nullptr, nullptr);
+  for (int e = t; e < kDoutMax * kH; e += kThreads) s_w1[e] = e / kH < oc ? a.w1[e] : 0.0f;
+  if (t < kH) s_b0[t] = a.b0[t];
+  if (t < kDoutMax) s_b1[t] = t < oc ? a.b1[t] : 0.0f;
+  if (warp == 0) {
+    tc::tmem_alloc(slot, kCols);
+    tc::tmem_relinquish();
+  }
+  if (t == 0) tc::mbar_init(bar, 1);
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = *slot;
+  const uint32_t lb = (uint32_t)(32 * q);
+  const uint32_t s_b1_hi = tc::smem_u32(sm + FwdSmem::b1_hi), s_b1_lo = tc::smem_u32(sm + FwdSmem::b1_lo);
+  uint32_t phase = 0;
+  bool ok = true;
+
+  const int64_t n = effective_n(a);
+  const int64_t n_tiles = (n + kTile - 1) / kTile;
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int64_t p = tile * kTile + pt;
+    const bool live = p < n;
+    float x[3] = {0.0f, 0.0f, 0.0f};
+    if (live) {
+      x[0] = a.x[3 * p];
+      x[1] = a.x[3 * p + 1];
+      x[2] = a.x[3 * p + 2];
+    }
+    {
+      float e[8];
+      encode_group(a, g, live, x, e);
+      st_split8(tc::taddr(tbase, lb, kColInHi + 8 * g), tc::taddr(tbase, lb, kColInLo + 8 * g), e);
+      if (g == 0) {
+        const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        st_split8(tc::taddr(tbase, lb, kColInHi + kXCol), tc::taddr(tbase, lb, kColInLo + kXCol), xv);
+      }
+    }
+    tc::tmem_wait_st();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (t == 0) {
+      tc::fence_after_sync();
+      issue_mma1(tbase, s_b1_hi, s_b1_lo);
+      tc::mma_commit(bar);
+    }
+    const bool got = tc::mbar_wait_bounded(bar, phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(got)) {
+      ok = false;
+      break;
+    }
+    tc::fence_after_sync();
+    // hidden units 16g..16g+15 of this point -> partial outputs
+    float h[16];
+    tc::tmem_ld16(tc::taddr(tbase, lb, kColH + 16 * g), h);
+    tc::tmem_wait_ld();
+    float part[kDoutMax];
+#pragma unroll
+    for (int o = 0; o < kDoutMax; ++o) part[o] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int j = 16 * g + i;
+      const float act = softplus_fwd(h[i] + s_b0[j], a.beta, a.thresh);
+#pragma unroll
+      for (int o = 0; o < kDoutMax; ++o)
+        if (o < oc) part[o] = fmaf(s_w1[o * kH + j], act, part[o]);
+    }
+#pragma unroll
+    for (int o = 0; o < kDoutMax; ++o)
+      if (o < oc) s_part[(g * kTile + pt) * kDoutMax + o] = part[o];
+    tc::fence_before_sync();
+    __syncthreads();
+    if (g == 0 && live) {
+      for (int o = 0; o < oc; ++o) {
+        float s = s_b1[o];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) s += s_part[(m * kTile + pt) * kDoutMax + o];
+        a.out[p * oc + o] = s;
+      }
+    }
+    __syncthreads();
+  }
+  if (!ok) {
+    if (t == 0 && a.status) atomicOr(a.status, SN_STATUS_TIMEOUT);
+    (void)tc::mbar_wait_bounded(bar, phase ^ 1u);
+    __syncthreads();
+  }
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tbase, kCols);
+}
+
+// ---------------------------------------------------------------------------
+// backward
+// ---------------------------------------------------------------------------
+struct BwdSmem {
+  static constexpr uint32_t b1_hi = 0, b1_lo = 10240, b2_hi = 20480, b2_lo = 32768, a3 = 45056,
+                            b3_hi = 110592, b3_lo = 135168, w1 = 159744, b0 = 163840, dx = 164096,
+                            bar = dx + 4 * kTile * 3 * 4, slot = bar + 8, dw1 = slot + 8,
+                            db1 = dw1 + kDoutMax * kH * 4, end = db1 + kDoutMax * 4;
+};
+constexpr size_t kBwdSmemBytes = BwdSmem::end;
+static_assert(BwdSmem::end <= 227 * 1024, "backward shared memory map");
+
+__device__ __forceinline__ void st_smem_u32(uint8_t* base, uint32_t off, uint32_t v) {
+  *reinterpret_cast<uint32_t*>(base + off) = v;
+}
+
+// Second and third MMAs of the backward: dIN = dH W0 (3xTF32, M=128, N=48,
+// K=64) and dW0 += [dH_hi; dH_lo]^T-rows x IN^T (M=128, N=48, K=128 points).
+__device__ __forceinline__ void issue_mma23(uint32_t tbase, const uint8_t* sm, bool first_tile) {
+  const uint32_t s_b2_hi = tc::smem_u32(sm + BwdSmem::b2_hi), s_b2_lo = tc::smem_u32(sm + BwdSmem::b2_lo);
+  const uint32_t s_a3 = tc::smem_u32(sm + BwdSmem::a3);
+  const uint32_t s_b3_hi = tc::smem_u32(sm + BwdSmem::b3_hi), s_b3_lo = tc::smem_u32(sm + BwdSmem::b3_lo);
+  const uint32_t idesc = tc::idesc_tf32(kTile, kN2);
+  const uint32_t d2 = tc::taddr(tbase, 0, kColH);
+  const uint32_t sbo2 = (kH / 4) * 128u;
+  for (int ks = 0; ks < kH / 8; ++ks)
+    tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhHi + 8 * ks), tc::smem_desc(s_b2_hi + 256u * ks, 128u, sbo2),
+               idesc, ks > 0);
+  for (int ks = 0; ks < kH / 8; ++ks)
+    tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhLo + 8 * ks), tc::smem_desc(s_b2_hi + 256u * ks, 128u, sbo2),
+               idesc, 1);
+  for (int ks = 0; ks < kH / 8; ++ks)
+    tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhHi + 8 * ks), tc::smem_desc(s_b2_lo + 256u * ks, 128u, sbo2),
+               idesc, 1);
+  const uint32_t d3 = tc::taddr(tbase, 0, kColDw0);
+  const uint32_t sbo3 = (kTile / 4) * 128u;
+  for (int ks = 0; ks < kTile / 8; ++ks) {
+    tc::mma_ss(d3, tc::smem_desc(s_a3 + 256u * ks, 128u, sbo3), tc::smem_desc(s_b3_hi + 256u * ks, 128u, sbo3),
+               idesc, (first_tile && ks == 0) ? 0u : 1u);
+    tc::mma_ss(d3, tc::smem_desc(s_a3 + 256u * ks, 128u, sbo3), tc::smem_desc(s_b3_lo + 256u * ks, 128u, sbo3),
+               idesc, 1);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) {
+  extern __shared__ __align__(1024) uint8_t sm[];
+  float* s_w1 = reinterpret_cast<float*>(sm + BwdSmem::w1);
+  float* s_b0 = reinterpret_cast<float*>(sm + BwdSmem::b0);
+  float* s_dx = reinterpret_cast<float*>(sm + BwdSmem::dx);
+  uint8_t* a3 = sm + BwdSmem::a3;
+  uint8_t* b3_hi = sm + BwdSmem::b3_hi;
+  uint8_t* b3_lo = sm + BwdSmem::b3_lo;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + BwdSmem::bar);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + BwdSmem::slot);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int q = warp & 3, g = warp >> 2;
+  const int pt = 32 * q + lane;
+  const int oc = a.out_cols;
+  const bool want_table = a.grad_table != nullptr;
+  const bool want_x = a.grad_x != nullptr;
+
+  stage_w0(a, sm + BwdSmem::b1_hi, sm + BwdSmem::b1_lo, sm + BwdSmem::b2_hi, sm + BwdSmem::b2_lo);
+  for (int e = t; e < kDoutMax * kH; e += kThreads) s_w1[e] = e / kH < oc ? a.w1[e] : 0.0f;
+  if (t < kH) s_b0[t] = a.b0[t];
+  float* s_dw1 = reinterpret_cast<float*>(sm + BwdSmem::dw1);
+  float* s_db1 = reinterpret_cast<float*>(sm + BwdSmem::db1);
+  for (int e = t; e < kDoutMax * kH; e += kThreads) s_dw1[e] = 0.0f;
+  if (t < kDoutMax) s_db1[t] = 0.0f;
+  // constant rows of IN^T: ones (hi) at kOnesRow, zeros above it
+  for (int e = t; e < (kN2 - kOnesRow) * kTile; e += kThreads) {
+    const int r = kOnesRow + e / kTile, c = e % kTile;
+    const uint32_t off = tc::kmajor_offset(r, c, kTile);
+    st_smem_u32(b3_hi, off, r == kOnesRow ? __float_as_uint(1.0f) : 0u);
+    st_smem_u32(b3_lo, off, 0u);
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(slot, kCols);
+    tc::tmem_relinquish();
+  }
+  if (t == 0) tc::mbar_init(bar, 1);
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = *slot;
+  const uint32_t lb = (uint32_t)(32 * q);
+  const uint32_t s_b1_hi = tc::smem_u32(sm + BwdSmem::b1_hi), s_b1_lo = tc::smem_u32(sm + BwdSmem::b1_lo);
+  uint32_t phase = 0;
+  bool ok = true, first = true;
+
+  const int64_t n = effective_n(a);
+  const int64_t n_tiles = (n + kTile - 1) / kTile;
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int64_t p = tile * kTile + pt;
+    const bool live = p < n;
+    float x[3] = {0.0f, 0.0f, 0.0f};
+    if (live) {
+      x[0] = a.x[3 * p];
+      x[1] = a.x[3 * p + 1];
+      x[2] = a.x[3 * p + 2];
+    }
+    // ---- input rows: TMEM (A of the first MMA) and IN^T (B of the third) ----
+    {
+      float e[8];
+      encode_group(a, g, live, x, e);
+      st_split8(tc::taddr(tbase, lb, kColInHi + 8 * g), tc::taddr(tbase, lb, kColInLo + 8 * g), e);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        uint32_t hi, lo;
+        tc::tf32_split(e[i], hi, lo);
+        const uint32_t off = tc::kmajor_offset(8 * g + i, pt, kTile);
+        st_smem_u32(b3_hi, off, hi);
+        st_smem_u32(b3_lo, off, lo);
+      }
+      if (g == 0) {
+        const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        st_split8(tc::taddr(tbase, lb, kColInHi + kXCol), tc::taddr(tbase, lb, kColInLo + kXCol), xv);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          uint32_t hi, lo;
+          tc::tf32_split(x[d], hi, lo);
+          const uint32_t off = tc::kmajor_offset(kXCol + d, pt, kTile);
+          st_smem_u32(b3_hi, off, hi);
+          st_smem_u32(b3_lo, off, lo);
+        }
+      }
+    }
+    tc::tmem_wait_st();
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (t == 0) {
+      tc::fence_after_sync();
+      issue_mma1(tbase, s_b1_hi, s_b1_lo);
+      tc::mma_commit(bar);
+    }
+    bool got = tc::mbar_wait_bounded(bar, phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(got)) {
+      ok = false;
+      break;
+    }
+    tc::fence_after_sync();
+    // ---- dH for hidden units 16g..16g+15 ----
+    {
+      float h[16];
+      tc::tmem_ld16(tc::taddr(tbase, lb, kColH + 16 * g), h);
+      tc::tmem_wait_ld();
+      float go[kDoutMax];
+#pragma unroll
+      for (int o = 0; o < kDoutMax; ++o) go[o] = (live && o < oc) ? a.grad_out[p * oc + o] : 0.0f;
+      float dh[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int j = 16 * g + i;
+        const float pre = h[i] + s_b0[j];
+        const float act = softplus_fwd(pre, a.beta, a.thresh);
+        const float sg = softplus_grad(pre, a.beta, a.thresh);
+        float da = 0.0f;
+#pragma unroll
+        for (int o = 0; o < kDoutMax; ++o)
+          if (o < oc) da = fmaf(go[o], s_w1[o * kH + j], da);
+        dh[i] = live ? da * sg : 0.0f;
+        // dW1[o][j] += sum over the warp's points of g_o * act_j
+#pragma unroll
+        for (int o = 0; o < kDoutMax; ++o) {
+          if (o < oc) {
+            float v = live ? go[o] * act : 0.0f;
+#pragma unroll
+            for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+            if (lane == 0) atomicAdd(s_dw1 + o * kH + j, v);
+          }
+        }
+      }
+      if (g == 0) {
+#pragma unroll
+        for (int o = 0; o < kDoutMax; ++o) {
+          if (o < oc) {
+            float v = go[o];
+#pragma unroll
+            for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+            if (lane == 0) atomicAdd(s_db1 + o, v);
+          }
+        }
+      }
+      st_split8(tc::taddr(tbase, lb, kColDhHi + 16 * g), tc::taddr(tbase, lb, kColDhLo + 16 * g), dh);
+      st_split8(tc::taddr(tbase, lb, kColDhHi + 16 * g + 8), tc::taddr(tbase, lb, kColDhLo + 16 * g + 8),
+                dh + 8);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        uint32_t hi, lo;
+        tc::tf32_split(dh[i], hi, lo);
+        st_smem_u32(a3, tc::kmajor_offset(16 * g + i, pt, kTile), hi);
+        st_smem_u32(a3, tc::kmajor_offset(kH + 16 * g + i, pt, kTile), lo);
+      }
+    }
+    tc::tmem_wait_st();
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (t == 0) {
+      tc::fence_after_sync();
+      issue_mma23(tbase, sm, first);
+      tc::mma_commit(bar);
+    }
+    first = false;
+    got = tc::mbar_wait_bounded(bar, phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(got)) {
+      ok = false;
+      break;
+    }
+    tc::fence_after_sync();
+    // ---- dIN: table-gradient scatter for levels 4g..4g+3, dL/dx ----
+    {
+      float din[8];
+      tc::tmem_ld8(tc::taddr(tbase, lb, kColH + 8 * g), din);
+      tc::tmem_wait_ld();
+      float dxl[8];
+      if (g == 0) {
+        tc::tmem_ld8(tc::taddr(tbase, lb, kColH + kXCol), dxl);
+        tc::tmem_wait_ld();
+      }
+      float dx[3] = {0.0f, 0.0f, 0.0f};
+      if (g == 0) {
+        dx[0] = dxl[0];
+        dx[1] = dxl[1];
+        dx[2] = dxl[2];
+      }
+      float2* gt2 = reinterpret_cast<float2*>(a.grad_table);
+      const float2* t2 = reinterpret_cast<const float2*>(a.table);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int l = 4 * g + i;
+        if (l < a.active) {
+          LevelCorners c;
+          level_corners(a.g, l, x, c);
+          const float d0 = live ? din[2 * i] : 0.0f, d1 = live ? din[2 * i + 1] : 0.0f;
+          if (want_table) {
+            if (warp_same_cell(c)) {
+#pragma unroll
+              for (int k = 0; k < 8; ++k) {
+                float v0 = c.w[k] * d0, v1 = c.w[k] * d1;
+#pragma unroll
+                for (int s = 16; s > 0; s >>= 1) {
+                  v0 += __shfl_xor_sync(0xffffffffu, v0, s);
+                  v1 += __shfl_xor_sync(0xffffffffu, v1, s);
+                }
+                if (lane == k) atomicAdd(gt2 + c.idx[k], make_float2(v0, v1));
+              }
+            } else if (live) {
+#pragma unroll
+              for (int k = 0; k < 8; ++k) atomicAdd(gt2 + c.idx[k], make_float2(c.w[k] * d0, c.w[k] * d1));
+            }
+          }
+          if (want_x && live) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              const float2 v = __ldg(t2 + c.idx[k]);
+              const float gv = d0 * v.x + d1 * v.y;
+#pragma unroll
+              for (int d = 0; d < 3; ++d) dx[d] = fmaf(gv, corner_dw(c, k, d, a.g.scale[l]), dx[d]);
+            }
+          }
+        }
+      }
+      if (want_x) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) s_dx[(g * kTile + pt) * 3 + d] = dx[d];
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (want_x && g == 0 && live) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        float s = 0.0f;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) s += s_dx[(m * kTile + pt) * 3 + d];
+        a.grad_x[3 * p + d] = s;
+      }
+    }
+  }
+  if (!ok) {
+    if (t == 0 && a.status) atomicOr(a.status, SN_STATUS_TIMEOUT);
+    (void)tc::mbar_wait_bounded(bar, phase ^ 1u);
+  }
+  __syncthreads();
+  tc::fence_after_sync();
+  if (ok && !first) {
+    // dW0 / db0: lanes 0..63 hold the dH_hi rows, 64..127 the dH_lo rows
+    if (g == 0) {
+      const int j = pt & (kH - 1);
+#pragma unroll
+      for (int c0 = 0; c0 < kN2; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tc::taddr(tbase, lb, kColDw0 + c0), v);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int c = c0 + i;
+          if (c == kOnesRow) {
+            if (a.grad_b0) atomicAdd(a.grad_b0 + j, v[i]);
+          } else if (c < kK1 && a.grad_w0) {
+            const int col = w0_col(c, a.g.L);
+            if (col >= 0 && v[i] != 0.0f) atomicAdd(a.grad_w0 + j * a.din + col, v[i]);
+          }
+        }
+      }
+    }
+    // dW1 / db1 (block sums in shared memory)
+    if (a.grad_w1)
+      for (int e = t; e < oc * kH; e += kThreads)
+        if (s_dw1[e] != 0.0f) atomicAdd(a.grad_w1 + e, s_dw1[e]);
+    if (a.grad_b1 && t < oc && s_db1[t] != 0.0f) atomicAdd(a.grad_b1 + t, s_db1[t]);
+  }
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tbase, kCols);
+}
+
+int set_smem(const void* fn, size_t bytes, const char* what) {
+  const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) {
+    set_error("%s: cannot set shared memory limit: %s", what, cudaGetErrorString(e));
+    return SN_ERR_CUDA;
+  }
+  return SN_OK;
+}
+
+}  // namespace
+
+// Launchers used by sn_field_fwd / sn_field_bwd (field.cu).
+int field_fwd_tc(const FieldArgs& a, cudaStream_t st) {
+  SN_TRY(set_smem(reinterpret_cast<const void*>(field_fwd_tc_kernel), kFwdSmemBytes, "field_fwd"));
+  const int64_t n_tiles = (a.cap + kTile - 1) / kTile;
+  const int64_t cap = 2LL * num_sms();
+  const int64_t grid = n_tiles < cap ? n_tiles : cap;
+  field_fwd_tc_kernel<<<(unsigned)grid, kThreads, kFwdSmemBytes, st>>>(a);
+  return check_launch("field_fwd");
+}
+
+int field_bwd_tc(const FieldArgs& a, cudaStream_t st) {
+  SN_TRY(set_smem(reinterpret_cast<const void*>(field_bwd_tc_kernel), kBwdSmemBytes, "field_bwd"));
+  const int64_t n_tiles = (a.cap + kTile - 1) / kTile;
+  const int64_t cap = num_sms();
+  const int64_t grid = n_tiles < cap ? n_tiles : cap;
+  field_bwd_tc_kernel<<<(unsigned)grid, kThreads, kBwdSmemBytes, st>>>(a);
+  return check_launch("field_bwd");
+}
+
+}  // namespace sn

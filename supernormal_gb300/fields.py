@@ -19,7 +19,7 @@ import torch
 import torch.nn as nn
 from torch import Tensor
 
-from ._lib import GridDesc, MlpDesc, call, lib, stream_handle
+from ._lib import SN_STATUS_TIMEOUT, GridDesc, MlpDesc, call, lib, stream_handle
 
 __all__ = ["HashGridEncoding", "WeightNormLinear", "SDFNetwork", "SingleVarianceNetwork",
            "grid_desc"]
@@ -275,6 +275,8 @@ class SDFNetwork(nn.Module):
                     torch.nn.init.normal_(lin.weight, 0.0, np.sqrt(2) / np.sqrt(out_dim))
             setattr(self, "lin" + str(l), WeightNormLinear(lin, weight_norm))
         self.beta, self.threshold = 100.0, 20.0
+        # device status word of the tensor-core field kernels (not in the state_dict)
+        self.register_buffer("_kernel_status", torch.zeros(1, dtype=torch.int32), persistent=False)
         self._supported = (n_layers == 1 and d_hidden == 64 and input_concat and d_in == 3
                            and self.encoding.n_features_per_level == 2
                            and self.encoding.n_levels <= 16 and 1 <= d_out <= 16)
@@ -301,7 +303,13 @@ class SDFNetwork(nn.Module):
         d.beta = self.beta
         d.threshold = self.threshold
         d.w0, d.b0, d.w1, d.b1 = w0.data_ptr(), b0.data_ptr(), w1.data_ptr(), b1.data_ptr()
+        d.status = self._kernel_status.data_ptr()
         return d
+
+    def check_status(self) -> None:
+        """Raise if a field kernel reported a failed bounded wait (host sync)."""
+        if int(self._kernel_status.item()) & SN_STATUS_TIMEOUT:
+            raise RuntimeError("a tensor-core field kernel timed out waiting for its MMAs")
 
     def mlp_tensors(self):
         return (self.lin0.effective_weight(), self.lin0.bias, self.lin1.effective_weight(),

@@ -21,7 +21,7 @@ from typing import Optional
 import torch
 from torch import Tensor
 
-from ._lib import SN_STATUS_CAPACITY, SN_STATUS_MARCH_LIMIT, call, stream_handle
+from ._lib import SN_STATUS_CAPACITY, SN_STATUS_MARCH_LIMIT, SN_STATUS_TIMEOUT, call, stream_handle
 from .fields import SDFNetwork, SingleVarianceNetwork
 
 __all__ = ["TrainConfig", "FusedTrainer"]
@@ -210,6 +210,7 @@ class FusedTrainer:
 
     def _mlp(self):
         d = self.net._mlp_desc(self.w0, self.views["b0"], self.w1, self.views["b1"])
+        d.status = self.status.data_ptr()
         return d
 
     def step_size(self, it: int) -> float:
@@ -378,6 +379,8 @@ class FusedTrainer:
             raise RuntimeError("marching iteration limit hit")
         if v & SN_STATUS_CAPACITY:
             raise RuntimeError("sample capacity exceeded")
+        if v & SN_STATUS_TIMEOUT:
+            raise RuntimeError("a tensor-core field kernel timed out waiting for its MMAs")
 
 
 def _center_ptr(t: Tensor, kc: int) -> int:
