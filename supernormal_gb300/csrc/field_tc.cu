@@ -35,6 +35,10 @@ constexpr int kN2 = 48;        // dIN columns (N of the second MMA; 35 used)
 constexpr int kXCol = 32;      // first column of x in the permuted input
 constexpr int kOnesRow = 35;   // row of ones in IN^T (gives db0)
 constexpr uint32_t kCols = 256;
+// IN^T and [dH_hi; dH_lo] (K = the tile's points, written one point per
+// thread): core matrices 144 bytes apart along K so a warp's 32 stores of one
+// row fall in 32 banks.
+constexpr uint32_t kLboP = 144, kSboP = (kTile / 4) * kLboP;
 
 // TMEM column map (both kernels): H / dIN share [0, 64); the input rows
 // (hi, lo) and later dH (hi, lo) share [64, 192); dW0 accumulates in [192, 240).
@@ -119,7 +123,10 @@ struct FwdSmem {
 constexpr size_t kFwdSmemBytes = 80 * 1024;  // > 228/3 KB: at most two CTAs (2 x 256 TMEM columns) per SM
 static_assert(FwdSmem::end <= kFwdSmemBytes, "forward shared memory map");
 
+// ONE: a single output column (the sdf; every training call), else up to kDoutMax.
+template <bool ONE>
 __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) {
+  constexpr int kOc = ONE ? 1 : kDoutMax;
   extern __shared__ __align__(1024) uint8_t sm[];
   float* s_w1 = reinterpret_cast<float*>(sm + FwdSmem::w1);
   float* s_b0 = reinterpret_cast<float*>(sm + FwdSmem::b0);
@@ -190,19 +197,19 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
     float h[16];
     tc::tmem_ld16(tc::taddr(tbase, lb, kColH + 16 * g), h);
     tc::tmem_wait_ld();
-    float part[kDoutMax];
+    float part[kOc];
 #pragma unroll
-    for (int o = 0; o < kDoutMax; ++o) part[o] = 0.0f;
+    for (int o = 0; o < kOc; ++o) part[o] = 0.0f;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
       const int j = 16 * g + i;
       const float act = softplus_fwd(h[i] + s_b0[j], a.beta, a.thresh);
 #pragma unroll
-      for (int o = 0; o < kDoutMax; ++o)
+      for (int o = 0; o < kOc; ++o)
         if (o < oc) part[o] = fmaf(s_w1[o * kH + j], act, part[o]);
     }
 #pragma unroll
-    for (int o = 0; o < kDoutMax; ++o)
+    for (int o = 0; o < kOc; ++o)
       if (o < oc) s_part[(g * kTile + pt) * kDoutMax + o] = part[o];
     tc::fence_before_sync();
     __syncthreads();
@@ -230,9 +237,10 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
 // ---------------------------------------------------------------------------
 struct BwdSmem {
   static constexpr uint32_t b1_hi = 0, b1_lo = 10240, b2_hi = 20480, b2_lo = 32768, a3 = 45056,
-                            b3_hi = 110592, b3_lo = 135168, w1 = 159744, b0 = 163840, dx = 164096,
-                            bar = dx + 4 * kTile * 3 * 4, slot = bar + 8, dw1 = slot + 8,
-                            db1 = dw1 + kDoutMax * kH * 4, end = db1 + kDoutMax * 4;
+                            b3_hi = a3 + 16 * kSboP, b3_lo = b3_hi + 6 * kSboP, w1 = b3_lo + 6 * kSboP,
+                            b0 = w1 + kDoutMax * kH * 4, dx = b0 + kH * 4, bar = dx + 4 * kTile * 3 * 4,
+                            slot = bar + 8, dw1 = slot + 8, db1 = dw1 + kDoutMax * kH * 4,
+                            end = db1 + kDoutMax * 4;
 };
 constexpr size_t kBwdSmemBytes = BwdSmem::end;
 static_assert(BwdSmem::end <= 227 * 1024, "backward shared memory map");
@@ -260,16 +268,17 @@ __device__ __forceinline__ void issue_mma23(uint32_t tbase, const uint8_t* sm, b
     tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhHi + 8 * ks), tc::smem_desc(s_b2_lo + 256u * ks, 128u, sbo2),
                idesc, 1);
   const uint32_t d3 = tc::taddr(tbase, 0, kColDw0);
-  const uint32_t sbo3 = (kTile / 4) * 128u;
   for (int ks = 0; ks < kTile / 8; ++ks) {
-    tc::mma_ss(d3, tc::smem_desc(s_a3 + 256u * ks, 128u, sbo3), tc::smem_desc(s_b3_hi + 256u * ks, 128u, sbo3),
-               idesc, (first_tile && ks == 0) ? 0u : 1u);
-    tc::mma_ss(d3, tc::smem_desc(s_a3 + 256u * ks, 128u, sbo3), tc::smem_desc(s_b3_lo + 256u * ks, 128u, sbo3),
-               idesc, 1);
+    const uint32_t k0 = 2u * kLboP * ks;
+    tc::mma_ss(d3, tc::smem_desc(s_a3 + k0, kLboP, kSboP), tc::smem_desc(s_b3_hi + k0, kLboP, kSboP), idesc,
+               (first_tile && ks == 0) ? 0u : 1u);
+    tc::mma_ss(d3, tc::smem_desc(s_a3 + k0, kLboP, kSboP), tc::smem_desc(s_b3_lo + k0, kLboP, kSboP), idesc, 1);
   }
 }
 
+template <bool ONE>
 __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) {
+  constexpr int kOc = ONE ? 1 : kDoutMax;
   extern __shared__ __align__(1024) uint8_t sm[];
   float* s_w1 = reinterpret_cast<float*>(sm + BwdSmem::w1);
   float* s_b0 = reinterpret_cast<float*>(sm + BwdSmem::b0);
@@ -296,7 +305,7 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
   // constant rows of IN^T: ones (hi) at kOnesRow, zeros above it
   for (int e = t; e < (kN2 - kOnesRow) * kTile; e += kThreads) {
     const int r = kOnesRow + e / kTile, c = e % kTile;
-    const uint32_t off = tc::kmajor_offset(r, c, kTile);
+    const uint32_t off = tc::kmajor_offset_strided(r, c, kLboP, kSboP);
     st_smem_u32(b3_hi, off, r == kOnesRow ? __float_as_uint(1.0f) : 0u);
     st_smem_u32(b3_lo, off, 0u);
   }
@@ -335,7 +344,7 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       for (int i = 0; i < 8; ++i) {
         uint32_t hi, lo;
         tc::tf32_split(e[i], hi, lo);
-        const uint32_t off = tc::kmajor_offset(8 * g + i, pt, kTile);
+        const uint32_t off = tc::kmajor_offset_strided(8 * g + i, pt, kLboP, kSboP);
         st_smem_u32(b3_hi, off, hi);
         st_smem_u32(b3_lo, off, lo);
       }
@@ -346,7 +355,7 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
         for (int d = 0; d < 3; ++d) {
           uint32_t hi, lo;
           tc::tf32_split(x[d], hi, lo);
-          const uint32_t off = tc::kmajor_offset(kXCol + d, pt, kTile);
+          const uint32_t off = tc::kmajor_offset_strided(kXCol + d, pt, kLboP, kSboP);
           st_smem_u32(b3_hi, off, hi);
           st_smem_u32(b3_lo, off, lo);
         }
@@ -373,9 +382,9 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       float h[16];
       tc::tmem_ld16(tc::taddr(tbase, lb, kColH + 16 * g), h);
       tc::tmem_wait_ld();
-      float go[kDoutMax];
+      float go[kOc];
 #pragma unroll
-      for (int o = 0; o < kDoutMax; ++o) go[o] = (live && o < oc) ? a.grad_out[p * oc + o] : 0.0f;
+      for (int o = 0; o < kOc; ++o) go[o] = (live && o < oc) ? a.grad_out[p * oc + o] : 0.0f;
       float dh[16];
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
@@ -385,12 +394,12 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
         const float sg = softplus_grad(pre, a.beta, a.thresh);
         float da = 0.0f;
 #pragma unroll
-        for (int o = 0; o < kDoutMax; ++o)
+        for (int o = 0; o < kOc; ++o)
           if (o < oc) da = fmaf(go[o], s_w1[o * kH + j], da);
         dh[i] = live ? da * sg : 0.0f;
         // dW1[o][j] += sum over the warp's points of g_o * act_j
 #pragma unroll
-        for (int o = 0; o < kDoutMax; ++o) {
+        for (int o = 0; o < kOc; ++o) {
           if (o < oc) {
             float v = live ? go[o] * act : 0.0f;
 #pragma unroll
@@ -401,7 +410,7 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       }
       if (g == 0) {
 #pragma unroll
-        for (int o = 0; o < kDoutMax; ++o) {
+        for (int o = 0; o < kOc; ++o) {
           if (o < oc) {
             float v = go[o];
 #pragma unroll
@@ -417,8 +426,8 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       for (int i = 0; i < 16; ++i) {
         uint32_t hi, lo;
         tc::tf32_split(dh[i], hi, lo);
-        st_smem_u32(a3, tc::kmajor_offset(16 * g + i, pt, kTile), hi);
-        st_smem_u32(a3, tc::kmajor_offset(kH + 16 * g + i, pt, kTile), lo);
+        st_smem_u32(a3, tc::kmajor_offset_strided(16 * g + i, pt, kLboP, kSboP), hi);
+        st_smem_u32(a3, tc::kmajor_offset_strided(kH + 16 * g + i, pt, kLboP, kSboP), lo);
       }
     }
     tc::tmem_wait_st();
@@ -496,16 +505,19 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
         for (int d = 0; d < 3; ++d) s_dx[(g * kTile + pt) * 3 + d] = dx[d];
       }
     }
-    tc::fence_before_sync();
-    __syncthreads();
-    if (want_x && g == 0 && live) {
+    // (the next tile's first barrier orders these TMEM reads before its MMAs)
+    if (want_x) {
+      __syncthreads();
+      if (g == 0 && live) {
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        float s = 0.0f;
+        for (int d = 0; d < 3; ++d) {
+          float s = 0.0f;
 #pragma unroll
-        for (int m = 0; m < 4; ++m) s += s_dx[(m * kTile + pt) * 3 + d];
-        a.grad_x[3 * p + d] = s;
+          for (int m = 0; m < 4; ++m) s += s_dx[(m * kTile + pt) * 3 + d];
+          a.grad_x[3 * p + d] = s;
+        }
       }
+      __syncthreads();
     }
   }
   if (!ok) {
@@ -559,20 +571,30 @@ int set_smem(const void* fn, size_t bytes, const char* what) {
 
 // Launchers used by sn_field_fwd / sn_field_bwd (field.cu).
 int field_fwd_tc(const FieldArgs& a, cudaStream_t st) {
-  SN_TRY(set_smem(reinterpret_cast<const void*>(field_fwd_tc_kernel), kFwdSmemBytes, "field_fwd"));
+  const void* fn = a.out_cols == 1 ? reinterpret_cast<const void*>(field_fwd_tc_kernel<true>)
+                                   : reinterpret_cast<const void*>(field_fwd_tc_kernel<false>);
+  SN_TRY(set_smem(fn, kFwdSmemBytes, "field_fwd"));
   const int64_t n_tiles = (a.cap + kTile - 1) / kTile;
   const int64_t cap = 2LL * num_sms();
-  const int64_t grid = n_tiles < cap ? n_tiles : cap;
-  field_fwd_tc_kernel<<<(unsigned)grid, kThreads, kFwdSmemBytes, st>>>(a);
+  const unsigned grid = (unsigned)(n_tiles < cap ? n_tiles : cap);
+  if (a.out_cols == 1)
+    field_fwd_tc_kernel<true><<<grid, kThreads, kFwdSmemBytes, st>>>(a);
+  else
+    field_fwd_tc_kernel<false><<<grid, kThreads, kFwdSmemBytes, st>>>(a);
   return check_launch("field_fwd");
 }
 
 int field_bwd_tc(const FieldArgs& a, cudaStream_t st) {
-  SN_TRY(set_smem(reinterpret_cast<const void*>(field_bwd_tc_kernel), kBwdSmemBytes, "field_bwd"));
+  const void* fn = a.out_cols == 1 ? reinterpret_cast<const void*>(field_bwd_tc_kernel<true>)
+                                   : reinterpret_cast<const void*>(field_bwd_tc_kernel<false>);
+  SN_TRY(set_smem(fn, kBwdSmemBytes, "field_bwd"));
   const int64_t n_tiles = (a.cap + kTile - 1) / kTile;
   const int64_t cap = num_sms();
-  const int64_t grid = n_tiles < cap ? n_tiles : cap;
-  field_bwd_tc_kernel<<<(unsigned)grid, kThreads, kBwdSmemBytes, st>>>(a);
+  const unsigned grid = (unsigned)(n_tiles < cap ? n_tiles : cap);
+  if (a.out_cols == 1)
+    field_bwd_tc_kernel<true><<<grid, kThreads, kBwdSmemBytes, st>>>(a);
+  else
+    field_bwd_tc_kernel<false><<<grid, kThreads, kBwdSmemBytes, st>>>(a);
   return check_launch("field_bwd");
 }
 

@@ -151,6 +151,14 @@ __host__ __device__ constexpr uint32_t kmajor_offset(uint32_t row, uint32_t k, u
   return (row >> 3) * (kdim / 4) * 128u + (k >> 2) * 128u + (row & 7u) * 16u + (k & 3u) * 4u;
 }
 
+// Same layout with free strides: lbo between K-adjacent core matrices, sbo
+// between 8-row groups (lbo = 144 puts the 16-byte rows of 32 consecutive K
+// positions in 32 different banks when each thread writes one K position).
+__host__ __device__ constexpr uint32_t kmajor_offset_strided(uint32_t row, uint32_t k, uint32_t lbo,
+                                                             uint32_t sbo) {
+  return (row >> 3) * sbo + (k >> 2) * lbo + (row & 7u) * 16u + (k & 3u) * 4u;
+}
+
 // D[tmem] (+)= A[tmem] * B[smem]^T, one K = 8 step; issued by one thread.
 __device__ __forceinline__ void mma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
                                        uint32_t accumulate) {
