@@ -104,6 +104,19 @@ __device__ __forceinline__ float softplus_grad(float x, float beta, float thresh
   float z = expf(bx);
   return z / (z + 1.0f);
 }
+// Both at once (one exponential); the same values as the two functions above.
+__device__ __forceinline__ void softplus_fwd_grad(float x, float beta, float threshold, float& y,
+                                                  float& dy) {
+  const float bx = x * beta;
+  if (bx > threshold) {
+    y = x;
+    dy = 1.0f;
+    return;
+  }
+  const float z = expf(bx);
+  y = log1pf(z) / beta;
+  dy = z / (z + 1.0f);
+}
 __device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + expf(-x)); }
 
 }  // namespace sn

@@ -76,241 +76,10 @@ __device__ __forceinline__ float hidden_pre(const float* s_w0, const float* s_b0
   return h;
 }
 
-__global__ void __launch_bounds__(128) field_fwd_kernel(FieldArgs a) {
-  extern __shared__ float4 smem4[];
-  float* s_w0 = reinterpret_cast<float*>(smem4);
-  float* s_b0 = s_w0 + kH * kDinPad;
-  float* s_w1 = s_b0 + kH;
-  float* s_b1 = s_w1 + kDoutMax * kH;
-  load_mlp(a, s_w0, s_b0, s_w1, s_b1);
-  __syncthreads();
-  const int64_t n = effective_n(a);
-  const int n_in4 = (3 + 2 * a.active + 3) / 4;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    float in[kDinPad];
-    build_input(a, p, in);
-    float out[kDoutMax];
-#pragma unroll
-    for (int o = 0; o < kDoutMax; ++o) out[o] = s_b1[o];
-#pragma unroll 4
-    for (int j = 0; j < kH; ++j) {
-      const float h = hidden_pre(s_w0, s_b0, j, in, n_in4);
-      const float act = softplus_fwd(h, a.beta, a.thresh);
-#pragma unroll
-      for (int o = 0; o < kDoutMax; ++o)
-        if (o < a.out_cols) out[o] = fmaf(s_w1[o * kH + j], act, out[o]);
-    }
-#pragma unroll
-    for (int o = 0; o < kDoutMax; ++o)
-      if (o < a.out_cols) a.out[p * a.out_cols + o] = out[o];
-  }
-}
-
-// Backward with recomputation: per 128-point batch, each thread rebuilds its
-// point's encoding and hidden layer, forms dL/dh and dL/denc, scatters the
-// table gradient with float2 atomics, and stages (in, dh, act, g) in shared
-// memory; the block then reduces the weight gradients over the batch with
-// thread-owned accumulators, flushed to global memory once per block.
+// Shared by the SIMT kernels of SDFNetwork.gradient below.
 constexpr int kBwdThreads = 128;
 
-__global__ void __launch_bounds__(kBwdThreads) field_bwd_kernel(FieldArgs a) {
-  extern __shared__ float4 smem4[];
-  float* s_w0 = reinterpret_cast<float*>(smem4);
-  float* s_b0 = s_w0 + kH * kDinPad;
-  float* s_w1 = s_b0 + kH;
-  float* s_b1 = s_w1 + kDoutMax * kH;
-  float* s_in = s_b1 + kDoutMax;                  // [128][kDinPad]
-  float* s_dh = s_in + kBwdThreads * kDinPad;     // [128][64]
-  float* s_act = s_dh + kBwdThreads * kH;         // [128][64]
-  float* s_g = s_act + kBwdThreads * kH;          // [128][kDoutMax]
-  load_mlp(a, s_w0, s_b0, s_w1, s_b1);
-  __syncthreads();
-
-  const int64_t n = effective_n(a);
-  const int n_in4 = (3 + 2 * a.active + 3) / 4;
-  const int din_used = 3 + 2 * a.active;
-  const int t = threadIdx.x;
-  const int lane = t & 31;
-  // register tile of the weight-gradient reduction: rows 4*rg..4*rg+3 of the
-  // hidden layer, input columns cg + 8m (m < 5) and outputs cg + 8m (m < 2)
-  const int rg = t >> 3, cg = t & 7;
-  float acc_w0[4][5];
-  float acc_w1[4][2];
-  float acc_b0[4];
-  float acc_b1 = 0.0f;
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    acc_b0[r] = 0.0f;
-#pragma unroll
-    for (int m = 0; m < 5; ++m) acc_w0[r][m] = 0.0f;
-#pragma unroll
-    for (int m = 0; m < 2; ++m) acc_w1[r][m] = 0.0f;
-  }
-
-  const int64_t stride = (int64_t)gridDim.x * kBwdThreads;
-  for (int64_t b0 = (int64_t)blockIdx.x * kBwdThreads; b0 < n; b0 += stride) {
-    const int64_t p = b0 + t;
-    const bool live = p < n;
-    // ---- phase 1: recompute forward, dL/dh, dL/denc ----
-    float in[kDinPad];
-    float g[kDoutMax];
-    if (live) {
-      build_input(a, p, in);
-#pragma unroll
-      for (int o = 0; o < kDoutMax; ++o) g[o] = o < a.out_cols ? a.grad_out[p * a.out_cols + o] : 0.0f;
-    } else {
-#pragma unroll
-      for (int i = 0; i < kDinPad; ++i) in[i] = 0.0f;
-#pragma unroll
-      for (int o = 0; o < kDoutMax; ++o) g[o] = 0.0f;
-    }
-    float denc[2 * kMaxL + 3];  // [0..2] = dL/dx from the linear part
-#pragma unroll
-    for (int i = 0; i < 2 * kMaxL + 3; ++i) denc[i] = 0.0f;
-#pragma unroll 2
-    for (int j = 0; j < kH; ++j) {
-      const float h = hidden_pre(s_w0, s_b0, j, in, n_in4);
-      const float act = softplus_fwd(h, a.beta, a.thresh);
-      const float sg = softplus_grad(h, a.beta, a.thresh);
-      float da = 0.0f;
-#pragma unroll
-      for (int o = 0; o < kDoutMax; ++o) da = fmaf(g[o], s_w1[o * kH + j], da);
-      const float dh = da * sg;
-      s_dh[t * kH + j] = dh;
-      s_act[t * kH + j] = act;
-      const float4* wr = reinterpret_cast<const float4*>(s_w0 + j * kDinPad);
-#pragma unroll
-      for (int q = 0; q < kDinPad / 4; ++q) {
-        if (q < n_in4) {
-          const float4 w = wr[q];
-          if (4 * q + 0 < 2 * kMaxL + 3) denc[4 * q + 0] = fmaf(w.x, dh, denc[4 * q + 0]);
-          if (4 * q + 1 < 2 * kMaxL + 3) denc[4 * q + 1] = fmaf(w.y, dh, denc[4 * q + 1]);
-          if (4 * q + 2 < 2 * kMaxL + 3) denc[4 * q + 2] = fmaf(w.z, dh, denc[4 * q + 2]);
-          if (4 * q + 3 < 2 * kMaxL + 3) denc[4 * q + 3] = fmaf(w.w, dh, denc[4 * q + 3]);
-        }
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < kDinPad; ++i) s_in[t * kDinPad + i] = in[i];
-#pragma unroll
-    for (int o = 0; o < kDoutMax; ++o) s_g[t * kDoutMax + o] = g[o];
-
-    // ---- phase 2: table gradient scatter (and optional dL/dx) ----
-    // All 32 lanes of a warp take part (dead lanes carry zero gradient at
-    // x = 0) so a level whose cell is the same for the whole warp -- most
-    // coarse levels, since a warp holds neighbouring pixels of consecutive
-    // samples -- is reduced with shuffles into 8 atomics instead of 256.
-    if (a.grad_table || a.grad_x) {
-      const float x[3] = {in[0], in[1], in[2]};
-      float dx[3] = {denc[0], denc[1], denc[2]};
-      float2* gt2 = reinterpret_cast<float2*>(a.grad_table);
-#pragma unroll
-      for (int l = 0; l < kMaxL; ++l) {
-        if (l < a.active) {
-          LevelCorners c;
-          level_corners(a.g, l, x, c);
-          const float d0 = live ? denc[3 + 2 * l] : 0.0f, d1 = live ? denc[4 + 2 * l] : 0.0f;
-          if (a.grad_table) {
-            if (warp_same_cell(c)) {
-#pragma unroll
-              for (int k = 0; k < 8; ++k) {
-                float v0 = c.w[k] * d0, v1 = c.w[k] * d1;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                  v0 += __shfl_xor_sync(0xffffffffu, v0, o);
-                  v1 += __shfl_xor_sync(0xffffffffu, v1, o);
-                }
-                if (lane == k) atomicAdd(gt2 + c.idx[k], make_float2(v0, v1));
-              }
-            } else if (live) {
-#pragma unroll
-              for (int k = 0; k < 8; ++k)
-                atomicAdd(gt2 + c.idx[k], make_float2(c.w[k] * d0, c.w[k] * d1));
-            }
-          }
-          if (a.grad_x && live) {
-            const float2* t2 = reinterpret_cast<const float2*>(a.table);
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-              const float2 v = __ldg(t2 + c.idx[k]);
-              const float gv = d0 * v.x + d1 * v.y;
-#pragma unroll
-              for (int d = 0; d < 3; ++d) dx[d] = fmaf(gv, corner_dw(c, k, d, a.g.scale[l]), dx[d]);
-            }
-          }
-        }
-      }
-      if (a.grad_x && live) {
-        a.grad_x[3 * p] = dx[0];
-        a.grad_x[3 * p + 1] = dx[1];
-        a.grad_x[3 * p + 2] = dx[2];
-      }
-    }
-    __syncthreads();
-
-    // ---- phase 3: weight gradients over the batch (register-tiled) ----
-    const int batch = (int)((n - b0) < kBwdThreads ? (n - b0) : kBwdThreads);
-    for (int q = 0; q < batch; ++q) {
-      const float4 dh = reinterpret_cast<const float4*>(s_dh + q * kH)[rg];
-      const float4 ac = reinterpret_cast<const float4*>(s_act + q * kH)[rg];
-      const float* iq = s_in + q * kDinPad;
-      const float* gq = s_g + q * kDoutMax;
-      const float dhr[4] = {dh.x, dh.y, dh.z, dh.w};
-      const float acr[4] = {ac.x, ac.y, ac.z, ac.w};
-#pragma unroll
-      for (int m = 0; m < 5; ++m) {
-        const int i = cg + 8 * m;
-        if (i < din_used) {
-          const float v = iq[i];
-#pragma unroll
-          for (int r = 0; r < 4; ++r) acc_w0[r][m] = fmaf(dhr[r], v, acc_w0[r][m]);
-        }
-      }
-#pragma unroll
-      for (int m = 0; m < 2; ++m) {
-        const int o = cg + 8 * m;
-        if (o < a.out_cols) {
-          const float gv = gq[o];
-#pragma unroll
-          for (int r = 0; r < 4; ++r) acc_w1[r][m] = fmaf(gv, acr[r], acc_w1[r][m]);
-        }
-      }
-      if (cg == 0) {
-#pragma unroll
-        for (int r = 0; r < 4; ++r) acc_b0[r] += dhr[r];
-      }
-      if (t < a.out_cols) acc_b1 += gq[t];
-    }
-    __syncthreads();
-  }
-
-  // ---- flush (one atomic per owned entry and block) ----
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int j = 4 * rg + r;
-    if (a.grad_w0) {
-#pragma unroll
-      for (int m = 0; m < 5; ++m) {
-        const int i = cg + 8 * m;
-        if (i < din_used && acc_w0[r][m] != 0.0f) atomicAdd(a.grad_w0 + j * a.din + i, acc_w0[r][m]);
-      }
-    }
-    if (a.grad_w1) {
-#pragma unroll
-      for (int m = 0; m < 2; ++m) {
-        const int o = cg + 8 * m;
-        if (o < a.out_cols && acc_w1[r][m] != 0.0f) atomicAdd(a.grad_w1 + o * kH + j, acc_w1[r][m]);
-      }
-    }
-    if (a.grad_b0 && cg == 0 && acc_b0[r] != 0.0f) atomicAdd(a.grad_b0 + j, acc_b0[r]);
-  }
-  if (a.grad_b1 && t < a.out_cols && acc_b1 != 0.0f) atomicAdd(a.grad_b1 + t, acc_b1);
-}
-
 constexpr size_t kFwdSmem = kSmemMlpFloats * sizeof(float);
-constexpr size_t kBwdSmem =
-    (kSmemMlpFloats + kBwdThreads * (kDinPad + 2 * kH + kDoutMax)) * sizeof(float);
 
 // ---------------------------------------------------------------------------
 // d sdf / d x (SDFNetwork.gradient, models/fields.py:107-119) and its adjoint
@@ -699,6 +468,7 @@ int make_grid_dev(const sn_grid_desc* d, GridDev& g) {
     g.scale[l] = d->scales[l];
     const uint64_t r = d->resolutions[l];
     g.dense[l] = (r * r * r <= (uint64_t)size) ? 1 : 0;
+    g.pow2[l] = (size & (size - 1)) == 0 ? 1 : 0;
     int lg = 0;
     while (((uint64_t)1 << lg) < size) ++lg;
     const uint64_t m = (((uint64_t)1 << 32) * (((uint64_t)1 << lg) - size)) / size + 1;

@@ -22,6 +22,7 @@ struct GridDev {
   uint32_t magic[kMaxL];    // Granlund-Montgomery reciprocal of size
   uint8_t sh1[kMaxL], sh2[kMaxL];
   uint8_t dense[kMaxL];
+  uint8_t pow2[kMaxL];      // size is a power of two (every hashed level): mod is a mask
   float scale[kMaxL];
 };
 
@@ -67,7 +68,8 @@ __device__ __forceinline__ void level_corners(const GridDev& g, int l, const flo
       index = q[0] + q[1] * res + q[2] * (res * res);
     else
       index = q[0] ^ (q[1] * 2654435761u) ^ (q[2] * 805459861u);
-    c.idx[k] = g.offset[l] + fast_mod(index, g.size[l], g.magic[l], g.sh1[l], g.sh2[l]);
+    c.idx[k] = g.offset[l] + (g.pow2[l] ? (index & (g.size[l] - 1u))
+                                        : fast_mod(index, g.size[l], g.magic[l], g.sh1[l], g.sh2[l]));
     c.w[k] = w;
   }
 }

@@ -390,8 +390,8 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       for (int i = 0; i < 16; ++i) {
         const int j = 16 * g + i;
         const float pre = h[i] + s_b0[j];
-        const float act = softplus_fwd(pre, a.beta, a.thresh);
-        const float sg = softplus_grad(pre, a.beta, a.thresh);
+        float act, sg;
+        softplus_fwd_grad(pre, a.beta, a.thresh, act, sg);
         float da = 0.0f;
 #pragma unroll
         for (int o = 0; o < kOc; ++o)
