@@ -76,24 +76,30 @@ __global__ void center_alpha_kernel(int64_t cap, const int32_t* __restrict__ cou
   }
 }
 
-// Keep visible samples, preserving order (one thread per ray).
-__global__ void compact_kernel(int64_t n_rays, const int32_t* __restrict__ pin,
-                               const uint8_t* __restrict__ vis, const int32_t* __restrict__ pout,
-                               const int64_t* __restrict__ ridx, const float* __restrict__ ts,
-                               const float* __restrict__ te, int64_t* __restrict__ ridx_o,
-                               float* __restrict__ ts_o, float* __restrict__ te_o) {
-  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= n_rays) return;
+// Keep visible samples, preserving order: one warp per ray, a ballot per
+// 32-sample chunk gives each visible sample its output slot.
+__global__ void __launch_bounds__(256) compact_kernel(
+    int64_t n_rays, const int32_t* __restrict__ pin, const uint8_t* __restrict__ vis,
+    const int32_t* __restrict__ pout, const int64_t* __restrict__ ridx, const float* __restrict__ ts,
+    const float* __restrict__ te, int64_t* __restrict__ ridx_o, float* __restrict__ ts_o,
+    float* __restrict__ te_o) {
+  const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= n_rays) return;  // whole warp
   const int64_t bi = pin[2 * r], bo = pout[2 * r];
   const int steps = pin[2 * r + 1];
   int c = 0;
-  for (int j = 0; j < steps; ++j) {
-    if (vis[bi + j]) {
-      ridx_o[bo + c] = ridx[bi + j];
-      ts_o[bo + c] = ts[bi + j];
-      te_o[bo + c] = te[bi + j];
-      ++c;
+  for (int j0 = 0; j0 < steps; j0 += 32) {
+    const int j = j0 + lane;
+    const bool v = j < steps && vis[bi + j];
+    const unsigned m = __ballot_sync(0xffffffffu, v);
+    if (v) {
+      const int64_t o = bo + c + __popc(m & ((1u << lane) - 1u));
+      ridx_o[o] = ridx[bi + j];
+      ts_o[o] = ts[bi + j];
+      te_o[o] = te[bi + j];
     }
+    c += __popc(m);
   }
 }
 
@@ -239,7 +245,7 @@ int sn_compact_samples(int64_t n_rays, const int32_t* packed_in, const uint8_t* 
                        float* t_starts_out, float* t_ends_out, void* stream) {
   SN_REQUIRE(n_rays >= 0, "compact: n_rays < 0");
   if (n_rays == 0) return SN_OK;
-  compact_kernel<<<div_up(n_rays, 128), 128, 0, as_stream(stream)>>>(
+  compact_kernel<<<div_up(n_rays * 32, 256), 256, 0, as_stream(stream)>>>(
       n_rays, packed_in, visibility, packed_out, ray_indices, t_starts, t_ends, ray_indices_out,
       t_starts_out, t_ends_out);
   return check_launch("compact_samples");

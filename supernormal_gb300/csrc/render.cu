@@ -58,24 +58,40 @@ __global__ void weight_bwd_kernel(int64_t n_rays, int P, const int32_t* __restri
   }
 }
 
-__global__ void visibility_kernel(int64_t n_rays, const int32_t* __restrict__ packed,
-                                  const float* __restrict__ alphas, float eps, float thre,
-                                  uint8_t* __restrict__ vis, int32_t* __restrict__ counts) {
-  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= n_rays) return;
+// One warp per ray: transmittance before each sample as a warp product scan of
+// (1 - alpha) with a carry between 32-sample chunks (the reference's CUB
+// scan is tree-ordered as well); visible = T >= eps (and alpha >= thre).
+__global__ void __launch_bounds__(256) visibility_kernel(int64_t n_rays, const int32_t* __restrict__ packed,
+                                                         const float* __restrict__ alphas, float eps,
+                                                         float thre, uint8_t* __restrict__ vis,
+                                                         int32_t* __restrict__ counts) {
+  const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= n_rays) return;  // whole warp
   const int64_t base = packed[2 * r];
   const int steps = packed[2 * r + 1];
-  float T = 1.0f;
+  float carry = 1.0f;
   int c = 0;
-  for (int j = 0; j < steps; ++j) {
-    const float al = alphas[base + j];
-    bool v = T >= eps;
+  for (int j0 = 0; j0 < steps; j0 += 32) {
+    const int j = j0 + lane;
+    const bool ok = j < steps;
+    const float al = ok ? alphas[base + j] : 0.0f;
+    float incl = ok ? __fsub_rn(1.0f, al) : 1.0f;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl = __fmul_rn(y, incl);
+    }
+    float excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) excl = 1.0f;
+    const float T = __fmul_rn(carry, excl);
+    carry = __fmul_rn(carry, __shfl_sync(0xffffffffu, incl, 31));
+    bool v = ok && T >= eps;
     if (thre > 0.0f) v = v && (al >= thre);
-    vis[base + j] = v ? 1 : 0;
-    c += v ? 1 : 0;
-    T = __fmul_rn(T, __fsub_rn(1.0f, al));
+    if (ok) vis[base + j] = v ? 1 : 0;
+    c += __popc(__ballot_sync(0xffffffffu, v));
   }
-  if (counts) counts[r] = c;
+  if (counts && lane == 0) counts[r] = c;
 }
 
 // out[idx[s], k, d] += w[s,k] * v[s,k,d]
@@ -147,7 +163,7 @@ int sn_visibility_from_alpha(int64_t n_rays, const int32_t* packed_info, const f
                              int32_t* vis_counts, void* stream) {
   SN_REQUIRE(n_rays >= 0, "visibility: n_rays < 0");
   if (n_rays == 0) return SN_OK;
-  visibility_kernel<<<div_up(n_rays, 128), 128, 0, as_stream(stream)>>>(
+  visibility_kernel<<<div_up(n_rays * 32, 256), 256, 0, as_stream(stream)>>>(
       n_rays, packed_info, alphas, early_stop_eps, alpha_thre, visibility, vis_counts);
   return check_launch("visibility_from_alpha");
 }
