@@ -40,37 +40,40 @@ struct LevelCorners {
   uint32_t cell[3];  // integer cell coordinates (the 8 indices are a function of these)
 };
 
+// The 8 corners of x's cell at level l: entry indices and trilinear weights.
+// Per-dimension terms are formed once (index of corner (dx,dy,dz) = a sum of
+// the dense strides or an XOR of the prime products, weight = (wx * wy) * wz),
+// which gives exactly the values of the corner-by-corner formula.
 __device__ __forceinline__ void level_corners(const GridDev& g, int l, const float x[3],
                                               LevelCorners& c) {
   const float s = g.scale[l];
-  uint32_t cell[3];
+  float w0[3], w1[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const float p = __fmaf_rn(s, x[d], 0.5f);
     const float f = floorf(p);
-    cell[d] = (uint32_t)(int)f;
-    c.cell[d] = cell[d];
+    c.cell[d] = (uint32_t)(int)f;
     c.frac[d] = __fsub_rn(p, f);
+    w1[d] = c.frac[d];
+    w0[d] = __fsub_rn(1.0f, c.frac[d]);
   }
-  const uint32_t res = g.res[l];
+  const bool dense = g.dense[l] != 0;
+  const uint32_t my = dense ? g.res[l] : 2654435761u;
+  const uint32_t mz = dense ? g.res[l] * g.res[l] : 805459861u;
+  const uint32_t tx[2] = {c.cell[0], c.cell[0] + 1u};
+  const uint32_t ty[2] = {c.cell[1] * my, (c.cell[1] + 1u) * my};
+  const uint32_t tz[2] = {c.cell[2] * mz, (c.cell[2] + 1u) * mz};
+  float wxy[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) wxy[k] = __fmul_rn((k & 1) ? w1[0] : w0[0], (k & 2) ? w1[1] : w0[1]);
+  const uint32_t off = g.offset[l], size = g.size[l];
+  const bool pow2 = g.pow2[l] != 0;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    float w = 1.0f;
-    uint32_t q[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const bool hi = (k >> d) & 1;
-      w = __fmul_rn(w, hi ? c.frac[d] : __fsub_rn(1.0f, c.frac[d]));
-      q[d] = cell[d] + (hi ? 1u : 0u);
-    }
-    uint32_t index;
-    if (g.dense[l])
-      index = q[0] + q[1] * res + q[2] * (res * res);
-    else
-      index = q[0] ^ (q[1] * 2654435761u) ^ (q[2] * 805459861u);
-    c.idx[k] = g.offset[l] + (g.pow2[l] ? (index & (g.size[l] - 1u))
-                                        : fast_mod(index, g.size[l], g.magic[l], g.sh1[l], g.sh2[l]));
-    c.w[k] = w;
+    const int dx = k & 1, dy = (k >> 1) & 1, dz = (k >> 2) & 1;
+    const uint32_t index = dense ? tx[dx] + ty[dy] + tz[dz] : tx[dx] ^ ty[dy] ^ tz[dz];
+    c.idx[k] = off + (pow2 ? (index & (size - 1u)) : fast_mod(index, size, g.magic[l], g.sh1[l], g.sh2[l]));
+    c.w[k] = __fmul_rn(wxy[k & 3], dz ? w1[2] : w0[2]);
   }
 }
 
