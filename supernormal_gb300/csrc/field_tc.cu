@@ -4,7 +4,7 @@
 // A CTA owns 128-point tiles (persistent over tiles) with 16 warps: warp w
 // serves TMEM lane quadrant q = w % 4 (points 32q..32q+31 of the tile) as
 // member g = w / 4 of that quadrant's group of four.  The four members split
-// the per-point work -- hash-grid levels 4g..4g+3, hidden units 16g..16g+15 --
+// the per-point work -- hash-grid levels g, g+4, g+8, g+12, hidden units 16g..16g+15 --
 // and write their parts of each point's row straight into the point's TMEM
 // lane, where the tensor core reads it as the A operand.  One thread issues
 // the MMAs; everyone else waits on an mbarrier (bounded).
@@ -45,11 +45,64 @@ constexpr uint32_t kLboP = 144, kSboP = (kTile / 4) * kLboP;
 constexpr uint32_t kColH = 0, kColInHi = 64, kColInLo = 64 + kK1;
 constexpr uint32_t kColDhHi = 64, kColDhLo = 128, kColDw0 = 192;
 
+// Member g of a quadrant group handles levels g, g+4, g+8, g+12 (coarse and
+// fine levels mixed, which balances the scatter's shuffle and atomic work);
+// its 8 features sit in permuted input columns 8g..8g+7.
+__device__ __forceinline__ int level_of(int g, int i) { return g + 4 * i; }
+
 // Permuted input column -> column of W0 (or -1 for a zero column).
 __device__ __forceinline__ int w0_col(int c, int L) {
-  if (c < 2 * L) return 3 + c;
-  if (c >= kXCol && c < kXCol + 3) return c - kXCol;
+  if (c < kXCol) {
+    const int l = level_of(c >> 3, (c & 7) >> 1);
+    return l < L ? 3 + 2 * l + (c & 1) : -1;
+  }
+  if (c < kXCol + 3) return c - kXCol;
   return -1;
+}
+
+// All 32 lanes share one cell: the warp's float2 contributions to the 8
+// corners are summed by a reduce-scatter (corner bit 2 follows lane bit 4,
+// bit 1 lane bit 3, bit 0 lane bit 2; 18 shuffles) and added with one float2
+// atomic per corner, issued together by lanes 0, 4, ..., 28.
+__device__ __forceinline__ void scatter_uniform(const LevelCorners& c, float d0, float d1, float2* gt2,
+                                                int lane) {
+  constexpr unsigned kAll = 0xffffffffu;
+  float v[16];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    v[2 * k] = c.w[k] * d0;
+    v[2 * k + 1] = c.w[k] * d1;
+  }
+  float a8[8], a4[4], a2[2];
+  {
+    const bool up = lane & 16;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      a8[i] = (up ? v[i + 8] : v[i]) + __shfl_xor_sync(kAll, up ? v[i] : v[i + 8], 16);
+  }
+  {
+    const bool up = lane & 8;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      a4[i] = (up ? a8[i + 4] : a8[i]) + __shfl_xor_sync(kAll, up ? a8[i] : a8[i + 4], 8);
+  }
+  {
+    const bool up = lane & 4;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+      a2[i] = (up ? a4[i + 2] : a4[i]) + __shfl_xor_sync(kAll, up ? a4[i] : a4[i + 2], 4);
+  }
+#pragma unroll
+  for (int s = 2; s > 0; s >>= 1) {
+    a2[0] += __shfl_xor_sync(kAll, a2[0], s);
+    a2[1] += __shfl_xor_sync(kAll, a2[1], s);
+  }
+  const int k = lane >> 2;
+  uint32_t idx = c.idx[0];
+#pragma unroll
+  for (int kk = 1; kk < 8; ++kk)
+    if (k == kk) idx = c.idx[kk];
+  if ((lane & 3) == 0) atomicAdd(gt2 + idx, make_float2(a2[0], a2[1]));
 }
 
 // W0 (64, din) -> B1 (N = 64 hidden, K = 40 inputs, K-major) hi/lo, and, when
@@ -75,12 +128,12 @@ __device__ void stage_w0(const FieldArgs& a, uint8_t* b1_hi, uint8_t* b1_lo, uin
   }
 }
 
-// Encoding of levels 4g..4g+3 of point x: e[2i + f] for level 4g + i.
+// Encoding of member g's levels of point x: e[2i + f] for level level_of(g, i).
 __device__ __forceinline__ void encode_group(const FieldArgs& a, int g, bool live, const float x[3],
                                              float e[8]) {
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    const int l = 4 * g + i;
+    const int l = level_of(g, i);
     float e0 = 0.0f, e1 = 0.0f;
     if (live && l < a.active) encode_level(a.table, a.g, l, x, e0, e1);
     e[2 * i] = e0;
@@ -447,7 +500,7 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       break;
     }
     tc::fence_after_sync();
-    // ---- dIN: table-gradient scatter for levels 4g..4g+3, dL/dx ----
+    // ---- dIN: table-gradient scatter for levels g, g+4, g+8, g+12, dL/dx ----
     {
       float din[8];
       tc::tmem_ld8(tc::taddr(tbase, lb, kColH + 8 * g), din);
@@ -467,23 +520,14 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       const float2* t2 = reinterpret_cast<const float2*>(a.table);
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const int l = 4 * g + i;
+        const int l = level_of(g, i);
         if (l < a.active) {
           LevelCorners c;
           level_corners(a.g, l, x, c);
           const float d0 = live ? din[2 * i] : 0.0f, d1 = live ? din[2 * i + 1] : 0.0f;
           if (want_table) {
             if (warp_same_cell(c)) {
-#pragma unroll
-              for (int k = 0; k < 8; ++k) {
-                float v0 = c.w[k] * d0, v1 = c.w[k] * d1;
-#pragma unroll
-                for (int s = 16; s > 0; s >>= 1) {
-                  v0 += __shfl_xor_sync(0xffffffffu, v0, s);
-                  v1 += __shfl_xor_sync(0xffffffffu, v1, s);
-                }
-                if (lane == k) atomicAdd(gt2 + c.idx[k], make_float2(v0, v1));
-              }
+              scatter_uniform(c, d0, d1, gt2, lane);
             } else if (live) {
 #pragma unroll
               for (int k = 0; k < 8; ++k) atomicAdd(gt2 + c.idx[k], make_float2(c.w[k] * d0, c.w[k] * d1));
