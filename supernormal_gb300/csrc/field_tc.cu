@@ -129,16 +129,80 @@ __device__ void stage_w0(const FieldArgs& a, uint8_t* b1_hi, uint8_t* b1_lo, uin
 }
 
 // Encoding of member g's levels of point x: e[2i + f] for level level_of(g, i).
+// PAIRED: two levels at a time, all 16 corner gathers issued before any is
+// used (about two L2 round trips per phase instead of four; the backward,
+// which has the registers for it).  Otherwise one level at a time.
+template <bool PAIRED>
 __device__ __forceinline__ void encode_group(const FieldArgs& a, int g, bool live, const float x[3],
                                              float e[8]) {
+  if (!PAIRED) {
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int l = level_of(g, i);
-    float e0 = 0.0f, e1 = 0.0f;
-    if (live && l < a.active) encode_level(a.table, a.g, l, x, e0, e1);
-    e[2 * i] = e0;
-    e[2 * i + 1] = e1;
+    for (int i = 0; i < 4; ++i) {
+      const int l = level_of(g, i);
+      float e0 = 0.0f, e1 = 0.0f;
+      if (live && l < a.active) encode_level(a.table, a.g, l, x, e0, e1);
+      e[2 * i] = e0;
+      e[2 * i + 1] = e1;
+    }
+    return;
   }
+  const float2* t2 = reinterpret_cast<const float2*>(a.table);
+#pragma unroll
+  for (int i0 = 0; i0 < 4; i0 += 2) {
+    const int la = level_of(g, i0), lb = level_of(g, i0 + 1);
+    const bool ua = la < a.active, ub = lb < a.active;  // uniform across the CTA
+    LevelCorners ca, cb;
+    float2 va[8], vb[8];
+    if (ua) {
+      level_corners(a.g, la, x, ca);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) va[k] = __ldg(t2 + ca.idx[k]);
+    }
+    if (ub) {
+      level_corners(a.g, lb, x, cb);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) vb[k] = __ldg(t2 + cb.idx[k]);
+    }
+    float a0 = 0.0f, a1 = 0.0f, b0 = 0.0f, b1 = 0.0f;
+    if (ua) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        a0 = __fmaf_rn(ca.w[k], va[k].x, a0);
+        a1 = __fmaf_rn(ca.w[k], va[k].y, a1);
+      }
+    }
+    if (ub) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        b0 = __fmaf_rn(cb.w[k], vb[k].x, b0);
+        b1 = __fmaf_rn(cb.w[k], vb[k].y, b1);
+      }
+    }
+    e[2 * i0] = live ? a0 : 0.0f;
+    e[2 * i0 + 1] = live ? a1 : 0.0f;
+    e[2 * i0 + 2] = live ? b0 : 0.0f;
+    e[2 * i0 + 3] = live ? b1 : 0.0f;
+  }
+}
+
+// Sums 16 per-lane values over the warp by a reduce-scatter (16 shuffles):
+// lanes 2m and 2m+1 end with the sum of value m.
+__device__ __forceinline__ float warp_reduce_scatter16(const float v[16], int lane) {
+  constexpr unsigned kAll = 0xffffffffu;
+  float a8[8], a4[4], a2[2];
+  bool up = lane & 16;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) a8[i] = (up ? v[i + 8] : v[i]) + __shfl_xor_sync(kAll, up ? v[i] : v[i + 8], 16);
+  up = lane & 8;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) a4[i] = (up ? a8[i + 4] : a8[i]) + __shfl_xor_sync(kAll, up ? a8[i] : a8[i + 4], 8);
+  up = lane & 4;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) a2[i] = (up ? a4[i + 2] : a4[i]) + __shfl_xor_sync(kAll, up ? a4[i] : a4[i + 2], 4);
+  up = lane & 2;
+  float a1 = (up ? a2[1] : a2[0]) + __shfl_xor_sync(kAll, up ? a2[0] : a2[1], 2);
+  a1 += __shfl_xor_sync(kAll, a1, 1);
+  return a1;
 }
 
 __device__ __forceinline__ void st_split8(uint32_t ta_hi, uint32_t ta_lo, const float v[8]) {
@@ -224,7 +288,7 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
     }
     {
       float e[8];
-      encode_group(a, g, live, x, e);
+      encode_group<false>(a, g, live, x, e);
       st_split8(tc::taddr(tbase, lb, kColInHi + 8 * g), tc::taddr(tbase, lb, kColInLo + 8 * g), e);
       if (g == 0) {
         const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
@@ -391,7 +455,7 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
     // ---- input rows: TMEM (A of the first MMA) and IN^T (B of the third) ----
     {
       float e[8];
-      encode_group(a, g, live, x, e);
+      encode_group<true>(a, g, live, x, e);
       st_split8(tc::taddr(tbase, lb, kColInHi + 8 * g), tc::taddr(tbase, lb, kColInLo + 8 * g), e);
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
@@ -438,27 +502,28 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       float go[kOc];
 #pragma unroll
       for (int o = 0; o < kOc; ++o) go[o] = (live && o < oc) ? a.grad_out[p * oc + o] : 0.0f;
-      float dh[16];
+      float dh[16], act[16];
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
         const int j = 16 * g + i;
         const float pre = h[i] + s_b0[j];
-        float act, sg;
-        softplus_fwd_grad(pre, a.beta, a.thresh, act, sg);
+        float sg;
+        softplus_fwd_grad(pre, a.beta, a.thresh, act[i], sg);
         float da = 0.0f;
 #pragma unroll
         for (int o = 0; o < kOc; ++o)
           if (o < oc) da = fmaf(go[o], s_w1[o * kH + j], da);
         dh[i] = live ? da * sg : 0.0f;
-        // dW1[o][j] += sum over the warp's points of g_o * act_j
+      }
+      // dW1[o][j] += sum over the warp's points of g_o * act_j
 #pragma unroll
-        for (int o = 0; o < kOc; ++o) {
-          if (o < oc) {
-            float v = live ? go[o] * act : 0.0f;
+      for (int o = 0; o < kOc; ++o) {
+        if (o < oc) {
+          float v[16];
 #pragma unroll
-            for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-            if (lane == 0) atomicAdd(s_dw1 + o * kH + j, v);
-          }
+          for (int i = 0; i < 16; ++i) v[i] = live ? go[o] * act[i] : 0.0f;
+          const float r = warp_reduce_scatter16(v, lane);
+          if ((lane & 1) == 0) atomicAdd(s_dw1 + o * kH + 16 * g + (lane >> 1), r);
         }
       }
       if (g == 0) {
