@@ -606,6 +606,7 @@ int sn_field_bwd(int64_t n, const int32_t* count, const float* x, const float* g
   a.grad_w1 = grad_w1;
   a.grad_b1 = grad_b1;
   a.grad_x = grad_x;
+  a.pair16 = (reinterpret_cast<uintptr_t>(grad_table) & 15u) == 0;
   if (n == 0) return SN_OK;
   return field_bwd_tc(a, as_stream(stream));
 }

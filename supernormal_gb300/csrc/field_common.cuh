@@ -143,6 +143,7 @@ struct FieldArgs {
   float* grad_b1;
   float* grad_x;          // (n, 3) optional
   int32_t* status;        // optional: SN_STATUS_TIMEOUT is OR-ed here
+  bool pair16;            // grad_table is 16-byte aligned: entry pairs may be added as float4
 };
 
 __device__ __forceinline__ int64_t effective_n(const FieldArgs& a) {

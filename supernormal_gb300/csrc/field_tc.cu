@@ -60,49 +60,77 @@ __device__ __forceinline__ int w0_col(int c, int L) {
   return -1;
 }
 
-// All 32 lanes share one cell: the warp's float2 contributions to the 8
-// corners are summed by a reduce-scatter (corner bit 2 follows lane bit 4,
-// bit 1 lane bit 3, bit 0 lane bit 2; 18 shuffles) and added with one float2
-// atomic per corner, issued together by lanes 0, 4, ..., 28.
-__device__ __forceinline__ void scatter_uniform(const LevelCorners& c, float d0, float d1, float2* gt2,
-                                                int lane) {
+// Table-gradient contributions of the warp's 32 points at one level.
+//  * Lanes sharing a cell are summed first: the cell of the first remaining
+//    lane is matched exactly (three coordinates), and if it holds at least
+//    kMinGroupLanes lanes their float2 contributions to the 8 corners are
+//    summed by a reduce-scatter over the warp (corner bit 2 follows lane bit
+//    4, bit 1 lane bit 3, bit 0 lane bit 2) and added by one float2 atomic per
+//    corner, issued together by lanes 0, 4, ..., 28; up to kMaxCellGroups cells.
+//  * The lanes left add their own 8 corners; an x-adjacent corner pair that
+//    occupies one aligned pair of entries goes out as one 16-byte atomic.
+constexpr int kMaxCellGroups = 4;
+constexpr int kMinGroupLanes = 4;
+
+__device__ __forceinline__ void scatter_level(const LevelCorners& c, float d0, float d1, bool live,
+                                              bool pair16, float2* gt2, int lane) {
   constexpr unsigned kAll = 0xffffffffu;
-  float v[16];
+  unsigned rest = __ballot_sync(kAll, live);
+  for (int it = 0; it < kMaxCellGroups && rest != 0u; ++it) {
+    const int ld = __ffs(rest) - 1;
+    const uint32_t c0 = __shfl_sync(kAll, c.cell[0], ld);
+    const uint32_t c1 = __shfl_sync(kAll, c.cell[1], ld);
+    const uint32_t c2 = __shfl_sync(kAll, c.cell[2], ld);
+    const bool in = ((rest >> lane) & 1u) & (c.cell[0] == c0) & (c.cell[1] == c1) & (c.cell[2] == c2);
+    const unsigned gm = __ballot_sync(kAll, in);
+    if (__popc(gm) < kMinGroupLanes) break;  // the same decision on every lane
+    const float e0 = in ? d0 : 0.0f, e1 = in ? d1 : 0.0f;
+    float v[16];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    v[2 * k] = c.w[k] * d0;
-    v[2 * k + 1] = c.w[k] * d1;
+    for (int k = 0; k < 8; ++k) {
+      v[2 * k] = c.w[k] * e0;
+      v[2 * k + 1] = c.w[k] * e1;
+    }
+    float a8[8], a4[4], a2[2];
+    bool up = lane & 16;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a8[i] = (up ? v[i + 8] : v[i]) + __shfl_xor_sync(kAll, up ? v[i] : v[i + 8], 16);
+    up = lane & 8;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a4[i] = (up ? a8[i + 4] : a8[i]) + __shfl_xor_sync(kAll, up ? a8[i] : a8[i + 4], 8);
+    up = lane & 4;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) a2[i] = (up ? a4[i + 2] : a4[i]) + __shfl_xor_sync(kAll, up ? a4[i] : a4[i + 2], 4);
+#pragma unroll
+    for (int sft = 2; sft > 0; sft >>= 1) {
+      a2[0] += __shfl_xor_sync(kAll, a2[0], sft);
+      a2[1] += __shfl_xor_sync(kAll, a2[1], sft);
+    }
+    const int k = lane >> 2;  // corner summed into lanes 4k..4k+3
+    uint32_t idx = __shfl_sync(kAll, c.idx[0], ld);
+#pragma unroll
+    for (int kk = 1; kk < 8; ++kk) {
+      const uint32_t t = __shfl_sync(kAll, c.idx[kk], ld);
+      if (k == kk) idx = t;
+    }
+    if ((lane & 3) == 0) atomicAdd(gt2 + idx, make_float2(a2[0], a2[1]));
+    rest &= ~gm;
   }
-  float a8[8], a4[4], a2[2];
-  {
-    const bool up = lane & 16;
+  if ((rest >> lane) & 1u) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
-      a8[i] = (up ? v[i + 8] : v[i]) + __shfl_xor_sync(kAll, up ? v[i] : v[i + 8], 16);
+    for (int m = 0; m < 4; ++m) {  // corners 2m (dx = 0) and 2m + 1 (dx = 1)
+      const uint32_t i0 = c.idx[2 * m], i1 = c.idx[2 * m + 1];
+      const float2 v0 = make_float2(c.w[2 * m] * d0, c.w[2 * m] * d1);
+      const float2 v1 = make_float2(c.w[2 * m + 1] * d0, c.w[2 * m + 1] * d1);
+      if (pair16 && i1 == (i0 ^ 1u)) {
+        const float4 q = (i0 & 1u) ? make_float4(v1.x, v1.y, v0.x, v0.y) : make_float4(v0.x, v0.y, v1.x, v1.y);
+        atomicAdd(reinterpret_cast<float4*>(gt2 + (i0 & ~1u)), q);
+      } else {
+        atomicAdd(gt2 + i0, v0);
+        atomicAdd(gt2 + i1, v1);
+      }
+    }
   }
-  {
-    const bool up = lane & 8;
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-      a4[i] = (up ? a8[i + 4] : a8[i]) + __shfl_xor_sync(kAll, up ? a8[i] : a8[i + 4], 8);
-  }
-  {
-    const bool up = lane & 4;
-#pragma unroll
-    for (int i = 0; i < 2; ++i)
-      a2[i] = (up ? a4[i + 2] : a4[i]) + __shfl_xor_sync(kAll, up ? a4[i] : a4[i + 2], 4);
-  }
-#pragma unroll
-  for (int s = 2; s > 0; s >>= 1) {
-    a2[0] += __shfl_xor_sync(kAll, a2[0], s);
-    a2[1] += __shfl_xor_sync(kAll, a2[1], s);
-  }
-  const int k = lane >> 2;
-  uint32_t idx = c.idx[0];
-#pragma unroll
-  for (int kk = 1; kk < 8; ++kk)
-    if (k == kk) idx = c.idx[kk];
-  if ((lane & 3) == 0) atomicAdd(gt2 + idx, make_float2(a2[0], a2[1]));
 }
 
 // W0 (64, din) -> B1 (N = 64 hidden, K = 40 inputs, K-major) hi/lo, and, when
@@ -591,12 +619,7 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
           level_corners(a.g, l, x, c);
           const float d0 = live ? din[2 * i] : 0.0f, d1 = live ? din[2 * i + 1] : 0.0f;
           if (want_table) {
-            if (warp_same_cell(c)) {
-              scatter_uniform(c, d0, d1, gt2, lane);
-            } else if (live) {
-#pragma unroll
-              for (int k = 0; k < 8; ++k) atomicAdd(gt2 + c.idx[k], make_float2(c.w[k] * d0, c.w[k] * d1));
-            }
+            scatter_level(c, d0, d1, live, a.pair16, gt2, lane);
           }
           if (want_x && live) {
 #pragma unroll
