@@ -117,6 +117,23 @@ __device__ __forceinline__ void softplus_fwd_grad(float x, float beta, float thr
   y = log1pf(z) / beta;
   dy = z / (z + 1.0f);
 }
+// Softplus and its derivative through the hardware exp2/log2 approximations
+// (__expf, __logf, __fdividef): y = log(1 + z) / beta, dy = z / (1 + z),
+// z = exp(beta x).  Against the accurate pair above the absolute error of y
+// stays below 4e-9 for beta = 100 and z < 1, and within a few ulp beyond.
+__device__ __forceinline__ void softplus_fwd_grad_fast(float x, float beta, float inv_beta,
+                                                       float threshold, float& y, float& dy) {
+  const float bx = x * beta;
+  if (bx > threshold) {
+    y = x;
+    dy = 1.0f;
+    return;
+  }
+  const float z = __expf(bx);
+  const float u = 1.0f + z;
+  y = __logf(u) * inv_beta;
+  dy = __fdividef(z, u);
+}
 __device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + expf(-x)); }
 
 }  // namespace sn

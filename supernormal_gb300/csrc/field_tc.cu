@@ -283,6 +283,7 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
   const int q = warp & 3, g = warp >> 2;
   const int pt = 32 * q + lane;  // point within the tile == TMEM lane
   const int oc = a.out_cols;
+  const float inv_beta = 1.0f / a.beta;
 
   stage_w0(a, sm + FwdSmem::b1_hi, sm + FwdSmem::b1_lo, nullptr, nullptr);
   for (int e = t; e < kDoutMax * kH; e += kThreads) s_w1[e] = e / kH < oc ? a.w1[e] : 0.0f;
@@ -348,7 +349,8 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
       const int j = 16 * g + i;
-      const float act = softplus_fwd(h[i] + s_b0[j], a.beta, a.thresh);
+      float act, sg_unused;
+      softplus_fwd_grad_fast(h[i] + s_b0[j], a.beta, inv_beta, a.thresh, act, sg_unused);
 #pragma unroll
       for (int o = 0; o < kOc; ++o)
         if (o < oc) part[o] = fmaf(s_w1[o * kH + j], act, part[o]);
@@ -384,7 +386,7 @@ struct BwdSmem {
   static constexpr uint32_t b1_hi = 0, b1_lo = 10240, b2_hi = 20480, b2_lo = 32768, a3 = 45056,
                             b3_hi = a3 + 16 * kSboP, b3_lo = b3_hi + 6 * kSboP, w1 = b3_lo + 6 * kSboP,
                             b0 = w1 + kDoutMax * kH * 4, dx = b0 + kH * 4, bar = dx + 4 * kTile * 3 * 4,
-                            slot = bar + 8, dw1 = slot + 8, db1 = dw1 + kDoutMax * kH * 4,
+                            bar3 = bar + 8, slot = bar3 + 8, dw1 = slot + 8, db1 = dw1 + kDoutMax * kH * 4,
                             end = db1 + kDoutMax * 4;
 };
 constexpr size_t kBwdSmemBytes = BwdSmem::end;
@@ -394,12 +396,9 @@ __device__ __forceinline__ void st_smem_u32(uint8_t* base, uint32_t off, uint32_
   *reinterpret_cast<uint32_t*>(base + off) = v;
 }
 
-// Second and third MMAs of the backward: dIN = dH W0 (3xTF32, M=128, N=48,
-// K=64) and dW0 += [dH_hi; dH_lo]^T-rows x IN^T (M=128, N=48, K=128 points).
-__device__ __forceinline__ void issue_mma23(uint32_t tbase, const uint8_t* sm, bool first_tile) {
+// Second MMA of the backward: dIN = dH W0 (3xTF32, M=128, N=48, K=64).
+__device__ __forceinline__ void issue_mma2(uint32_t tbase, const uint8_t* sm) {
   const uint32_t s_b2_hi = tc::smem_u32(sm + BwdSmem::b2_hi), s_b2_lo = tc::smem_u32(sm + BwdSmem::b2_lo);
-  const uint32_t s_a3 = tc::smem_u32(sm + BwdSmem::a3);
-  const uint32_t s_b3_hi = tc::smem_u32(sm + BwdSmem::b3_hi), s_b3_lo = tc::smem_u32(sm + BwdSmem::b3_lo);
   const uint32_t idesc = tc::idesc_tf32(kTile, kN2);
   const uint32_t d2 = tc::taddr(tbase, 0, kColH);
   const uint32_t sbo2 = (kH / 4) * 128u;
@@ -412,6 +411,14 @@ __device__ __forceinline__ void issue_mma23(uint32_t tbase, const uint8_t* sm, b
   for (int ks = 0; ks < kH / 8; ++ks)
     tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhHi + 8 * ks), tc::smem_desc(s_b2_lo + 256u * ks, 128u, sbo2),
                idesc, 1);
+}
+
+// Third MMA: dW0 += [dH_hi; dH_lo]^T-rows x IN^T (M=128, N=48, K=128 points),
+// accumulated in TMEM over all of the CTA's tiles.
+__device__ __forceinline__ void issue_mma3(uint32_t tbase, const uint8_t* sm, bool first_tile) {
+  const uint32_t s_a3 = tc::smem_u32(sm + BwdSmem::a3);
+  const uint32_t s_b3_hi = tc::smem_u32(sm + BwdSmem::b3_hi), s_b3_lo = tc::smem_u32(sm + BwdSmem::b3_lo);
+  const uint32_t idesc = tc::idesc_tf32(kTile, kN2);
   const uint32_t d3 = tc::taddr(tbase, 0, kColDw0);
   for (int ks = 0; ks < kTile / 8; ++ks) {
     const uint32_t k0 = 2u * kLboP * ks;
@@ -431,12 +438,14 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
   uint8_t* a3 = sm + BwdSmem::a3;
   uint8_t* b3_hi = sm + BwdSmem::b3_hi;
   uint8_t* b3_lo = sm + BwdSmem::b3_lo;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + BwdSmem::bar);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + BwdSmem::bar);    // first and second MMAs
+  uint64_t* bar3 = reinterpret_cast<uint64_t*>(sm + BwdSmem::bar3);  // weight-gradient MMAs
   uint32_t* slot = reinterpret_cast<uint32_t*>(sm + BwdSmem::slot);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int q = warp & 3, g = warp >> 2;
   const int pt = 32 * q + lane;
   const int oc = a.out_cols;
+  const float inv_beta = 1.0f / a.beta;
   const bool want_table = a.grad_table != nullptr;
   const bool want_x = a.grad_x != nullptr;
 
@@ -458,7 +467,10 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
     tc::tmem_alloc(slot, kCols);
     tc::tmem_relinquish();
   }
-  if (t == 0) tc::mbar_init(bar, 1);
+  if (t == 0) {
+    tc::mbar_init(bar, 1);
+    tc::mbar_init(bar3, 1);
+  }
   tc::fence_proxy_async_smem();
   tc::fence_before_sync();
   __syncthreads();
@@ -466,8 +478,8 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
   const uint32_t tbase = *slot;
   const uint32_t lb = (uint32_t)(32 * q);
   const uint32_t s_b1_hi = tc::smem_u32(sm + BwdSmem::b1_hi), s_b1_lo = tc::smem_u32(sm + BwdSmem::b1_lo);
-  uint32_t phase = 0;
-  bool ok = true, first = true;
+  uint32_t phase = 0, phase3 = 0;
+  bool ok = true, first = true, pending3 = false;
 
   const int64_t n = effective_n(a);
   const int64_t n_tiles = (n + kTile - 1) / kTile;
@@ -481,10 +493,20 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       x[2] = a.x[3 * p + 2];
     }
     // ---- input rows: TMEM (A of the first MMA) and IN^T (B of the third) ----
+    bool ok3 = true;
     {
       float e[8];
       encode_group<true>(a, g, live, x, e);
       st_split8(tc::taddr(tbase, lb, kColInHi + 8 * g), tc::taddr(tbase, lb, kColInLo + 8 * g), e);
+      // the previous tile's weight-gradient MMAs still read IN^T and dH^T:
+      // wait for them only now, so they overlap its scatter and these gathers
+      if (pending3) {
+        ok3 = tc::mbar_wait_bounded(bar3, phase3);
+        if (ok3) {
+          phase3 ^= 1u;
+          pending3 = false;
+        }
+      }
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         uint32_t hi, lo;
@@ -509,7 +531,10 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
     tc::tmem_wait_st();
     tc::fence_proxy_async_smem();
     tc::fence_before_sync();
-    __syncthreads();
+    if (!__syncthreads_and(ok3)) {
+      ok = false;
+      break;
+    }
     if (t == 0) {
       tc::fence_after_sync();
       issue_mma1(tbase, s_b1_hi, s_b1_lo);
@@ -536,7 +561,7 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
         const int j = 16 * g + i;
         const float pre = h[i] + s_b0[j];
         float sg;
-        softplus_fwd_grad(pre, a.beta, a.thresh, act[i], sg);
+        softplus_fwd_grad_fast(pre, a.beta, inv_beta, a.thresh, act[i], sg);
         float da = 0.0f;
 #pragma unroll
         for (int o = 0; o < kOc; ++o)
@@ -582,10 +607,13 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
     __syncthreads();
     if (t == 0) {
       tc::fence_after_sync();
-      issue_mma23(tbase, sm, first);
+      issue_mma2(tbase, sm);
       tc::mma_commit(bar);
+      issue_mma3(tbase, sm, first);
+      tc::mma_commit(bar3);
     }
     first = false;
+    pending3 = true;
     got = tc::mbar_wait_bounded(bar, phase);
     phase ^= 1u;
     if (!__syncthreads_and(got)) {
@@ -652,11 +680,10 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       __syncthreads();
     }
   }
-  if (!ok) {
-    if (t == 0 && a.status) atomicOr(a.status, SN_STATUS_TIMEOUT);
-    (void)tc::mbar_wait_bounded(bar, phase ^ 1u);
-  }
-  __syncthreads();
+  if (!ok) (void)tc::mbar_wait_bounded(bar, phase ^ 1u);  // drain a timed-out first/second MMA
+  if (pending3) ok = tc::mbar_wait_bounded(bar3, phase3) && ok;
+  ok = __syncthreads_and(ok);
+  if (!ok && t == 0 && a.status) atomicOr(a.status, SN_STATUS_TIMEOUT);
   tc::fence_after_sync();
   if (ok && !first) {
     // dW0 / db0: lanes 0..63 hold the dH_hi rows, 64..127 the dH_lo rows
