@@ -77,6 +77,18 @@ __device__ __forceinline__ void level_corners(const GridDev& g, int l, const flo
   }
 }
 
+// Entry index of the corner with integer coordinates (qx, qy, qz) at level l
+// (the same arithmetic as level_corners).
+__device__ __forceinline__ uint32_t corner_index(const GridDev& g, int l, uint32_t qx, uint32_t qy,
+                                                 uint32_t qz) {
+  const bool dense = g.dense[l] != 0;
+  const uint32_t my = dense ? g.res[l] : 2654435761u;
+  const uint32_t mz = dense ? g.res[l] * g.res[l] : 805459861u;
+  const uint32_t index = dense ? qx + qy * my + qz * mz : qx ^ (qy * my) ^ (qz * mz);
+  const uint32_t size = g.size[l];
+  return g.offset[l] + (g.pow2[l] ? (index & (size - 1u)) : fast_mod(index, size, g.magic[l], g.sh1[l], g.sh2[l]));
+}
+
 // True on every lane when all 32 lanes of the warp are in the same cell.  Must
 // be reached by all 32 lanes; the three shuffles are issued unconditionally
 // (a short-circuit && around them would leave some lanes out of a full-mask

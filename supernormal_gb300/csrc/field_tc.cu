@@ -72,8 +72,8 @@ __device__ __forceinline__ int w0_col(int c, int L) {
 constexpr int kMaxCellGroups = 4;
 constexpr int kMinGroupLanes = 4;
 
-__device__ __forceinline__ void scatter_level(const LevelCorners& c, float d0, float d1, bool live,
-                                              bool pair16, float2* gt2, int lane) {
+__device__ __forceinline__ void scatter_level(const GridDev& gd, int l, const LevelCorners& c, float d0,
+                                              float d1, bool live, bool pair16, float2* gt2, int lane) {
   constexpr unsigned kAll = 0xffffffffu;
   unsigned rest = __ballot_sync(kAll, live);
   for (int it = 0; it < kMaxCellGroups && rest != 0u; ++it) {
@@ -107,13 +107,9 @@ __device__ __forceinline__ void scatter_level(const LevelCorners& c, float d0, f
       a2[1] += __shfl_xor_sync(kAll, a2[1], sft);
     }
     const int k = lane >> 2;  // corner summed into lanes 4k..4k+3
-    uint32_t idx = __shfl_sync(kAll, c.idx[0], ld);
-#pragma unroll
-    for (int kk = 1; kk < 8; ++kk) {
-      const uint32_t t = __shfl_sync(kAll, c.idx[kk], ld);
-      if (k == kk) idx = t;
-    }
-    if ((lane & 3) == 0) atomicAdd(gt2 + idx, make_float2(a2[0], a2[1]));
+    if ((lane & 3) == 0)
+      atomicAdd(gt2 + corner_index(gd, l, c0 + (k & 1), c1 + ((k >> 1) & 1), c2 + (k >> 2)),
+                make_float2(a2[0], a2[1]));
     rest &= ~gm;
   }
   if ((rest >> lane) & 1u) {
@@ -154,6 +150,21 @@ __device__ void stage_w0(const FieldArgs& a, uint8_t* b1_hi, uint8_t* b1_lo, uin
       *reinterpret_cast<uint32_t*>(b2_lo + o2) = lo;
     }
   }
+}
+
+__device__ __forceinline__ void load_point(const FieldArgs& a, int64_t p, int64_t n, float x[3]) {
+  if (p < n) {
+    x[0] = a.x[3 * p];
+    x[1] = a.x[3 * p + 1];
+    x[2] = a.x[3 * p + 2];
+  } else {
+    x[0] = x[1] = x[2] = 0.0f;
+  }
+}
+template <int OC>
+__device__ __forceinline__ void load_grad(const FieldArgs& a, int64_t p, int64_t n, float go[OC]) {
+#pragma unroll
+  for (int o = 0; o < OC; ++o) go[o] = (p < n && o < a.out_cols) ? a.grad_out[p * a.out_cols + o] : 0.0f;
 }
 
 // Encoding of member g's levels of point x: e[2i + f] for level level_of(g, i).
@@ -246,15 +257,12 @@ __device__ __forceinline__ void issue_mma1(uint32_t tbase, uint32_t s_b1_hi, uin
   const uint32_t idesc = tc::idesc_tf32(kTile, kH);
   const uint32_t sbo = (kK1 / 4) * 128u;
   const uint32_t d = tc::taddr(tbase, 0, kColH);
+  // a descriptor advances by (byte offset >> 4) in its start-address field
+  const uint64_t w_hi = tc::smem_desc(s_b1_hi, 128u, sbo), w_lo = tc::smem_desc(s_b1_lo, 128u, sbo);
   for (int ks = 0; ks < kK1 / 8; ++ks)
-    tc::mma_ts(d, tc::taddr(tbase, 0, kColInHi + 8 * ks), tc::smem_desc(s_b1_hi + 256u * ks, 128u, sbo),
-               idesc, ks > 0);
-  for (int ks = 0; ks < kK1 / 8; ++ks)
-    tc::mma_ts(d, tc::taddr(tbase, 0, kColInLo + 8 * ks), tc::smem_desc(s_b1_hi + 256u * ks, 128u, sbo),
-               idesc, 1);
-  for (int ks = 0; ks < kK1 / 8; ++ks)
-    tc::mma_ts(d, tc::taddr(tbase, 0, kColInHi + 8 * ks), tc::smem_desc(s_b1_lo + 256u * ks, 128u, sbo),
-               idesc, 1);
+    tc::mma_ts(d, tc::taddr(tbase, 0, kColInHi + 8 * ks), w_hi + 16u * ks, idesc, ks > 0);
+  for (int ks = 0; ks < kK1 / 8; ++ks) tc::mma_ts(d, tc::taddr(tbase, 0, kColInLo + 8 * ks), w_hi + 16u * ks, idesc, 1);
+  for (int ks = 0; ks < kK1 / 8; ++ks) tc::mma_ts(d, tc::taddr(tbase, 0, kColInHi + 8 * ks), w_lo + 16u * ks, idesc, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -306,15 +314,14 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
 
   const int64_t n = effective_n(a);
   const int64_t n_tiles = (n + kTile - 1) / kTile;
+  // this point's coordinates one tile ahead: the stream read overlaps a tile
+  float xn[3] = {0.0f, 0.0f, 0.0f};
+  load_point(a, (int64_t)blockIdx.x * kTile + pt, n, xn);
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const int64_t p = tile * kTile + pt;
     const bool live = p < n;
-    float x[3] = {0.0f, 0.0f, 0.0f};
-    if (live) {
-      x[0] = a.x[3 * p];
-      x[1] = a.x[3 * p + 1];
-      x[2] = a.x[3 * p + 2];
-    }
+    const float x[3] = {xn[0], xn[1], xn[2]};
+    load_point(a, (tile + gridDim.x) * kTile + pt, n, xn);
     {
       float e[8];
       encode_group<false>(a, g, live, x, e);
@@ -402,15 +409,11 @@ __device__ __forceinline__ void issue_mma2(uint32_t tbase, const uint8_t* sm) {
   const uint32_t idesc = tc::idesc_tf32(kTile, kN2);
   const uint32_t d2 = tc::taddr(tbase, 0, kColH);
   const uint32_t sbo2 = (kH / 4) * 128u;
+  const uint64_t w_hi = tc::smem_desc(s_b2_hi, 128u, sbo2), w_lo = tc::smem_desc(s_b2_lo, 128u, sbo2);
   for (int ks = 0; ks < kH / 8; ++ks)
-    tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhHi + 8 * ks), tc::smem_desc(s_b2_hi + 256u * ks, 128u, sbo2),
-               idesc, ks > 0);
-  for (int ks = 0; ks < kH / 8; ++ks)
-    tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhLo + 8 * ks), tc::smem_desc(s_b2_hi + 256u * ks, 128u, sbo2),
-               idesc, 1);
-  for (int ks = 0; ks < kH / 8; ++ks)
-    tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhHi + 8 * ks), tc::smem_desc(s_b2_lo + 256u * ks, 128u, sbo2),
-               idesc, 1);
+    tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhHi + 8 * ks), w_hi + 16u * ks, idesc, ks > 0);
+  for (int ks = 0; ks < kH / 8; ++ks) tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhLo + 8 * ks), w_hi + 16u * ks, idesc, 1);
+  for (int ks = 0; ks < kH / 8; ++ks) tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhHi + 8 * ks), w_lo + 16u * ks, idesc, 1);
 }
 
 // Third MMA: dW0 += [dH_hi; dH_lo]^T-rows x IN^T (M=128, N=48, K=128 points),
@@ -420,11 +423,12 @@ __device__ __forceinline__ void issue_mma3(uint32_t tbase, const uint8_t* sm, bo
   const uint32_t s_b3_hi = tc::smem_u32(sm + BwdSmem::b3_hi), s_b3_lo = tc::smem_u32(sm + BwdSmem::b3_lo);
   const uint32_t idesc = tc::idesc_tf32(kTile, kN2);
   const uint32_t d3 = tc::taddr(tbase, 0, kColDw0);
+  const uint64_t da = tc::smem_desc(s_a3, kLboP, kSboP), dbh = tc::smem_desc(s_b3_hi, kLboP, kSboP),
+                 dbl = tc::smem_desc(s_b3_lo, kLboP, kSboP);
   for (int ks = 0; ks < kTile / 8; ++ks) {
-    const uint32_t k0 = 2u * kLboP * ks;
-    tc::mma_ss(d3, tc::smem_desc(s_a3 + k0, kLboP, kSboP), tc::smem_desc(s_b3_hi + k0, kLboP, kSboP), idesc,
-               (first_tile && ks == 0) ? 0u : 1u);
-    tc::mma_ss(d3, tc::smem_desc(s_a3 + k0, kLboP, kSboP), tc::smem_desc(s_b3_lo + k0, kLboP, kSboP), idesc, 1);
+    const uint64_t k0 = (2u * kLboP * ks) >> 4;
+    tc::mma_ss(d3, da + k0, dbh + k0, idesc, (first_tile && ks == 0) ? 0u : 1u);
+    tc::mma_ss(d3, da + k0, dbl + k0, idesc, 1);
   }
 }
 
@@ -483,15 +487,19 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
 
   const int64_t n = effective_n(a);
   const int64_t n_tiles = (n + kTile - 1) / kTile;
+  // this point's coordinates and output gradient one tile ahead
+  float xn[3] = {0.0f, 0.0f, 0.0f}, gon[kOc];
+  load_point(a, (int64_t)blockIdx.x * kTile + pt, n, xn);
+  load_grad<kOc>(a, (int64_t)blockIdx.x * kTile + pt, n, gon);
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const int64_t p = tile * kTile + pt;
     const bool live = p < n;
-    float x[3] = {0.0f, 0.0f, 0.0f};
-    if (live) {
-      x[0] = a.x[3 * p];
-      x[1] = a.x[3 * p + 1];
-      x[2] = a.x[3 * p + 2];
-    }
+    const float x[3] = {xn[0], xn[1], xn[2]};
+    float go[kOc];
+#pragma unroll
+    for (int o = 0; o < kOc; ++o) go[o] = gon[o];
+    load_point(a, (tile + gridDim.x) * kTile + pt, n, xn);
+    load_grad<kOc>(a, (tile + gridDim.x) * kTile + pt, n, gon);
     // ---- input rows: TMEM (A of the first MMA) and IN^T (B of the third) ----
     bool ok3 = true;
     {
@@ -552,9 +560,6 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       float h[16];
       tc::tmem_ld16(tc::taddr(tbase, lb, kColH + 16 * g), h);
       tc::tmem_wait_ld();
-      float go[kOc];
-#pragma unroll
-      for (int o = 0; o < kOc; ++o) go[o] = (live && o < oc) ? a.grad_out[p * oc + o] : 0.0f;
       float dh[16], act[16];
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
@@ -647,7 +652,7 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
           level_corners(a.g, l, x, c);
           const float d0 = live ? din[2 * i] : 0.0f, d1 = live ? din[2 * i + 1] : 0.0f;
           if (want_table) {
-            scatter_level(c, d0, d1, live, a.pair16, gt2, lane);
+            scatter_level(a.g, l, c, d0, d1, live, a.pair16, gt2, lane);
           }
           if (want_x && live) {
 #pragma unroll
