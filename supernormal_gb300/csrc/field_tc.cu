@@ -45,15 +45,19 @@ constexpr uint32_t kLboP = 144, kSboP = (kTile / 4) * kLboP;
 constexpr uint32_t kColH = 0, kColInHi = 64, kColInLo = 64 + kK1;
 constexpr uint32_t kColDhHi = 64, kColDhLo = 128, kColDw0 = 192;
 
-// Member g of a quadrant group handles levels g, g+4, g+8, g+12 (coarse and
-// fine levels mixed, which balances the scatter's shuffle and atomic work);
-// its 8 features sit in permuted input columns 8g..8g+7.
-__device__ __forceinline__ int level_of(int g, int i) { return g + 4 * i; }
+// With M members per quadrant group, member g handles levels g, g+M, g+2M, ...
+// (coarse and fine levels mixed, which balances the scatter's shuffle and
+// atomic work); its 32/M features sit in permuted input columns
+// (32/M)g .. (32/M)g + 32/M - 1.
+template <int M>
+__device__ __forceinline__ int level_of(int g, int i) { return g + M * i; }
 
 // Permuted input column -> column of W0 (or -1 for a zero column).
+template <int M>
 __device__ __forceinline__ int w0_col(int c, int L) {
+  constexpr int kFpm = kXCol / M;  // features per member
   if (c < kXCol) {
-    const int l = level_of(c >> 3, (c & 7) >> 1);
+    const int l = level_of<M>(c / kFpm, (c % kFpm) >> 1);
     return l < L ? 3 + 2 * l + (c & 1) : -1;
   }
   if (c < kXCol + 3) return c - kXCol;
@@ -131,11 +135,12 @@ __device__ __forceinline__ void scatter_level(const GridDev& gd, int l, const Le
 
 // W0 (64, din) -> B1 (N = 64 hidden, K = 40 inputs, K-major) hi/lo, and, when
 // b2 is given, W0^T -> B2 (N = 48 inputs, K = 64 hidden, K-major) hi/lo.
+template <int M>
 __device__ void stage_w0(const FieldArgs& a, uint8_t* b1_hi, uint8_t* b1_lo, uint8_t* b2_hi,
                          uint8_t* b2_lo) {
   for (int e = threadIdx.x; e < kH * kN2; e += blockDim.x) {
     const int j = e / kN2, c = e - j * kN2;
-    const int src = c < kK1 ? w0_col(c, a.g.L) : -1;
+    const int src = c < kK1 ? w0_col<M>(c, a.g.L) : -1;
     const float v = src >= 0 ? a.w0[j * a.din + src] : 0.0f;
     uint32_t hi, lo;
     tc::tf32_split(v, hi, lo);
@@ -171,13 +176,14 @@ __device__ __forceinline__ void load_grad(const FieldArgs& a, int64_t p, int64_t
 // PAIRED: two levels at a time, all 16 corner gathers issued before any is
 // used (about two L2 round trips per phase instead of four; the backward,
 // which has the registers for it).  Otherwise one level at a time.
-template <bool PAIRED>
+template <bool PAIRED, int M = 4>
 __device__ __forceinline__ void encode_group(const FieldArgs& a, int g, bool live, const float x[3],
-                                             float e[8]) {
+                                             float e[2 * (16 / M)]) {
+  constexpr int kLpm = 16 / M;  // levels per member
   if (!PAIRED) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int l = level_of(g, i);
+    for (int i = 0; i < kLpm; ++i) {
+      const int l = level_of<M>(g, i);
       float e0 = 0.0f, e1 = 0.0f;
       if (live && l < a.active) encode_level(a.table, a.g, l, x, e0, e1);
       e[2 * i] = e0;
@@ -187,8 +193,8 @@ __device__ __forceinline__ void encode_group(const FieldArgs& a, int g, bool liv
   }
   const float2* t2 = reinterpret_cast<const float2*>(a.table);
 #pragma unroll
-  for (int i0 = 0; i0 < 4; i0 += 2) {
-    const int la = level_of(g, i0), lb = level_of(g, i0 + 1);
+  for (int i0 = 0; i0 < kLpm; i0 += 2) {
+    const int la = level_of<M>(g, i0), lb = level_of<M>(g, i0 + 1);
     const bool ua = la < a.active, ub = lb < a.active;  // uniform across the CTA
     LevelCorners ca, cb;
     float2 va[8], vb[8];
@@ -224,6 +230,24 @@ __device__ __forceinline__ void encode_group(const FieldArgs& a, int g, bool liv
   }
 }
 
+// Sums 8 per-lane values over the warp by a reduce-scatter (9 shuffles):
+// lanes 4m .. 4m+3 end with the sum of value m.
+__device__ __forceinline__ float warp_reduce_scatter8(const float v[8], int lane) {
+  constexpr unsigned kAll = 0xffffffffu;
+  float a4[4], a2[2];
+  bool up = lane & 16;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) a4[i] = (up ? v[i + 4] : v[i]) + __shfl_xor_sync(kAll, up ? v[i] : v[i + 4], 16);
+  up = lane & 8;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) a2[i] = (up ? a4[i + 2] : a4[i]) + __shfl_xor_sync(kAll, up ? a4[i] : a4[i + 2], 8);
+  up = lane & 4;
+  float a1 = (up ? a2[1] : a2[0]) + __shfl_xor_sync(kAll, up ? a2[0] : a2[1], 4);
+  a1 += __shfl_xor_sync(kAll, a1, 2);
+  a1 += __shfl_xor_sync(kAll, a1, 1);
+  return a1;
+}
+
 // Sums 16 per-lane values over the warp by a reduce-scatter (16 shuffles):
 // lanes 2m and 2m+1 end with the sum of value m.
 __device__ __forceinline__ float warp_reduce_scatter16(const float v[16], int lane) {
@@ -250,6 +274,24 @@ __device__ __forceinline__ void st_split8(uint32_t ta_hi, uint32_t ta_lo, const 
   for (int i = 0; i < 8; ++i) tc::tf32_split(v[i], hi[i], lo[i]);
   tc::tmem_st8(ta_hi, hi);
   tc::tmem_st8(ta_lo, lo);
+}
+
+__device__ __forceinline__ void st_split4(uint32_t ta_hi, uint32_t ta_lo, const float v[4]) {
+  uint32_t hi[4], lo[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) tc::tf32_split(v[i], hi[i], lo[i]);
+  tc::tmem_st4(ta_hi, hi);
+  tc::tmem_st4(ta_lo, lo);
+}
+// Stores N (4, 8 or 16) values, split into TF32 hi/lo, at columns c_hi / c_lo.
+template <int N>
+__device__ __forceinline__ void st_split(uint32_t ta_hi, uint32_t ta_lo, const float* v) {
+  if (N == 4) {
+    st_split4(ta_hi, ta_lo, v);
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; i += 8) st_split8(ta_hi + i, ta_lo + i, v + i);
+  }
 }
 
 // Issues H = IN W0^T (3xTF32: in_hi w_hi + in_lo w_hi + in_hi w_lo), M=128, N=64, K=40.
@@ -293,7 +335,7 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
   const int oc = a.out_cols;
   const float inv_beta = 1.0f / a.beta;
 
-  stage_w0(a, sm + FwdSmem::b1_hi, sm + FwdSmem::b1_lo, nullptr, nullptr);
+  stage_w0<4>(a, sm + FwdSmem::b1_hi, sm + FwdSmem::b1_lo, nullptr, nullptr);
   for (int e = t; e < kDoutMax * kH; e += kThreads) s_w1[e] = e / kH < oc ? a.w1[e] : 0.0f;
   if (t < kH) s_b0[t] = a.b0[t];
   if (t < kDoutMax) s_b1[t] = t < oc ? a.b1[t] : 0.0f;
@@ -324,7 +366,7 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
     load_point(a, (tile + gridDim.x) * kTile + pt, n, xn);
     {
       float e[8];
-      encode_group<false>(a, g, live, x, e);
+      encode_group<false, 4>(a, g, live, x, e);
       st_split8(tc::taddr(tbase, lb, kColInHi + 8 * g), tc::taddr(tbase, lb, kColInLo + 8 * g), e);
       if (g == 0) {
         const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
@@ -392,7 +434,7 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
 struct BwdSmem {
   static constexpr uint32_t b1_hi = 0, b1_lo = 10240, b2_hi = 20480, b2_lo = 32768, a3 = 45056,
                             b3_hi = a3 + 16 * kSboP, b3_lo = b3_hi + 6 * kSboP, w1 = b3_lo + 6 * kSboP,
-                            b0 = w1 + kDoutMax * kH * 4, dx = b0 + kH * 4, bar = dx + 4 * kTile * 3 * 4,
+                            b0 = w1 + kDoutMax * kH * 4, dx = b0 + kH * 4, bar = dx + 8 * kTile * 3 * 4,
                             bar3 = bar + 8, slot = bar3 + 8, dw1 = slot + 8, db1 = dw1 + kDoutMax * kH * 4,
                             end = db1 + kDoutMax * 4;
 };
@@ -432,9 +474,17 @@ __device__ __forceinline__ void issue_mma3(uint32_t tbase, const uint8_t* sm, bo
   }
 }
 
-template <bool ONE>
-__global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) {
+// M members per TMEM lane quadrant: 128 M threads, each member owning 16/M
+// levels, 32/M input columns and 64/M hidden units of its 32 points.
+constexpr int kBwdMembers = 8;
+
+template <bool ONE, int M>
+__global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
   constexpr int kOc = ONE ? 1 : kDoutMax;
+  constexpr int kNt = 128 * M;      // threads
+  constexpr int kLpm = 16 / M;      // levels per member
+  constexpr int kFpm = 2 * kLpm;    // input features per member
+  constexpr int kHpm = kH / M;      // hidden units per member
   extern __shared__ __align__(1024) uint8_t sm[];
   float* s_w1 = reinterpret_cast<float*>(sm + BwdSmem::w1);
   float* s_b0 = reinterpret_cast<float*>(sm + BwdSmem::b0);
@@ -453,15 +503,15 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
   const bool want_table = a.grad_table != nullptr;
   const bool want_x = a.grad_x != nullptr;
 
-  stage_w0(a, sm + BwdSmem::b1_hi, sm + BwdSmem::b1_lo, sm + BwdSmem::b2_hi, sm + BwdSmem::b2_lo);
-  for (int e = t; e < kDoutMax * kH; e += kThreads) s_w1[e] = e / kH < oc ? a.w1[e] : 0.0f;
+  stage_w0<M>(a, sm + BwdSmem::b1_hi, sm + BwdSmem::b1_lo, sm + BwdSmem::b2_hi, sm + BwdSmem::b2_lo);
+  for (int e = t; e < kDoutMax * kH; e += kNt) s_w1[e] = e / kH < oc ? a.w1[e] : 0.0f;
   if (t < kH) s_b0[t] = a.b0[t];
   float* s_dw1 = reinterpret_cast<float*>(sm + BwdSmem::dw1);
   float* s_db1 = reinterpret_cast<float*>(sm + BwdSmem::db1);
-  for (int e = t; e < kDoutMax * kH; e += kThreads) s_dw1[e] = 0.0f;
+  for (int e = t; e < kDoutMax * kH; e += kNt) s_dw1[e] = 0.0f;
   if (t < kDoutMax) s_db1[t] = 0.0f;
   // constant rows of IN^T: ones (hi) at kOnesRow, zeros above it
-  for (int e = t; e < (kN2 - kOnesRow) * kTile; e += kThreads) {
+  for (int e = t; e < (kN2 - kOnesRow) * kTile; e += kNt) {
     const int r = kOnesRow + e / kTile, c = e % kTile;
     const uint32_t off = tc::kmajor_offset_strided(r, c, kLboP, kSboP);
     st_smem_u32(b3_hi, off, r == kOnesRow ? __float_as_uint(1.0f) : 0u);
@@ -503,9 +553,9 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
     // ---- input rows: TMEM (A of the first MMA) and IN^T (B of the third) ----
     bool ok3 = true;
     {
-      float e[8];
-      encode_group<true>(a, g, live, x, e);
-      st_split8(tc::taddr(tbase, lb, kColInHi + 8 * g), tc::taddr(tbase, lb, kColInLo + 8 * g), e);
+      float e[kFpm];
+      encode_group<(M == 4), M>(a, g, live, x, e);
+      st_split<kFpm>(tc::taddr(tbase, lb, kColInHi + kFpm * g), tc::taddr(tbase, lb, kColInLo + kFpm * g), e);
       // the previous tile's weight-gradient MMAs still read IN^T and dH^T:
       // wait for them only now, so they overlap its scatter and these gathers
       if (pending3) {
@@ -516,10 +566,10 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
         }
       }
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
+      for (int i = 0; i < kFpm; ++i) {
         uint32_t hi, lo;
         tc::tf32_split(e[i], hi, lo);
-        const uint32_t off = tc::kmajor_offset_strided(8 * g + i, pt, kLboP, kSboP);
+        const uint32_t off = tc::kmajor_offset_strided(kFpm * g + i, pt, kLboP, kSboP);
         st_smem_u32(b3_hi, off, hi);
         st_smem_u32(b3_lo, off, lo);
       }
@@ -555,15 +605,19 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       break;
     }
     tc::fence_after_sync();
-    // ---- dH for hidden units 16g..16g+15 ----
+    // ---- dH for this member's hidden units kHpm g .. kHpm g + kHpm - 1 ----
     {
-      float h[16];
-      tc::tmem_ld16(tc::taddr(tbase, lb, kColH + 16 * g), h);
+      float h[kHpm];
+      if (kHpm == 16) {
+        tc::tmem_ld16(tc::taddr(tbase, lb, kColH + kHpm * g), h);
+      } else {
+        tc::tmem_ld8(tc::taddr(tbase, lb, kColH + kHpm * g), h);
+      }
       tc::tmem_wait_ld();
-      float dh[16], act[16];
+      float dh[kHpm], act[kHpm];
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int j = 16 * g + i;
+      for (int i = 0; i < kHpm; ++i) {
+        const int j = kHpm * g + i;
         const float pre = h[i] + s_b0[j];
         float sg;
         softplus_fwd_grad_fast(pre, a.beta, inv_beta, a.thresh, act[i], sg);
@@ -577,11 +631,16 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
 #pragma unroll
       for (int o = 0; o < kOc; ++o) {
         if (o < oc) {
-          float v[16];
+          float v[kHpm];
 #pragma unroll
-          for (int i = 0; i < 16; ++i) v[i] = live ? go[o] * act[i] : 0.0f;
-          const float r = warp_reduce_scatter16(v, lane);
-          if ((lane & 1) == 0) atomicAdd(s_dw1 + o * kH + 16 * g + (lane >> 1), r);
+          for (int i = 0; i < kHpm; ++i) v[i] = live ? go[o] * act[i] : 0.0f;
+          if (kHpm == 16) {
+            const float r = warp_reduce_scatter16(v, lane);
+            if ((lane & 1) == 0) atomicAdd(s_dw1 + o * kH + kHpm * g + (lane >> 1), r);
+          } else {
+            const float r = warp_reduce_scatter8(v, lane);
+            if ((lane & 3) == 0) atomicAdd(s_dw1 + o * kH + kHpm * g + (lane >> 2), r);
+          }
         }
       }
       if (g == 0) {
@@ -595,15 +654,13 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
           }
         }
       }
-      st_split8(tc::taddr(tbase, lb, kColDhHi + 16 * g), tc::taddr(tbase, lb, kColDhLo + 16 * g), dh);
-      st_split8(tc::taddr(tbase, lb, kColDhHi + 16 * g + 8), tc::taddr(tbase, lb, kColDhLo + 16 * g + 8),
-                dh + 8);
+      st_split<kHpm>(tc::taddr(tbase, lb, kColDhHi + kHpm * g), tc::taddr(tbase, lb, kColDhLo + kHpm * g), dh);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
+      for (int i = 0; i < kHpm; ++i) {
         uint32_t hi, lo;
         tc::tf32_split(dh[i], hi, lo);
-        st_smem_u32(a3, tc::kmajor_offset_strided(16 * g + i, pt, kLboP, kSboP), hi);
-        st_smem_u32(a3, tc::kmajor_offset_strided(kH + 16 * g + i, pt, kLboP, kSboP), lo);
+        st_smem_u32(a3, tc::kmajor_offset_strided(kHpm * g + i, pt, kLboP, kSboP), hi);
+        st_smem_u32(a3, tc::kmajor_offset_strided(kH + kHpm * g + i, pt, kLboP, kSboP), lo);
       }
     }
     tc::tmem_wait_st();
@@ -626,10 +683,14 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       break;
     }
     tc::fence_after_sync();
-    // ---- dIN: table-gradient scatter for levels g, g+4, g+8, g+12, dL/dx ----
+    // ---- dIN: table-gradient scatter for this member's levels, dL/dx ----
     {
-      float din[8];
-      tc::tmem_ld8(tc::taddr(tbase, lb, kColH + 8 * g), din);
+      float din[kFpm];
+      if (kFpm == 8) {
+        tc::tmem_ld8(tc::taddr(tbase, lb, kColH + kFpm * g), din);
+      } else {
+        tc::tmem_ld4(tc::taddr(tbase, lb, kColH + kFpm * g), din);
+      }
       tc::tmem_wait_ld();
       float dxl[8];
       if (g == 0) {
@@ -645,15 +706,13 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
       float2* gt2 = reinterpret_cast<float2*>(a.grad_table);
       const float2* t2 = reinterpret_cast<const float2*>(a.table);
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int l = level_of(g, i);
+      for (int i = 0; i < kLpm; ++i) {
+        const int l = level_of<M>(g, i);
         if (l < a.active) {
           LevelCorners c;
           level_corners(a.g, l, x, c);
           const float d0 = live ? din[2 * i] : 0.0f, d1 = live ? din[2 * i + 1] : 0.0f;
-          if (want_table) {
-            scatter_level(a.g, l, c, d0, d1, live, a.pair16, gt2, lane);
-          }
+          if (want_table) scatter_level(a.g, l, c, d0, d1, live, a.pair16, gt2, lane);
           if (want_x && live) {
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
@@ -678,7 +737,7 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
         for (int d = 0; d < 3; ++d) {
           float s = 0.0f;
 #pragma unroll
-          for (int m = 0; m < 4; ++m) s += s_dx[(m * kTile + pt) * 3 + d];
+          for (int m = 0; m < M; ++m) s += s_dx[(m * kTile + pt) * 3 + d];
           a.grad_x[3 * p + d] = s;
         }
       }
@@ -705,7 +764,7 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
           if (c == kOnesRow) {
             if (a.grad_b0) atomicAdd(a.grad_b0 + j, v[i]);
           } else if (c < kK1 && a.grad_w0) {
-            const int col = w0_col(c, a.g.L);
+            const int col = w0_col<M>(c, a.g.L);
             if (col >= 0 && v[i] != 0.0f) atomicAdd(a.grad_w0 + j * a.din + col, v[i]);
           }
         }
@@ -713,7 +772,7 @@ __global__ void __launch_bounds__(kThreads, 1) field_bwd_tc_kernel(FieldArgs a) 
     }
     // dW1 / db1 (block sums in shared memory)
     if (a.grad_w1)
-      for (int e = t; e < oc * kH; e += kThreads)
+      for (int e = t; e < oc * kH; e += kNt)
         if (s_dw1[e] != 0.0f) atomicAdd(a.grad_w1 + e, s_dw1[e]);
     if (a.grad_b1 && t < oc && s_db1[t] != 0.0f) atomicAdd(a.grad_b1 + t, s_db1[t]);
   }
@@ -749,16 +808,17 @@ int field_fwd_tc(const FieldArgs& a, cudaStream_t st) {
 }
 
 int field_bwd_tc(const FieldArgs& a, cudaStream_t st) {
-  const void* fn = a.out_cols == 1 ? reinterpret_cast<const void*>(field_bwd_tc_kernel<true>)
-                                   : reinterpret_cast<const void*>(field_bwd_tc_kernel<false>);
+  constexpr int M = kBwdMembers;
+  const void* fn = a.out_cols == 1 ? reinterpret_cast<const void*>(field_bwd_tc_kernel<true, M>)
+                                   : reinterpret_cast<const void*>(field_bwd_tc_kernel<false, M>);
   SN_TRY(set_smem(fn, kBwdSmemBytes, "field_bwd"));
   const int64_t n_tiles = (a.cap + kTile - 1) / kTile;
   const int64_t cap = num_sms();
   const unsigned grid = (unsigned)(n_tiles < cap ? n_tiles : cap);
   if (a.out_cols == 1)
-    field_bwd_tc_kernel<true><<<grid, kThreads, kBwdSmemBytes, st>>>(a);
+    field_bwd_tc_kernel<true, M><<<grid, 128 * M, kBwdSmemBytes, st>>>(a);
   else
-    field_bwd_tc_kernel<false><<<grid, kThreads, kBwdSmemBytes, st>>>(a);
+    field_bwd_tc_kernel<false, M><<<grid, 128 * M, kBwdSmemBytes, st>>>(a);
   return check_launch("field_bwd");
 }
 
