@@ -4,7 +4,7 @@
 // A CTA owns 128-point tiles (persistent over tiles) with 16 warps: warp w
 // serves TMEM lane quadrant q = w % 4 (points 32q..32q+31 of the tile) as
 // member g = w / 4 of that quadrant's group of four.  The four members split
-// the per-point work -- hash-grid levels g, g+4, g+8, g+12, hidden units 16g..16g+15 --
+// the per-point work -- hash-grid levels (interleaved, see level_of), hidden units --
 // and write their parts of each point's row straight into the point's TMEM
 // lane, where the tensor core reads it as the A operand.  One thread issues
 // the MMAs; everyone else waits on an mbarrier (bounded).
