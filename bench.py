@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--cpu-sample-patches", type=int, default=8)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-clocks", action="store_true")
+    p.add_argument("--serve", choices=["small", "full", "off"], default="small",
+                   help="serving-loop trace after the training measurement (p50/p99 latency)")
     return p.parse_args()
 
 
@@ -268,6 +270,44 @@ def run_ours(args, world, rank, local):
         out["clocks"] = clk
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, tr, scene, rig, budget_s=20.0)
+    if args.serve != "off":
+        del tr, ds, pool, host, dev_in
+        torch.cuda.empty_cache()
+        out["serve"] = run_serve(args.serve, dev)
+    return out
+
+
+def run_serve(size: str, dev) -> dict:
+    """The serving loop on a seeded request trace, served (CUDA graphs, short
+    requests between reconstruction slices) and plain (one request at a time,
+    eager), under an HBM budget that forces offloads."""
+    from supernormal_gb300.serve import ServedObject, Server, object_specs, poisson_trace
+
+    if size == "full":   # 32 objects, 8-100 views at 256^2-1024^2, tables 2^17-2^21
+        cfg = dict(objects=32, views=(8, 100), res=(256, 1024), log2_table=(17, 21), duration=20.0, rate=4.0,
+                   budget_frac=0.6)
+    else:
+        cfg = dict(objects=8, views=(8, 24), res=(192, 384), log2_table=(17, 19), duration=6.0, rate=6.0,
+                   budget_frac=0.6)
+    t0 = time.perf_counter()
+    specs = object_specs(cfg["objects"], seed=5, views=cfg["views"], res=cfg["res"], log2_table=cfg["log2_table"])
+    objs = [ServedObject(s, dev, batch=512) for s in specs]
+    total = sum(o.nbytes() for o in objs)
+    budget = int(cfg["budget_frac"] * total)
+    setup_s = time.perf_counter() - t0
+    trace = poisson_trace(len(objs), cfg["duration"], cfg["rate"], seed=11, recon_iters=100)
+    out = {"config": {"objects": len(objs), "views": list(cfg["views"]), "resolution": list(cfg["res"]),
+                      "log2_table": list(cfg["log2_table"]), "patches_per_iteration": 512,
+                      "recon_block_iterations": 100, "query_grid": 256, "arrival_rate_per_s": cfg["rate"],
+                      "trace_s": cfg["duration"], "requests": len(trace),
+                      "hbm_budget_gb": budget / 1e9, "objects_total_gb": total / 1e9,
+                      "setup_s": setup_s}}
+    for policy in ("served", "plain"):
+        srv = Server(objs, budget, query_res=256, slice_iters=10)
+        srv.fit_budget()
+        r = srv.run(trace, policy)
+        r["swaps"] = srv.swaps
+        out[policy] = r
     return out
 
 

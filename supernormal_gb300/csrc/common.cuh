@@ -52,6 +52,11 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 // Number of SMs of the current device (cached per process; single-GPU use).
 int num_sms();
 
+// Raises a kernel's dynamic shared-memory limit to `bytes` once per (device,
+// kernel); later calls only look the pair up, so launches made while a stream
+// is being captured issue no attribute calls.
+int ensure_smem_limit(const void* fn, size_t bytes, const char* what);
+
 inline unsigned int div_up(int64_t a, int64_t b) {
   return (unsigned int)((a + b - 1) / b);
 }

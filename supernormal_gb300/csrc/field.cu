@@ -618,12 +618,7 @@ int sn_field_grad_fwd(int64_t n, const int32_t* count, const float* x, const flo
   SN_TRY(fill_field_args(a, n, count, x, table, grid, active_levels, mlp, 1));
   SN_REQUIRE(grad != nullptr, "field_grad_fwd: grad is null");
   if (n == 0) return SN_OK;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(field_grad_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kFwdSmem);
-    attr = true;
-  }
+  SN_TRY(ensure_smem_limit(reinterpret_cast<const void*>(field_grad_fwd_kernel), kFwdSmem, "field_grad_fwd_kernel"));
   field_grad_fwd_kernel<<<stride_grid(n, 128, 8), 128, kFwdSmem, as_stream(stream)>>>(a, sdf, grad);
   return check_launch("field_grad_fwd");
 }
@@ -642,12 +637,7 @@ int sn_field_grad_bwd(int64_t n, const int32_t* count, const float* x, const flo
   a.grad_b1 = grad_b1;
   if (n == 0) return SN_OK;
   GradBwdArgs b{grad_grad, grad_sdf};
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(field_grad_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kGradBwdSmem);
-    attr = true;
-  }
+  SN_TRY(ensure_smem_limit(reinterpret_cast<const void*>(field_grad_bwd_kernel), kGradBwdSmem, "field_grad_bwd_kernel"));
   field_grad_bwd_kernel<<<stride_grid(n, kBwdThreads, 1), kBwdThreads, kGradBwdSmem,
                           as_stream(stream)>>>(a, b);
   return check_launch("field_grad_bwd");

@@ -781,14 +781,6 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
   if (warp == 0) tc::tmem_dealloc(tbase, kCols);
 }
 
-int set_smem(const void* fn, size_t bytes, const char* what) {
-  const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (e != cudaSuccess) {
-    set_error("%s: cannot set shared memory limit: %s", what, cudaGetErrorString(e));
-    return SN_ERR_CUDA;
-  }
-  return SN_OK;
-}
 
 }  // namespace
 
@@ -796,7 +788,7 @@ int set_smem(const void* fn, size_t bytes, const char* what) {
 int field_fwd_tc(const FieldArgs& a, cudaStream_t st) {
   const void* fn = a.out_cols == 1 ? reinterpret_cast<const void*>(field_fwd_tc_kernel<true>)
                                    : reinterpret_cast<const void*>(field_fwd_tc_kernel<false>);
-  SN_TRY(set_smem(fn, kFwdSmemBytes, "field_fwd"));
+  SN_TRY(ensure_smem_limit(fn, kFwdSmemBytes, "field_fwd"));
   const int64_t n_tiles = (a.cap + kTile - 1) / kTile;
   const int64_t cap = 2LL * num_sms();
   const unsigned grid = (unsigned)(n_tiles < cap ? n_tiles : cap);
@@ -811,7 +803,7 @@ int field_bwd_tc(const FieldArgs& a, cudaStream_t st) {
   constexpr int M = kBwdMembers;
   const void* fn = a.out_cols == 1 ? reinterpret_cast<const void*>(field_bwd_tc_kernel<true, M>)
                                    : reinterpret_cast<const void*>(field_bwd_tc_kernel<false, M>);
-  SN_TRY(set_smem(fn, kBwdSmemBytes, "field_bwd"));
+  SN_TRY(ensure_smem_limit(fn, kBwdSmemBytes, "field_bwd"));
   const int64_t n_tiles = (a.cap + kTile - 1) / kTile;
   const int64_t cap = num_sms();
   const unsigned grid = (unsigned)(n_tiles < cap ? n_tiles : cap);

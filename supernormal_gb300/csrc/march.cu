@@ -174,6 +174,34 @@ int pack_counts(int64_t n, const int32_t* counts, int32_t* packed, int32_t* tota
   return check_launch("pack_counts", 3);
 }
 
+struct SmemLimit {
+  int dev;
+  const void* fn;
+  size_t bytes;
+};
+static std::mutex g_smem_mu;
+static SmemLimit g_smem_set[64];
+static int g_smem_n = 0;
+
+int ensure_smem_limit(const void* fn, size_t bytes, const char* what) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_error("%s: cudaGetDevice failed: %s", what, cudaGetErrorString(e));
+    return SN_ERR_CUDA;
+  }
+  std::lock_guard<std::mutex> lock(g_smem_mu);
+  for (int i = 0; i < g_smem_n; ++i)
+    if (g_smem_set[i].dev == dev && g_smem_set[i].fn == fn && g_smem_set[i].bytes >= bytes) return SN_OK;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) {
+    set_error("%s: cannot set the shared memory limit to %zu bytes: %s", what, bytes, cudaGetErrorString(e));
+    return SN_ERR_CUDA;
+  }
+  if (g_smem_n < 64) g_smem_set[g_smem_n++] = SmemLimit{dev, fn, bytes};
+  return SN_OK;
+}
+
 // Static scratch of sn_pack_counts_static: tile sums of up to kPackStaticMaxTiles
 // tiles.  Its device address is looked up once per device (with that device
 // current) and cached.

@@ -21,14 +21,6 @@ constexpr uint32_t kTcCols = 256;  // TMEM columns allocated per CTA
 // a third of the SM's 228 KB, so at most two CTAs (2 x 256 TMEM columns) share an SM.
 constexpr size_t kTcSmemFloor = 80 * 1024;
 
-static int set_smem_limit(const void* fn, size_t bytes, const char* what) {
-  const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (e != cudaSuccess) {
-    set_error("%s: cannot set shared memory limit: %s", what, cudaGetErrorString(e));
-    return SN_ERR_CUDA;
-  }
-  return SN_OK;
-}
 
 struct LinearTcArgs {
   int64_t n;
@@ -177,7 +169,7 @@ int sn_linear_tc(int64_t n, int k, const float* x, const float* w, const float* 
   // The shared-memory request also caps residency at two CTAs per SM, so the
   // two 256-column TMEM allocations per SM never wait on each other.
   const size_t smem = kTcSmemFloor;
-  SN_TRY(set_smem_limit(reinterpret_cast<const void*>(linear_tc_kernel), smem, "linear_tc"));
+  SN_TRY(ensure_smem_limit(reinterpret_cast<const void*>(linear_tc_kernel), smem, "linear_tc"));
   const int64_t n_tiles = (n + kTcRows - 1) / kTcRows;
   const int64_t grid = n_tiles < 2LL * num_sms() ? n_tiles : 2LL * num_sms();
   linear_tc_kernel<<<(unsigned)grid, kTcRows, smem, as_stream(stream)>>>(a);

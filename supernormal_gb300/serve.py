@@ -1,0 +1,341 @@
+"""Serving loop over many resident reconstruction objects.
+
+A stand-in for a reconstruction service: each object is one SuperNormal
+reconstruction (an analytic scene seen by its own views, a hash-grid SDF, the
+variance, Adam state and an occupancy grid) and requests arrive as a seeded
+Poisson process:
+
+* ``recon``  -- a block of training iterations (exp_runner.py:147-210),
+* ``render`` -- a normal map of the current SDF at a new camera pose
+  (NeuSRenderer.render in eval mode over the image's 3x3 patches),
+* ``query``  -- the SDF on a regular grid, the input of mesh extraction
+  (models/renderer.py:9-34 ``extract_fields``).
+
+Objects are admitted under a fixed HBM budget: the least recently used
+resident objects are offloaded (persistent state copied to pinned host
+memory, every storage shrunk to zero bytes) to make room, and brought back on
+their next request.  Two service policies run the same trace:
+
+* ``plain``  -- one request at a time in arrival order, eager launches;
+* ``served`` -- training iterations replayed as CUDA graphs, and render /
+  query requests served between iterations of a running reconstruction block
+  (the block is resumed afterwards), so short requests do not wait behind
+  long blocks.
+
+Latency = completion (after a device synchronisation) minus arrival.
+"""
+from __future__ import annotations
+
+import math
+import time
+from collections import deque
+from dataclasses import dataclass, field
+from typing import Optional
+
+import torch
+
+from . import scenes
+from .fields import SDFNetwork, SingleVarianceNetwork
+from .renderer import NeuSRenderer, near_far_from_sphere
+from .trainer import FusedTrainer, GraphStep, TrainConfig
+
+
+@dataclass
+class ObjectSpec:
+    index: int
+    seed: int
+    n_views: int
+    res: int
+    log2_table: int
+
+
+def object_specs(n_objects: int, seed: int = 0, views=(8, 100), res=(256, 1024),
+                 log2_table=(17, 21)) -> list:
+    """Seeded object sizes: views, square resolution and table size drawn uniformly."""
+    g = torch.Generator().manual_seed(seed)
+    out = []
+    for i in range(n_objects):
+        nv = int(torch.randint(views[0], views[1] + 1, (1,), generator=g))
+        r = int(torch.randint(res[0], res[1] + 1, (1,), generator=g)) // 3 * 3
+        t = int(torch.randint(log2_table[0], log2_table[1] + 1, (1,), generator=g))
+        out.append(ObjectSpec(i, seed * 1000 + i, nv, r, t))
+    return out
+
+
+class ServedObject:
+    """One reconstruction: dataset views, field, optimiser state, occupancy grid."""
+
+    def __init__(self, spec: ObjectSpec, device, batch: int = 512, step_size: float = 2.0 / 1024):
+        self.spec = spec
+        dev = torch.device(device)
+        scene = scenes.random_scene(spec.seed)
+        rig = scenes.ring_cameras(spec.n_views, spec.res, spec.res, radius=3.0, elevation_deg=20.0)
+        self.ds = scenes.SyntheticDataset(scene, rig, dev)
+        self.scene = scene
+        enc = dict(otype="HashGrid", n_levels=16, n_features_per_level=2, log2_hashmap_size=spec.log2_table,
+                   base_resolution=16, per_level_scale=1.447)
+        torch.manual_seed(spec.seed)
+        net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=enc, input_concat=True).to(dev)
+        var = SingleVarianceNetwork(0.3).to(dev)
+        cfg = TrainConfig(batch_size=batch, step_size=step_size, occ_update_freq=8, occ_warmup_steps=16,
+                          increase_bandwidth_every=100, end_iter=5000, seed=spec.seed)
+        self.tr = FusedTrainer(net, var, cfg, device=dev)
+        self.graph = GraphStep(self.tr)
+        self.renderer = NeuSRenderer(net, var)
+        self.renderer.occupancy_grid = self.tr.grid
+        self.renderer.sampling_step_size = step_size
+        self.gen = torch.Generator(device=dev).manual_seed(spec.seed)
+        self.resident = True
+        self.last_used = 0.0
+        self._host: dict = {}
+        self._state, self._work = self._classify()
+        self._sizes = [st.nbytes() for st in self._state], [st.nbytes() for st in self._work]
+        self._nbytes = sum(self._sizes[0]) + sum(self._sizes[1])
+
+    # ---- residency -------------------------------------------------------
+    def _classify(self):
+        """Storages holding persistent state (copied on offload) vs workspace."""
+        tr, ds = self.tr, self.ds
+        state_t = [tr.params, tr.exp_avg, tr.exp_avg_sq, tr.iter_dev, tr.lr_dev, tr.adam_step_dev,
+                   tr.status, ds.normals, ds.masks, ds.V_inverse_all, ds.rays_all, ds.pose_all,
+                   ds.intrinsics_all]
+        state_t += list(tr.grid.buffers()) + list(tr.net.buffers())
+        state, seen = [], set()
+        for t in state_t:
+            st = t.untyped_storage()
+            if st.data_ptr() not in seen and t.is_cuda:
+                seen.add(st.data_ptr())
+                state.append(st)
+        work = []
+        for t in list(vars(tr).values()) + list(self.graph.inputs):
+            if isinstance(t, torch.Tensor) and t.is_cuda:
+                st = t.untyped_storage()
+                if st.data_ptr() not in seen:
+                    seen.add(st.data_ptr())
+                    work.append(st)
+        return state, work
+
+    def nbytes(self) -> int:
+        """Device bytes of the object when resident (fixed at construction)."""
+        return self._nbytes
+
+    def offload(self) -> None:
+        if not self.resident:
+            return
+        torch.cuda.synchronize()
+        self._host = {}
+        for i, st in enumerate(self._state):
+            h = torch.empty(st.nbytes(), dtype=torch.uint8, pin_memory=True)
+            h.untyped_storage().copy_(st)
+            self._host[i] = h
+        for st in self._state + self._work:
+            st.resize_(0)
+        self.graph.invalidate()
+        self.resident = False
+
+    def onload(self) -> None:
+        if self.resident:
+            return
+        ss, ws = self._sizes
+        for st, n in zip(self._state, ss):
+            st.resize_(n)
+        for st, n in zip(self._work, ws):
+            st.resize_(n)
+        for i, st in enumerate(self._state):
+            st.copy_(self._host[i].untyped_storage(), non_blocking=True)
+        self.tr.grads.zero_()          # zero at rest (Adam consumes and clears them)
+        self._host = {}
+        self.graph.invalidate()
+        self.resident = True
+
+    # ---- requests --------------------------------------------------------
+    def train_iterations(self, n: int, graphs: bool) -> None:
+        for _ in range(n):
+            batch = self.ds.gen_random_patches(self.tr.B, generator=self.gen)
+            if graphs:
+                self.graph.step(batch)
+            else:
+                self.tr.train_step(*batch)
+
+    @torch.no_grad()
+    def render(self, pose_seed: int, chunk: int = 4096) -> torch.Tensor:
+        """Normal map (H, W, 3) of the current field at a seeded new pose."""
+        g = torch.Generator().manual_seed(pose_seed)
+        az = float(torch.rand(1, generator=g)) * 2 * math.pi
+        el = 10.0 + 30.0 * float(torch.rand(1, generator=g))
+        rig = scenes.ring_cameras(1, self.spec.res, self.spec.res, radius=3.0, elevation_deg=el)
+        c, s = math.cos(az), math.sin(az)
+        rot = torch.tensor([[c, -s, 0.0, 0.0], [s, c, 0.0, 0.0], [0.0, 0.0, 1.0, 0.0], [0.0, 0.0, 0.0, 1.0]],
+                           dtype=rig.poses.dtype)
+        rig.poses = rot @ rig.poses
+        view = scenes.SyntheticDataset(self.scene, rig, self.tr.device)
+        H = W = self.spec.res
+        ph, pw = H // 3, W // 3
+        blk = lambda t: t[0].reshape(ph, 3, pw, 3, *t.shape[3:]).transpose(1, 2).reshape(
+            ph * pw, 3, 3, *t.shape[3:]).contiguous()
+        rays_d = blk(view.rays_all)
+        vinv = blk(view.V_inverse_all)
+        rays_o = view.pose_all[0, :3, 3].expand(rays_d.shape).contiguous()
+        plane_n = view.pose_all[0, :3, 2].expand(rays_d.shape[0], 3).contiguous()
+        out = torch.empty_like(rays_d)
+        self.renderer.gradient_method = "dfd"
+        for a in range(0, rays_d.shape[0], chunk):
+            b = min(a + chunk, rays_d.shape[0])
+            near, far = near_far_from_sphere(rays_o[a:b, 1, 1].contiguous(), rays_d[a:b, 1, 1].contiguous())
+            r = self.renderer.render(rays_o[a:b], rays_d[a:b], plane_n[a:b], near, far, vinv[a:b],
+                                     mode="eval")
+            out[a:b] = r["comp_normal"]
+        return out.reshape(ph, pw, 3, 3, 3).transpose(1, 2).reshape(H, W, 3)
+
+    @torch.no_grad()
+    def query(self, res: int = 256, chunk: int = 1 << 22) -> torch.Tensor:
+        """SDF on a res^3 grid over [-1, 1]^3 (models/renderer.py:9-34)."""
+        dev = self.tr.device
+        lin = torch.linspace(-1.0, 1.0, res, device=dev)
+        out = torch.empty(res ** 3, device=dev)
+        n_plane = res * res
+        for z0 in range(0, res, max(1, chunk // n_plane)):
+            z1 = min(res, z0 + max(1, chunk // n_plane))
+            zz, yy, xx = torch.meshgrid(lin[z0:z1], lin, lin, indexing="ij")
+            pts = torch.stack([xx, yy, zz], dim=-1).reshape(-1, 3).contiguous()
+            out[z0 * n_plane:z1 * n_plane] = self.tr.net.sdf_raw(pts).reshape(-1)
+        return out.reshape(res, res, res)
+
+
+@dataclass
+class Request:
+    rid: int
+    kind: str            # 'recon' | 'render' | 'query'
+    obj: int
+    arrival: float       # seconds after the start of the trace
+    iters: int = 0       # recon: iterations left
+    done_at: Optional[float] = None
+    rays: int = 0
+
+
+def poisson_trace(n_objects: int, duration: float, rate: float, seed: int = 0,
+                  mix=(0.4, 0.35, 0.25), recon_iters: int = 100) -> list:
+    """Seeded arrivals over ``duration`` seconds at ``rate`` per second."""
+    g = torch.Generator().manual_seed(seed)
+    t, out = 0.0, []
+    while True:
+        t += float(-math.log(1.0 - float(torch.rand(1, generator=g))) / rate)
+        if t > duration:
+            break
+        u = float(torch.rand(1, generator=g))
+        kind = "recon" if u < mix[0] else ("render" if u < mix[0] + mix[1] else "query")
+        obj = int(torch.randint(0, n_objects, (1,), generator=g))
+        out.append(Request(len(out), kind, obj, t, recon_iters if kind == "recon" else 0))
+    return out
+
+
+class Server:
+    """Runs a request trace over ServedObjects under an HBM budget."""
+
+    def __init__(self, objects: list, budget_bytes: int, query_res: int = 256, slice_iters: int = 10):
+        self.objects = objects
+        self.budget = budget_bytes
+        self.query_res = query_res
+        self.slice_iters = slice_iters
+        self.swaps = 0
+
+    def resident_bytes(self) -> int:
+        return sum(o.nbytes() for o in self.objects if o.resident)
+
+    def admit(self, obj: ServedObject, now: float) -> None:
+        """Make ``obj`` resident, offloading least recently used objects as needed."""
+        obj.last_used = now
+        if obj.resident:
+            return
+        need = obj.nbytes()
+        for o in sorted((o for o in self.objects if o.resident), key=lambda o: o.last_used):
+            if self.resident_bytes() + need <= self.budget:
+                break
+            o.offload()
+            self.swaps += 1
+        obj.onload()
+        self.swaps += 1
+
+    def fit_budget(self) -> None:
+        """Initial admission: the first objects that fit stay resident."""
+        used = 0
+        for o in self.objects:
+            if used + o.nbytes() <= self.budget:
+                used += o.nbytes()
+            else:
+                o.offload()
+
+    def run(self, trace: list, policy: str) -> dict:
+        graphs = policy == "served"
+        reqs = [Request(r.rid, r.kind, r.obj, r.arrival, r.iters) for r in trace]
+        pending = deque(sorted(reqs, key=lambda r: r.arrival))
+        recon_q: deque = deque()
+        short_q: deque = deque()
+        fifo: deque = deque()
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0
+        busy = 0.0
+        train_rays = render_rays = 0
+
+        def arrive():
+            while pending and pending[0].arrival <= now():
+                r = pending.popleft()
+                if policy == "plain":
+                    fifo.append(r)
+                elif r.kind == "recon":
+                    recon_q.append(r)
+                else:
+                    short_q.append(r)
+
+        def finish(r):
+            torch.cuda.synchronize()
+            r.done_at = now()
+
+        while pending or recon_q or short_q or fifo:
+            arrive()
+            if policy == "plain":
+                r = fifo.popleft() if fifo else None
+            else:
+                r = short_q.popleft() if short_q else (recon_q[0] if recon_q else None)
+            if r is None:
+                time.sleep(max(0.0, min(0.002, pending[0].arrival - now())) if pending else 0.0)
+                continue
+            s = now()
+            obj = self.objects[r.obj]
+            self.admit(obj, s)
+            if r.kind == "recon":
+                k = r.iters if policy == "plain" else min(r.iters, self.slice_iters)
+                obj.train_iterations(k, graphs)
+                r.iters -= k
+                train_rays += k * obj.tr.B * obj.tr.P
+                if r.iters == 0:
+                    finish(r)
+                    if policy != "plain":
+                        recon_q.popleft()
+                else:
+                    torch.cuda.synchronize()   # the slice is done: look at new arrivals
+            elif r.kind == "render":
+                img = obj.render(pose_seed=r.rid)
+                render_rays += img.shape[0] * img.shape[1]
+                finish(r)
+            else:
+                obj.query(self.query_res)
+                finish(r)
+            busy += now() - s
+        span = now()
+        lat = {k: sorted(r.done_at - r.arrival for r in reqs if r.kind == k) for k in ("recon", "render", "query")}
+        allv = sorted(r.done_at - r.arrival for r in reqs)
+
+        def pct(v, p):
+            if not v:
+                return None
+            i = min(len(v) - 1, max(0, int(math.ceil(p / 100.0 * len(v))) - 1))
+            return 1e3 * v[i]
+
+        return {
+            "policy": policy, "requests": len(reqs), "makespan_s": span, "busy_s": busy,
+            "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
+            "by_kind": {k: {"n": len(v), "p50_ms": pct(v, 50), "p99_ms": pct(v, 99)} for k, v in lat.items()},
+            "rays_per_s": (train_rays + render_rays) / span if span > 0 else 0.0,
+            "train_rays": train_rays, "render_rays": render_rays,
+        }

@@ -386,3 +386,61 @@ class FusedTrainer:
 def _center_ptr(t: Tensor, kc: int) -> int:
     """Address of pixel kc of patch 0 in a (B, H, W, 3) tensor."""
     return t.data_ptr() + kc * 3 * t.element_size()
+
+
+class GraphStep:
+    """A training iteration of a FusedTrainer as CUDA-graph replays.
+
+    ``run_step`` (fixed step size and active levels) is captured over static
+    input buffers; the post-warm-up occupancy update is captured too.  Both
+    are re-captured when the step size or the bandwidth changes, and after
+    the trainer's storages were reallocated (``invalidate``).  During the
+    occupancy warm-up the update runs eagerly."""
+
+    def __init__(self, trainer: FusedTrainer):
+        self.tr = trainer
+        c, dev = trainer.cfg, trainer.device
+        B, H, W = trainer.B, c.patch_h, c.patch_w
+        self.inputs = (torch.empty((B, H, W, 3), device=dev), torch.empty((B, H, W, 3), device=dev),
+                       torch.empty((B, 3), device=dev), torch.empty((B, H, W, 3, 3), device=dev),
+                       torch.empty((B, H, W, 3), device=dev), torch.empty((B, H, W, 1), device=dev))
+        self._step = None
+        self._step_key = None
+        self._occ = None
+
+    def invalidate(self) -> None:
+        self._step = self._step_key = self._occ = None
+
+    def _capture(self, fn):
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            fn()
+        return g
+
+    def step(self, batch=None) -> Tensor:
+        """One iteration; ``batch`` (6 tensors as from gen_random_patches) is
+        copied into the static inputs, or the caller filled ``inputs``."""
+        tr, c = self.tr, self.tr.cfg
+        if tr.profile:
+            raise RuntimeError("GraphStep does not record stage events")
+        it = tr.iter_step
+        if c.occ_update_freq > 0 and it % c.occ_update_freq == 0:
+            if it < c.occ_warmup_steps:
+                tr.occupancy_update(it)
+            else:
+                if self._occ is None:
+                    self._occ = self._capture(lambda: tr.occupancy_update(c.occ_warmup_steps))
+                self._occ.replay()
+        if c.increase_bandwidth_every > 0 and it % c.increase_bandwidth_every == 0:
+            tr.net.increase_bandwidth()
+        if batch is not None:
+            for dst, src in zip(self.inputs, batch):
+                dst.copy_(src, non_blocking=True)
+        key = (tr.step_size(it), tr.net.active_levels())
+        if self._step is None or key != self._step_key:
+            self._step = self._capture(lambda: tr.run_step(*self.inputs, key[0], key[1]))
+            self._step_key = key
+        self._step.replay()
+        tr.iter_step += 1
+        return tr.loss_out

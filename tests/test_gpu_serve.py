@@ -1,0 +1,73 @@
+"""CUDA-graph training step and the serving loop (GPU)."""
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def test_graph_step_matches_eager(built_lib):
+    """The captured iteration gives the eager iteration's loss (the forward is
+    deterministic; later steps differ only by float atomics order)."""
+    from supernormal_gb300 import scenes
+    from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
+    from supernormal_gb300.trainer import FusedTrainer, GraphStep, TrainConfig
+
+    ds = scenes.SyntheticDataset(scenes.sphere(0.5), scenes.ring_cameras(6, 96, 96, elevation_deg=20),
+                                 torch.device("cuda"))
+    enc = dict(otype="HashGrid", n_levels=16, n_features_per_level=2, log2_hashmap_size=15,
+               base_resolution=16, per_level_scale=1.447)
+
+    def make():
+        torch.manual_seed(0)
+        net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=enc, input_concat=True).cuda()
+        var = SingleVarianceNetwork(0.3).cuda()
+        cfg = TrainConfig(batch_size=128, step_size=1.0 / 96, occ_update_freq=4, occ_warmup_steps=4,
+                          increase_bandwidth_every=0, end_iter=100, seed=3)
+        net.bindwidth = 16
+        return FusedTrainer(net, var, cfg)
+
+    g = torch.Generator(device="cuda").manual_seed(1)
+    batches = [ds.gen_random_patches(128, generator=g) for _ in range(12)]
+    eager, graphed = make(), make()
+    gs = GraphStep(graphed)
+    le, lg = [], []
+    for b in batches:
+        le.append(eager.train_step(*b).clone())
+        lg.append(gs.step(b).clone())
+    torch.cuda.synchronize()
+    eager.check_status()
+    graphed.check_status()
+    assert torch.equal(le[0], lg[0])
+    for a, b in zip(le, lg):
+        assert torch.allclose(a, b, rtol=2e-3, atol=1e-6), (a, b)
+    assert gs._step is not None and gs._occ is not None
+
+
+def test_serving_loop_small_trace(built_lib):
+    from supernormal_gb300.serve import ServedObject, Server, object_specs, poisson_trace
+
+    specs = object_specs(3, seed=1, views=(6, 8), res=(96, 120), log2_table=(15, 16))
+    objs = [ServedObject(s, "cuda", batch=128, step_size=1.0 / 96) for s in specs]
+    budget = objs[0].nbytes() + objs[1].nbytes()         # two of three fit: forces offloads
+    trace = poisson_trace(3, duration=1.5, rate=8.0, seed=2, recon_iters=12)
+    assert len(trace) > 4
+    srv = Server(objs, budget, query_res=64, slice_iters=4)
+    srv.fit_budget()
+    assert srv.resident_bytes() <= budget
+    res = srv.run(trace, "served")
+    assert res["requests"] == len(trace) and res["p50_ms"] is not None and res["p99_ms"] >= res["p50_ms"]
+    assert srv.resident_bytes() <= budget
+    assert srv.swaps > 0
+    res_plain = Server(objs, budget, query_res=64).run(trace, "plain")
+    assert res_plain["requests"] == len(trace)
+    for o in objs:
+        if o.resident:
+            o.tr.check_status()
+    # an offloaded object comes back with its state intact
+    o = objs[0]
+    if not o.resident:
+        o.onload()
+    p = o.tr.params.clone()
+    o.offload()
+    o.onload()
+    assert torch.equal(p, o.tr.params)
