@@ -224,6 +224,13 @@ int sn_center_points(int64_t cap, const int32_t* count, const int64_t* ray_indic
                      const float* rays_d, const int32_t* end_packed, const int32_t* n_ends,
                      float* xyz, int32_t* n_points, void* stream) {
   SN_REQUIRE(cap >= 0, "center_points: cap < 0");
+  if (cap == 0) {  // no samples: no points
+    if (n_points && cudaMemsetAsync(n_points, 0, sizeof(int32_t), as_stream(stream)) != cudaSuccess) {
+      set_error("center_points: memset failed");
+      return SN_ERR_CUDA;
+    }
+    return SN_OK;
+  }
   SN_REQUIRE(n_ends != nullptr && end_packed != nullptr, "center_points: null end info");
   center_points_kernel<<<stride_grid(cap > 0 ? cap : 1, 256, 8), 256, 0, as_stream(stream)>>>(
       cap, count, ray_indices, t_starts, t_ends, rays_o, rays_d, end_packed, n_ends, xyz, n_points);

@@ -117,6 +117,8 @@ class NeuSRenderer:
         def alpha_fn(t_starts, t_ends, ray_indices):
             n = t_starts.shape[0]
             dev = t_starts.device
+            if n == 0:
+                return torch.empty((0, 1), device=dev)
             st = stream_handle()
             ts = t_starts.reshape(-1).contiguous()
             te = t_ends.reshape(-1).contiguous()

@@ -281,3 +281,21 @@ def test_training_reduces_loss(scene):
         last = v
     tr.check_status()
     assert np.isfinite(last) and last < first
+
+
+def test_render_with_no_samples_returns_zeros(scene):
+    """An empty occupancy grid marches no sample: the culling callback gets
+    empty tensors and the render is all zeros (the reference's torch ops
+    accept the empty case too)."""
+    from supernormal_gb300.renderer import NeuSRenderer, near_far_from_sphere
+
+    net, var = make()
+    r = NeuSRenderer(net, var)
+    r.occupancy_grid = full_grid()
+    r.occupancy_grid._binary.zero_()
+    g = torch.Generator(device="cuda").manual_seed(4)
+    ro, rd, pn, vinv, _, _ = scene.gen_random_patches(16, generator=g)
+    near, far = near_far_from_sphere(ro[:, 1, 1], rd[:, 1, 1])
+    out = r.render(ro, rd, pn, near, far, vinv, mode="eval")
+    assert out["gradients"] is None
+    assert torch.count_nonzero(out["comp_normal"]) == 0 and torch.count_nonzero(out["weight_sum"]) == 0
