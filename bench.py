@@ -287,7 +287,7 @@ def run_serve(size: str, dev) -> dict:
         cfg = dict(objects=32, views=(8, 100), res=(256, 1024), log2_table=(17, 21), duration=20.0, rate=4.0,
                    budget_frac=0.6)
     else:
-        cfg = dict(objects=8, views=(8, 24), res=(192, 384), log2_table=(17, 19), duration=6.0, rate=6.0,
+        cfg = dict(objects=8, views=(8, 24), res=(192, 384), log2_table=(17, 19), duration=6.0, rate=10.0,
                    budget_frac=0.6)
     t0 = time.perf_counter()
     specs = object_specs(cfg["objects"], seed=5, views=cfg["views"], res=cfg["res"], log2_table=cfg["log2_table"])

@@ -168,6 +168,20 @@ def pixel_rays(rig: CameraRig, view: int, px: Tensor, py: Tensor) -> Tensor:
     return v @ rig.poses[view, :3, :3].to(px.device).T
 
 
+def view_rays(rig: CameraRig, view: int, device) -> tuple:
+    """Ray directions (H, W, 3) and per-pixel V^-1 (H, W, 3, 3) of one view,
+    float32, without ground truth (models/dataset_loader.py:112-137: V has
+    rows d, camera right, camera down)."""
+    H, W = rig.H, rig.W
+    ys, xs = torch.meshgrid(torch.arange(H, device=device, dtype=torch.float64),
+                            torch.arange(W, device=device, dtype=torch.float64), indexing="ij")
+    d = pixel_rays(rig, view, xs, ys)
+    right = rig.poses[view, :3, 0].to(device).expand_as(d)
+    down = rig.poses[view, :3, 1].to(device).expand_as(d)
+    V = torch.stack([d, right, down], dim=-2)
+    return d.float(), inv3x3(V).float()
+
+
 def sphere_trace(scene: SDFScene, o: Tensor, d: Tensor, near: Tensor, far: Tensor,
                  iters: int = 400, eps: float = 1e-6):
     t = near.clone()

@@ -168,15 +168,17 @@ class ServedObject:
         rot = torch.tensor([[c, -s, 0.0, 0.0], [s, c, 0.0, 0.0], [0.0, 0.0, 1.0, 0.0], [0.0, 0.0, 0.0, 1.0]],
                            dtype=rig.poses.dtype)
         rig.poses = rot @ rig.poses
-        view = scenes.SyntheticDataset(self.scene, rig, self.tr.device)
+        dev = self.tr.device
+        d, v = scenes.view_rays(rig, 0, dev)
         H = W = self.spec.res
         ph, pw = H // 3, W // 3
-        blk = lambda t: t[0].reshape(ph, 3, pw, 3, *t.shape[3:]).transpose(1, 2).reshape(
-            ph * pw, 3, 3, *t.shape[3:]).contiguous()
-        rays_d = blk(view.rays_all)
-        vinv = blk(view.V_inverse_all)
-        rays_o = view.pose_all[0, :3, 3].expand(rays_d.shape).contiguous()
-        plane_n = view.pose_all[0, :3, 2].expand(rays_d.shape[0], 3).contiguous()
+        blk = lambda t: t.reshape(ph, 3, pw, 3, *t.shape[2:]).transpose(1, 2).reshape(
+            ph * pw, 3, 3, *t.shape[2:]).contiguous()
+        rays_d = blk(d)
+        vinv = blk(v)
+        pose = rig.poses[0].to(dev).float()
+        rays_o = pose[:3, 3].expand(rays_d.shape).contiguous()
+        plane_n = pose[:3, 2].expand(rays_d.shape[0], 3).contiguous()
         out = torch.empty_like(rays_d)
         self.renderer.gradient_method = "dfd"
         for a in range(0, rays_d.shape[0], chunk):
@@ -312,8 +314,8 @@ class Server:
                     finish(r)
                     if policy != "plain":
                         recon_q.popleft()
-                else:
-                    torch.cuda.synchronize()   # the slice is done: look at new arrivals
+                # (a slice ends without a device sync: the host looks at new
+                # arrivals while the GPU works through the queued iterations)
             elif r.kind == "render":
                 img = obj.render(pose_seed=r.rid)
                 render_rays += img.shape[0] * img.shape[1]
