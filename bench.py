@@ -302,11 +302,17 @@ def run_serve(size: str, dev) -> dict:
                       "trace_s": cfg["duration"], "requests": len(trace),
                       "hbm_budget_gb": budget / 1e9, "objects_total_gb": total / 1e9,
                       "setup_s": setup_s}}
+    # capacity: a saturating burst of the same request mix (rays/s over its makespan)
+    burst = poisson_trace(len(objs), 2.0, 40.0, seed=13, recon_iters=100)
+    out["config"]["burst_requests"] = len(burst)
     for policy in ("served", "plain"):
         srv = Server(objs, budget, query_res=256, slice_iters=10)
         srv.fit_budget()
         r = srv.run(trace, policy)
         r["swaps"] = srv.swaps
+        b = Server(objs, budget, query_res=256, slice_iters=10).run(burst, policy)
+        r["burst"] = {"makespan_s": b["makespan_s"], "rays_per_s": b["rays_per_s"], "p50_ms": b["p50_ms"],
+                      "p99_ms": b["p99_ms"]}
         out[policy] = r
     return out
 
