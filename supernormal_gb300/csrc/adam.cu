@@ -53,12 +53,19 @@ __device__ __forceinline__ void adam_one(float& p, float& m, float& v, float g, 
 }
 
 __global__ void __launch_bounds__(256) adam_kernel(AdamArgs a) {
-  const float lr = a.lr_dev ? *a.lr_dev : a.lr;
-  const int step = a.step_dev ? *a.step_dev : a.step;
-  const double bc1 = 1.0 - pow((double)a.beta1, (double)step);
-  const double bc2 = 1.0 - pow((double)a.beta2, (double)step);
-  const float step_size = (float)((double)lr / bc1);
-  const float bc2s = (float)sqrt(bc2);
+  // bias corrections (torch.optim.Adam, double precision) once per block: FP64
+  // throughput is a small fraction of FP32 here, so not once per thread
+  __shared__ float s_step_size, s_bc2s;
+  if (threadIdx.x == 0) {
+    const float lr = a.lr_dev ? *a.lr_dev : a.lr;
+    const int step = a.step_dev ? *a.step_dev : a.step;
+    const double bc1 = 1.0 - pow((double)a.beta1, (double)step);
+    const double bc2 = 1.0 - pow((double)a.beta2, (double)step);
+    s_step_size = (float)((double)lr / bc1);
+    s_bc2s = (float)sqrt(bc2);
+  }
+  __syncthreads();
+  const float step_size = s_step_size, bc2s = s_bc2s;
   const float omb1 = 1.0f - a.beta1, omb2 = 1.0f - a.beta2;
   const int64_t n4 = a.n >> 2;
   float4* p4 = reinterpret_cast<float4*>(a.p);
