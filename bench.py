@@ -61,6 +61,10 @@ def parse():
     p.add_argument("--no-clocks", action="store_true")
     p.add_argument("--serve", choices=["small", "full", "off"], default="small",
                    help="serving-loop trace after the training measurement (p50/p99 latency)")
+    p.add_argument("--quality", action="store_true",
+                   help="instead of the throughput run: FP32 vs mixed precision reconstruction quality "
+                        "on the sphere scene (angular error, mask IoU, Chamfer / F@0.01)")
+    p.add_argument("--quality-iters", type=int, default=1000)
     return p.parse_args()
 
 
@@ -274,6 +278,48 @@ def run_ours(args, world, rank, local):
         del tr, ds, pool, host, dev_in
         torch.cuda.empty_cache()
         out["serve"] = run_serve(args.serve, dev)
+    return out
+
+
+def run_quality(iters: int, dev) -> dict:
+    """FP32 and mixed precision (FP16 table copy, one-pass TF32 MLP) trained
+    from the same initialisation on the sphere scene of the small
+    configuration, then measured against the analytic scene."""
+    from supernormal_gb300 import quality, scenes
+    from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
+    from supernormal_gb300.nerfacc import OccupancyGrid
+    from supernormal_gb300.trainer import FusedTrainer, TrainConfig
+
+    scene = scenes.sphere(0.5)
+    rig = scenes.ring_cameras(8, 128, 128, radius=3.0, elevation_deg=0.0)
+    ds = scenes.SyntheticDataset(scene, rig, dev)
+    enc = dict(otype="HashGrid", n_levels=16, n_features_per_level=2, log2_hashmap_size=15, base_resolution=16,
+               per_level_scale=1.447)
+    out = {"config": {"scene": "sphere r=0.5", "views": "8 x 128x128, ring radius 3", "hash": "L16 F2 T2^15",
+                      "patches_per_iteration": 256, "samples_per_ray": 128, "iterations": iters,
+                      "mixed": "FP16 table copy of FP32 master weights, FP32 gradients, one-pass TF32 MLP"}}
+    for prec in ("fp32", "mixed"):
+        torch.manual_seed(0)
+        net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=enc, input_concat=True).to(dev)
+        var = SingleVarianceNetwork(0.3).to(dev)
+        net.bindwidth = 16
+        grid = OccupancyGrid(roi_aabb=[-1.0, -1.0, -1.0, 1.0, 1.0, 1.0], resolution=128).to(dev)
+        grid._binary = torch.ones_like(grid._binary)
+        cfg = TrainConfig(batch_size=256, step_size=1.0 / 64, occ_update_freq=0, increase_bandwidth_every=0,
+                          learning_rate=1e-3, warm_up_end=50, end_iter=iters, precision=prec, seed=0)
+        tr = FusedTrainer(net, var, cfg, occupancy_grid=grid, device=dev)
+        g = torch.Generator(device=dev).manual_seed(7)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(iters):
+            loss = tr.train_step(*ds.gen_random_patches(256, generator=g))
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        tr.check_status()
+        m = quality.evaluate(net, var, grid, ds, scene, cfg.step_size)
+        m["final_loss"] = float(loss[4].item())
+        m["ms_per_iteration"] = 1e3 * dt / iters
+        out[prec] = m
     return out
 
 
@@ -504,7 +550,9 @@ def run_reference(args, world, rank, local):
 def main():
     args = parse()
     world, rank, local = dist_setup()
-    if args.impl == "reference":
+    if args.quality:
+        out = {"quality": run_quality(args.quality_iters, torch.device("cuda", local))} if rank == 0 else None
+    elif args.impl == "reference":
         out = run_reference(args, world, rank, local)
     else:
         out = run_ours(args, world, rank, local)

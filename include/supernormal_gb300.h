@@ -240,7 +240,16 @@ typedef struct sn_mlp_desc {
   const float* w1;
   const float* b1;
   int32_t* status;   /* nullable device word: SN_STATUS_TIMEOUT is OR-ed here */
+  uint32_t flags;    /* SN_FIELD_* precision options of the fused field kernels */
 } sn_mlp_desc;
+
+/* sn_mlp_desc.flags (fused field forward / backward only):
+ * SN_FIELD_TABLE_FP16 -- the `table` pointer addresses the hash table as FP16
+ *   pairs (an FP16 copy of FP32 master weights; gradients stay FP32);
+ * SN_FIELD_MLP_TF32 -- the MLP's tensor-core products in one TF32 pass
+ *   instead of the FP32-accurate three. */
+#define SN_FIELD_TABLE_FP16 1u
+#define SN_FIELD_MLP_TF32 2u
 
 /* Level offsets, resolutions and scales of tcnn's GridEncoding for
  * {otype: HashGrid, n_levels, n_features_per_level, log2_hashmap_size,

@@ -22,6 +22,8 @@ SN_ERR_UNSUPPORTED = 5
 SN_STATUS_MARCH_LIMIT = 1
 SN_STATUS_CAPACITY = 2
 SN_STATUS_TIMEOUT = 4
+SN_FIELD_TABLE_FP16 = 1
+SN_FIELD_MLP_TF32 = 2
 SN_MAX_LEVELS = 32
 
 
@@ -53,6 +55,7 @@ class MlpDesc(C.Structure):
         ("w1", C.c_void_p),
         ("b1", C.c_void_p),
         ("status", C.c_void_p),
+        ("flags", C.c_uint32),
     ]
 
 

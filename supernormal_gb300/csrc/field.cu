@@ -513,6 +513,8 @@ int fill_field_args(FieldArgs& a, int64_t n, const int32_t* count, const float* 
   a.w1 = mlp->w1;
   a.b1 = mlp->b1;
   a.status = mlp->status;
+  a.table_half = (mlp->flags & SN_FIELD_TABLE_FP16) != 0;
+  a.one_pass = (mlp->flags & SN_FIELD_MLP_TF32) != 0;
   return SN_OK;
 }
 
@@ -616,6 +618,10 @@ int sn_field_grad_fwd(int64_t n, const int32_t* count, const float* x, const flo
                       float* sdf, float* grad, void* stream) {
   FieldArgs a;
   SN_TRY(fill_field_args(a, n, count, x, table, grid, active_levels, mlp, 1));
+  if (a.table_half || a.one_pass) {
+    set_error("field_grad: SN_FIELD_* precision flags are supported by the fused field forward/backward only");
+    return SN_ERR_UNSUPPORTED;
+  }
   SN_REQUIRE(grad != nullptr, "field_grad_fwd: grad is null");
   if (n == 0) return SN_OK;
   SN_TRY(ensure_smem_limit(reinterpret_cast<const void*>(field_grad_fwd_kernel), kFwdSmem, "field_grad_fwd_kernel"));
@@ -629,6 +635,10 @@ int sn_field_grad_bwd(int64_t n, const int32_t* count, const float* x, const flo
                       float* grad_b0, float* grad_w1, float* grad_b1, void* stream) {
   FieldArgs a;
   SN_TRY(fill_field_args(a, n, count, x, table, grid, active_levels, mlp, 1));
+  if (a.table_half || a.one_pass) {
+    set_error("field_grad: SN_FIELD_* precision flags are supported by the fused field forward/backward only");
+    return SN_ERR_UNSUPPORTED;
+  }
   SN_REQUIRE(grad_grad != nullptr, "field_grad_bwd: grad_grad is null");
   a.grad_table = grad_table;
   a.grad_w0 = grad_w0;

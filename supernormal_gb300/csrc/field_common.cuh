@@ -156,7 +156,33 @@ struct FieldArgs {
   float* grad_x;          // (n, 3) optional
   int32_t* status;        // optional: SN_STATUS_TIMEOUT is OR-ed here
   bool pair16;            // grad_table is 16-byte aligned: entry pairs may be added as float4
+  bool table_half;        // table holds FP16 pairs (SN_FIELD_TABLE_FP16)
+  bool one_pass;          // single-pass TF32 MLP products (SN_FIELD_MLP_TF32)
 };
+
+// Table entry (F = 2 features) as float2, from an FP32 or FP16 table.
+__device__ __forceinline__ float2 load_entry(const FieldArgs& a, uint32_t idx) {
+  if (a.table_half) return __half22float2(__ldg(reinterpret_cast<const __half2*>(a.table) + idx));
+  return __ldg(reinterpret_cast<const float2*>(a.table) + idx);
+}
+
+// Encoding of one level from either table type.
+__device__ __forceinline__ void encode_level_a(const FieldArgs& a, int l, const float x[3], float& e0,
+                                               float& e1) {
+  LevelCorners c;
+  level_corners(a.g, l, x, c);
+  float2 v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = load_entry(a, c.idx[k]);
+  float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    s0 = __fmaf_rn(c.w[k], v[k].x, s0);
+    s1 = __fmaf_rn(c.w[k], v[k].y, s1);
+  }
+  e0 = s0;
+  e1 = s1;
+}
 
 __device__ __forceinline__ int64_t effective_n(const FieldArgs& a) {
   if (!a.count) return a.cap;

@@ -185,13 +185,12 @@ __device__ __forceinline__ void encode_group(const FieldArgs& a, int g, bool liv
     for (int i = 0; i < kLpm; ++i) {
       const int l = level_of<M>(g, i);
       float e0 = 0.0f, e1 = 0.0f;
-      if (live && l < a.active) encode_level(a.table, a.g, l, x, e0, e1);
+      if (live && l < a.active) encode_level_a(a, l, x, e0, e1);
       e[2 * i] = e0;
       e[2 * i + 1] = e1;
     }
     return;
   }
-  const float2* t2 = reinterpret_cast<const float2*>(a.table);
 #pragma unroll
   for (int i0 = 0; i0 < kLpm; i0 += 2) {
     const int la = level_of<M>(g, i0), lb = level_of<M>(g, i0 + 1);
@@ -201,12 +200,12 @@ __device__ __forceinline__ void encode_group(const FieldArgs& a, int g, bool liv
     if (ua) {
       level_corners(a.g, la, x, ca);
 #pragma unroll
-      for (int k = 0; k < 8; ++k) va[k] = __ldg(t2 + ca.idx[k]);
+      for (int k = 0; k < 8; ++k) va[k] = load_entry(a, ca.idx[k]);
     }
     if (ub) {
       level_corners(a.g, lb, x, cb);
 #pragma unroll
-      for (int k = 0; k < 8; ++k) vb[k] = __ldg(t2 + cb.idx[k]);
+      for (int k = 0; k < 8; ++k) vb[k] = load_entry(a, cb.idx[k]);
     }
     float a0 = 0.0f, a1 = 0.0f, b0 = 0.0f, b1 = 0.0f;
     if (ua) {
@@ -295,7 +294,7 @@ __device__ __forceinline__ void st_split(uint32_t ta_hi, uint32_t ta_lo, const f
 }
 
 // Issues H = IN W0^T (3xTF32: in_hi w_hi + in_lo w_hi + in_hi w_lo), M=128, N=64, K=40.
-__device__ __forceinline__ void issue_mma1(uint32_t tbase, uint32_t s_b1_hi, uint32_t s_b1_lo) {
+__device__ __forceinline__ void issue_mma1(uint32_t tbase, uint32_t s_b1_hi, uint32_t s_b1_lo, bool one_pass) {
   const uint32_t idesc = tc::idesc_tf32(kTile, kH);
   const uint32_t sbo = (kK1 / 4) * 128u;
   const uint32_t d = tc::taddr(tbase, 0, kColH);
@@ -303,6 +302,7 @@ __device__ __forceinline__ void issue_mma1(uint32_t tbase, uint32_t s_b1_hi, uin
   const uint64_t w_hi = tc::smem_desc(s_b1_hi, 128u, sbo), w_lo = tc::smem_desc(s_b1_lo, 128u, sbo);
   for (int ks = 0; ks < kK1 / 8; ++ks)
     tc::mma_ts(d, tc::taddr(tbase, 0, kColInHi + 8 * ks), w_hi + 16u * ks, idesc, ks > 0);
+  if (one_pass) return;
   for (int ks = 0; ks < kK1 / 8; ++ks) tc::mma_ts(d, tc::taddr(tbase, 0, kColInLo + 8 * ks), w_hi + 16u * ks, idesc, 1);
   for (int ks = 0; ks < kK1 / 8; ++ks) tc::mma_ts(d, tc::taddr(tbase, 0, kColInHi + 8 * ks), w_lo + 16u * ks, idesc, 1);
 }
@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
     __syncthreads();
     if (t == 0) {
       tc::fence_after_sync();
-      issue_mma1(tbase, s_b1_hi, s_b1_lo);
+      issue_mma1(tbase, s_b1_hi, s_b1_lo, a.one_pass);
       tc::mma_commit(bar);
     }
     const bool got = tc::mbar_wait_bounded(bar, phase);
@@ -446,7 +446,7 @@ __device__ __forceinline__ void st_smem_u32(uint8_t* base, uint32_t off, uint32_
 }
 
 // Second MMA of the backward: dIN = dH W0 (3xTF32, M=128, N=48, K=64).
-__device__ __forceinline__ void issue_mma2(uint32_t tbase, const uint8_t* sm) {
+__device__ __forceinline__ void issue_mma2(uint32_t tbase, const uint8_t* sm, bool one_pass) {
   const uint32_t s_b2_hi = tc::smem_u32(sm + BwdSmem::b2_hi), s_b2_lo = tc::smem_u32(sm + BwdSmem::b2_lo);
   const uint32_t idesc = tc::idesc_tf32(kTile, kN2);
   const uint32_t d2 = tc::taddr(tbase, 0, kColH);
@@ -454,13 +454,14 @@ __device__ __forceinline__ void issue_mma2(uint32_t tbase, const uint8_t* sm) {
   const uint64_t w_hi = tc::smem_desc(s_b2_hi, 128u, sbo2), w_lo = tc::smem_desc(s_b2_lo, 128u, sbo2);
   for (int ks = 0; ks < kH / 8; ++ks)
     tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhHi + 8 * ks), w_hi + 16u * ks, idesc, ks > 0);
+  if (one_pass) return;
   for (int ks = 0; ks < kH / 8; ++ks) tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhLo + 8 * ks), w_hi + 16u * ks, idesc, 1);
   for (int ks = 0; ks < kH / 8; ++ks) tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhHi + 8 * ks), w_lo + 16u * ks, idesc, 1);
 }
 
 // Third MMA: dW0 += [dH_hi; dH_lo]^T-rows x IN^T (M=128, N=48, K=128 points),
 // accumulated in TMEM over all of the CTA's tiles.
-__device__ __forceinline__ void issue_mma3(uint32_t tbase, const uint8_t* sm, bool first_tile) {
+__device__ __forceinline__ void issue_mma3(uint32_t tbase, const uint8_t* sm, bool first_tile, bool one_pass) {
   const uint32_t s_a3 = tc::smem_u32(sm + BwdSmem::a3);
   const uint32_t s_b3_hi = tc::smem_u32(sm + BwdSmem::b3_hi), s_b3_lo = tc::smem_u32(sm + BwdSmem::b3_lo);
   const uint32_t idesc = tc::idesc_tf32(kTile, kN2);
@@ -470,7 +471,7 @@ __device__ __forceinline__ void issue_mma3(uint32_t tbase, const uint8_t* sm, bo
   for (int ks = 0; ks < kTile / 8; ++ks) {
     const uint64_t k0 = (2u * kLboP * ks) >> 4;
     tc::mma_ss(d3, da + k0, dbh + k0, idesc, (first_tile && ks == 0) ? 0u : 1u);
-    tc::mma_ss(d3, da + k0, dbl + k0, idesc, 1);
+    if (!one_pass) tc::mma_ss(d3, da + k0, dbl + k0, idesc, 1);
   }
 }
 
@@ -595,7 +596,7 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
     }
     if (t == 0) {
       tc::fence_after_sync();
-      issue_mma1(tbase, s_b1_hi, s_b1_lo);
+      issue_mma1(tbase, s_b1_hi, s_b1_lo, a.one_pass);
       tc::mma_commit(bar);
     }
     bool got = tc::mbar_wait_bounded(bar, phase);
@@ -669,9 +670,9 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
     __syncthreads();
     if (t == 0) {
       tc::fence_after_sync();
-      issue_mma2(tbase, sm);
+      issue_mma2(tbase, sm, a.one_pass);
       tc::mma_commit(bar);
-      issue_mma3(tbase, sm, first);
+      issue_mma3(tbase, sm, first, a.one_pass);
       tc::mma_commit(bar3);
     }
     first = false;
@@ -704,7 +705,6 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
         dx[2] = dxl[2];
       }
       float2* gt2 = reinterpret_cast<float2*>(a.grad_table);
-      const float2* t2 = reinterpret_cast<const float2*>(a.table);
 #pragma unroll
       for (int i = 0; i < kLpm; ++i) {
         const int l = level_of<M>(g, i);
@@ -716,7 +716,7 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
           if (want_x && live) {
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-              const float2 v = __ldg(t2 + c.idx[k]);
+              const float2 v = load_entry(a, c.idx[k]);
               const float gv = d0 * v.x + d1 * v.y;
 #pragma unroll
               for (int d = 0; d < 3; ++d) dx[d] = fmaf(gv, corner_dw(c, k, d, a.g.scale[l]), dx[d]);

@@ -100,6 +100,8 @@ class ServedObject:
                    tr.status, ds.normals, ds.masks, ds.V_inverse_all, ds.rays_all, ds.pose_all,
                    ds.intrinsics_all]
         state_t += list(tr.grid.buffers()) + list(tr.net.buffers())
+        if tr.params_half is not None:
+            state_t.append(tr.params_half)
         state, seen = [], set()
         for t in state_t:
             st = t.untyped_storage()

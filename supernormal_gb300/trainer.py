@@ -21,7 +21,8 @@ from typing import Optional
 import torch
 from torch import Tensor
 
-from ._lib import SN_STATUS_CAPACITY, SN_STATUS_MARCH_LIMIT, SN_STATUS_TIMEOUT, call, stream_handle
+from ._lib import (SN_FIELD_MLP_TF32, SN_FIELD_TABLE_FP16, SN_STATUS_CAPACITY, SN_STATUS_MARCH_LIMIT,
+                   SN_STATUS_TIMEOUT, call, stream_handle)
 from .fields import SDFNetwork, SingleVarianceNetwork
 
 __all__ = ["TrainConfig", "FusedTrainer"]
@@ -48,6 +49,7 @@ class TrainConfig:
     early_stop_eps: float = 1e-8
     loss_type: str = "l2"
     gradient_method: str = "dfd"            # 'dfd' (shipped) or 'ad' (second-order adjoint)
+    precision: str = "fp32"                 # 'fp32' or 'mixed' (FP16 table copy, one-pass TF32 MLP)
     normal_weight: float = 1.0
     eikonal_weight: float = 1.0
     mask_weight: float = 1.0
@@ -101,6 +103,16 @@ class FusedTrainer:
                 p.data = v
                 p.grad = gv
                 self.views[name], self.gviews[name] = v, gv
+        if cfg.precision not in ("fp32", "mixed"):
+            raise ValueError(f"precision {cfg.precision!r}: 'fp32' or 'mixed'")
+        if cfg.precision == "mixed" and cfg.gradient_method != "dfd":
+            raise NotImplementedError("mixed precision is built for the dfd gradient path")
+        # mixed: the field kernels read an FP16 copy of the table, refreshed by
+        # every Adam step from the FP32 master weights (gradients stay FP32)
+        self.params_half = None
+        if cfg.precision == "mixed":
+            self.params_half = self.params.to(torch.float16)
+        self.table_numel = offs["table"][1]
         self.H = sdf_network.d_hidden
         self.dout = sdf_network.d_out
         self.din = sdf_network.lin0.in_features
@@ -208,9 +220,17 @@ class FusedTrainer:
     def _grid_desc(self):
         return C.byref(self.net.encoding.desc)
 
+    def _table(self) -> Tensor:
+        """The table the field kernels read: FP32 master or its FP16 copy."""
+        if self.params_half is not None:
+            return self.params_half[: self.table_numel]
+        return self.views["table"]
+
     def _mlp(self):
         d = self.net._mlp_desc(self.w0, self.views["b0"], self.w1, self.views["b1"])
         d.status = self.status.data_ptr()
+        if self.params_half is not None:
+            d.flags = SN_FIELD_TABLE_FP16 | SN_FIELD_MLP_TF32
         return d
 
     def step_size(self, it: int) -> float:
@@ -245,7 +265,7 @@ class FusedTrainer:
             cells, cap, count = self.occ_cells, 2 * n_u, self.occ_count
         call("sn_occ_points_n", cap, count, cells, seed ^ 0x9E37, self.iter_dev, *self.res, roi,
              g._contraction_type.value, self.occ_xyz, st)
-        call("sn_field_fwd", cap, count, self.occ_xyz, self.views["table"], self._grid_desc(), active,
+        call("sn_field_fwd", cap, count, self.occ_xyz, self._table(), self._grid_desc(), active,
              C.byref(self._mlp()), 1, self.occ_sdf, st)
         call("sn_occ_ema_sdf", cap, count, cells, self.occ_sdf, float(c.occ_sigmoid_k),
              float(c.occ_ema_decay), g.occs, st)
@@ -283,7 +303,7 @@ class FusedTrainer:
              int(c.warm_up_end), int(c.end_iter), float(c.learning_rate_alpha), st)
         self._mark("adam_begin")
         call("sn_adam_step", self.n_params, self.params, self.grads, self.exp_avg, self.exp_avg_sq,
-             None, self.lr_dev, self.adam_step_dev, 0.0, 1, 0.9, 0.999, 1e-8, 1, st)
+             self.params_half, self.lr_dev, self.adam_step_dev, 0.0, 1, 0.9, 0.999, 1e-8, 1, st)
         self._mark("adam_end")
 
     @torch.no_grad()
@@ -321,7 +341,7 @@ class FusedTrainer:
         call("sn_pack_counts", C0, self.diff, self.endp, self.n_ends, self.scan_ws, st)
         call("sn_center_points", C0, self.total0, self.ridx0, self.ts0, self.te0, self.ro_c,
              self.rd_c, self.endp, self.n_ends, self.xyz0, self.q0, st)
-        call("sn_field_fwd", 2 * C0, self.q0, self.xyz0, v["table"], gd, active, mlp, 1, self.sdf0, st)
+        call("sn_field_fwd", 2 * C0, self.q0, self.xyz0, self._table(), gd, active, mlp, 1, self.sdf0, st)
         call("sn_center_alpha", C0, self.total0, self.sdf0, 1, self.endp, v["variance"], self.alpha0, st)
         call("sn_visibility_from_alpha", B, self.packed0, self.alpha0, float(c.early_stop_eps), 0.0,
              self.vis, self.counts1, st)
@@ -336,7 +356,7 @@ class FusedTrainer:
              plane_n, self.endp1, self.n_ends1, self.xyz1, self.tps, self.tpe, self.q1, st)
         cap1 = 2 * C0 * P
         self._mark("field_fwd_begin")
-        call("sn_field_fwd", cap1, self.q1, self.xyz1, v["table"], gd, active, mlp, 1, self.sdf1, st)
+        call("sn_field_fwd", cap1, self.q1, self.xyz1, self._table(), gd, active, mlp, 1, self.sdf1, st)
         self._mark("field_fwd_end")
         if self.profile:
             self.q_hist.append(self.q1.clone())   # field points of this step (device copy)
@@ -362,7 +382,7 @@ class FusedTrainer:
         self.dw0.zero_()
         self.dw1.zero_()
         self._mark("field_bwd_begin")
-        call("sn_field_bwd", cap1, self.q1, self.xyz1, self.d_sdf, 1, v["table"], gd, active, mlp,
+        call("sn_field_bwd", cap1, self.q1, self.xyz1, self.d_sdf, 1, self._table(), gd, active, mlp,
              g["table"], self.dw0, g["b0"], self.dw1, g["b1"], None, st)
         if ad:  # second-order adjoint of the gradients
             call("sn_field_grad_bwd", C0 * P, self.sp_count, self.xyz1, self.d_ext, None, v["table"],
