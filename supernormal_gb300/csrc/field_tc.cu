@@ -668,10 +668,15 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
     tc::fence_proxy_async_smem();
     tc::fence_before_sync();
     __syncthreads();
+    // dIN (needed next) and the weight-gradient MMAs are issued by two threads
+    // of different warps, each committing its own to its own mbarrier, so the
+    // dIN chain is queued without waiting behind the longer dW0 issue
     if (t == 0) {
       tc::fence_after_sync();
       issue_mma2(tbase, sm, a.one_pass);
       tc::mma_commit(bar);
+    } else if (t == 32) {
+      tc::fence_after_sync();
       issue_mma3(tbase, sm, first, a.one_pass);
       tc::mma_commit(bar3);
     }
