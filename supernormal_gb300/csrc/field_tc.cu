@@ -34,16 +34,34 @@ constexpr int kK1 = 40;        // MLP input width inside the kernels (35 used)
 constexpr int kN2 = 48;        // dIN columns (N of the second MMA; 35 used)
 constexpr int kXCol = 32;      // first column of x in the permuted input
 constexpr int kOnesRow = 35;   // row of ones in IN^T (gives db0)
-constexpr uint32_t kCols = 256;
+constexpr uint32_t kCols = 256;      // forward: two CTAs per SM
+constexpr uint32_t kBwdCols = 512;   // backward: one CTA per SM
 // IN^T and [dH_hi; dH_lo] (K = the tile's points, written one point per
 // thread): core matrices 144 bytes apart along K so a warp's 32 stores of one
 // row fall in 32 banks.
 constexpr uint32_t kLboP = 144, kSboP = (kTile / 4) * kLboP;
 
-// TMEM column map (both kernels): H / dIN share [0, 64); the input rows
-// (hi, lo) and later dH (hi, lo) share [64, 192); dW0 accumulates in [192, 240).
-constexpr uint32_t kColH = 0, kColInHi = 64, kColInLo = 64 + kK1;
-constexpr uint32_t kColDhHi = 64, kColDhLo = 128, kColDw0 = 192;
+// The three 3xTF32 passes (hi.hi, lo.hi, hi.lo) of a GEMM are issued by
+// threads of different warps into separate TMEM accumulators (no ordering
+// between the issuing threads is needed) and summed by the readers; one
+// mbarrier counts one commit per issuing thread.
+//
+// Forward TMEM columns (256): H part 0 [0,64), parts 1+2 [64,128); input
+// rows hi [128,168), lo [168,208).
+constexpr uint32_t kFwdColH0 = 0, kFwdColH1 = 64, kFwdColInHi = 128, kFwdColInLo = 128 + kK1;
+// Backward TMEM columns (512): H parts / dIN parts at [0,64), [64,128),
+// [128,192); input rows then dH (hi, lo) share [192,320); dW0 accumulates in
+// [320,368).
+__host__ __device__ constexpr uint32_t col_part(int p) { return 64u * (uint32_t)p; }
+constexpr uint32_t kColInHi = 192, kColInLo = 192 + kK1;
+constexpr uint32_t kColDhHi = 192, kColDhLo = 256, kColDw0 = 320;
+
+// K steps of D (+)= A[TMEM columns from a] B[shared memory, descriptor b]^T.
+__device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint64_t b, int ksteps, uint32_t idesc,
+                                          bool fresh) {
+  for (int ks = 0; ks < ksteps; ++ks)
+    tc::mma_ts(d, a + 8u * ks, b + 16u * ks, idesc, (fresh && ks == 0) ? 0u : 1u);
+}
 
 // With M members per quadrant group, member g handles levels g, g+M, g+2M, ...
 // (coarse and fine levels mixed, which balances the scatter's shuffle and
@@ -293,20 +311,6 @@ __device__ __forceinline__ void st_split(uint32_t ta_hi, uint32_t ta_lo, const f
   }
 }
 
-// Issues H = IN W0^T (3xTF32: in_hi w_hi + in_lo w_hi + in_hi w_lo), M=128, N=64, K=40.
-__device__ __forceinline__ void issue_mma1(uint32_t tbase, uint32_t s_b1_hi, uint32_t s_b1_lo, bool one_pass) {
-  const uint32_t idesc = tc::idesc_tf32(kTile, kH);
-  const uint32_t sbo = (kK1 / 4) * 128u;
-  const uint32_t d = tc::taddr(tbase, 0, kColH);
-  // a descriptor advances by (byte offset >> 4) in its start-address field
-  const uint64_t w_hi = tc::smem_desc(s_b1_hi, 128u, sbo), w_lo = tc::smem_desc(s_b1_lo, 128u, sbo);
-  for (int ks = 0; ks < kK1 / 8; ++ks)
-    tc::mma_ts(d, tc::taddr(tbase, 0, kColInHi + 8 * ks), w_hi + 16u * ks, idesc, ks > 0);
-  if (one_pass) return;
-  for (int ks = 0; ks < kK1 / 8; ++ks) tc::mma_ts(d, tc::taddr(tbase, 0, kColInLo + 8 * ks), w_hi + 16u * ks, idesc, 1);
-  for (int ks = 0; ks < kK1 / 8; ++ks) tc::mma_ts(d, tc::taddr(tbase, 0, kColInHi + 8 * ks), w_lo + 16u * ks, idesc, 1);
-}
-
 // ---------------------------------------------------------------------------
 // forward
 // ---------------------------------------------------------------------------
@@ -343,7 +347,7 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
     tc::tmem_alloc(slot, kCols);
     tc::tmem_relinquish();
   }
-  if (t == 0) tc::mbar_init(bar, 1);
+  if (t == 0) tc::mbar_init(bar, 2);  // one commit each from threads 0 and 32
   tc::fence_proxy_async_smem();
   tc::fence_before_sync();
   __syncthreads();
@@ -367,18 +371,26 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
     {
       float e[8];
       encode_group<false, 4>(a, g, live, x, e);
-      st_split8(tc::taddr(tbase, lb, kColInHi + 8 * g), tc::taddr(tbase, lb, kColInLo + 8 * g), e);
+      st_split8(tc::taddr(tbase, lb, kFwdColInHi + 8 * g), tc::taddr(tbase, lb, kFwdColInLo + 8 * g), e);
       if (g == 0) {
         const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-        st_split8(tc::taddr(tbase, lb, kColInHi + kXCol), tc::taddr(tbase, lb, kColInLo + kXCol), xv);
+        st_split8(tc::taddr(tbase, lb, kFwdColInHi + kXCol), tc::taddr(tbase, lb, kFwdColInLo + kXCol), xv);
       }
     }
     tc::tmem_wait_st();
     tc::fence_before_sync();
     __syncthreads();
-    if (t == 0) {
+    if (t == 0 || t == 32) {  // H = IN W0^T, M=128, N=64, K=40
       tc::fence_after_sync();
-      issue_mma1(tbase, s_b1_hi, s_b1_lo, a.one_pass);
+      const uint32_t idesc = tc::idesc_tf32(kTile, kH);
+      const uint32_t sbo = (kK1 / 4) * 128u;
+      const uint64_t w_hi = tc::smem_desc(s_b1_hi, 128u, sbo), w_lo = tc::smem_desc(s_b1_lo, 128u, sbo);
+      if (t == 0) {
+        mma_chain(tc::taddr(tbase, 0, kFwdColH0), tc::taddr(tbase, 0, kFwdColInHi), w_hi, kK1 / 8, idesc, true);
+      } else if (!a.one_pass) {
+        mma_chain(tc::taddr(tbase, 0, kFwdColH1), tc::taddr(tbase, 0, kFwdColInLo), w_hi, kK1 / 8, idesc, true);
+        mma_chain(tc::taddr(tbase, 0, kFwdColH1), tc::taddr(tbase, 0, kFwdColInHi), w_lo, kK1 / 8, idesc, false);
+      }
       tc::mma_commit(bar);
     }
     const bool got = tc::mbar_wait_bounded(bar, phase);
@@ -390,7 +402,14 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
     tc::fence_after_sync();
     // hidden units 16g..16g+15 of this point -> partial outputs
     float h[16];
-    tc::tmem_ld16(tc::taddr(tbase, lb, kColH + 16 * g), h);
+    tc::tmem_ld16(tc::taddr(tbase, lb, kFwdColH0 + 16 * g), h);
+    if (!a.one_pass) {
+      float h1[16];
+      tc::tmem_ld16(tc::taddr(tbase, lb, kFwdColH1 + 16 * g), h1);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int i = 0; i < 16; ++i) h[i] += h1[i];
+    }
     tc::tmem_wait_ld();
     float part[kOc];
 #pragma unroll
@@ -445,18 +464,21 @@ __device__ __forceinline__ void st_smem_u32(uint8_t* base, uint32_t off, uint32_
   *reinterpret_cast<uint32_t*>(base + off) = v;
 }
 
-// Second MMA of the backward: dIN = dH W0 (3xTF32, M=128, N=48, K=64).
-__device__ __forceinline__ void issue_mma2(uint32_t tbase, const uint8_t* sm, bool one_pass) {
-  const uint32_t s_b2_hi = tc::smem_u32(sm + BwdSmem::b2_hi), s_b2_lo = tc::smem_u32(sm + BwdSmem::b2_lo);
-  const uint32_t idesc = tc::idesc_tf32(kTile, kN2);
-  const uint32_t d2 = tc::taddr(tbase, 0, kColH);
+// Part p of the second MMA, dIN = dH W0 (M=128, N=48, K=64): p = 0 dH_hi W_hi,
+// 1 dH_lo W_hi, 2 dH_hi W_lo, each into its own accumulator.
+__device__ __forceinline__ void issue_mma2_part(uint32_t tbase, const uint8_t* sm, int part) {
   const uint32_t sbo2 = (kH / 4) * 128u;
-  const uint64_t w_hi = tc::smem_desc(s_b2_hi, 128u, sbo2), w_lo = tc::smem_desc(s_b2_lo, 128u, sbo2);
-  for (int ks = 0; ks < kH / 8; ++ks)
-    tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhHi + 8 * ks), w_hi + 16u * ks, idesc, ks > 0);
-  if (one_pass) return;
-  for (int ks = 0; ks < kH / 8; ++ks) tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhLo + 8 * ks), w_hi + 16u * ks, idesc, 1);
-  for (int ks = 0; ks < kH / 8; ++ks) tc::mma_ts(d2, tc::taddr(tbase, 0, kColDhHi + 8 * ks), w_lo + 16u * ks, idesc, 1);
+  const uint64_t w = tc::smem_desc(tc::smem_u32(sm + (part == 2 ? BwdSmem::b2_lo : BwdSmem::b2_hi)), 128u, sbo2);
+  mma_chain(tc::taddr(tbase, 0, col_part(part)), tc::taddr(tbase, 0, part == 1 ? kColDhLo : kColDhHi), w, kH / 8,
+            tc::idesc_tf32(kTile, kN2), true);
+}
+
+// Part p of the first MMA, H = IN W0^T (M=128, N=64, K=40).
+__device__ __forceinline__ void issue_mma1_part(uint32_t tbase, uint32_t s_b1_hi, uint32_t s_b1_lo, int part) {
+  const uint32_t sbo = (kK1 / 4) * 128u;
+  const uint64_t w = tc::smem_desc(part == 2 ? s_b1_lo : s_b1_hi, 128u, sbo);
+  mma_chain(tc::taddr(tbase, 0, col_part(part)), tc::taddr(tbase, 0, part == 1 ? kColInLo : kColInHi), w, kK1 / 8,
+            tc::idesc_tf32(kTile, kH), true);
 }
 
 // Third MMA: dW0 += [dH_hi; dH_lo]^T-rows x IN^T (M=128, N=48, K=128 points),
@@ -472,6 +494,28 @@ __device__ __forceinline__ void issue_mma3(uint32_t tbase, const uint8_t* sm, bo
     const uint64_t k0 = (2u * kLboP * ks) >> 4;
     tc::mma_ss(d3, da + k0, dbh + k0, idesc, (first_tile && ks == 0) ? 0u : 1u);
     if (!one_pass) tc::mma_ss(d3, da + k0, dbl + k0, idesc, 1);
+  }
+}
+
+// N (4, 8 or 16) columns from col of this warp's lanes, summed over the
+// three accumulator parts (part 0 alone for one-pass products).
+template <int N>
+__device__ __forceinline__ void ld_parts(uint32_t tbase, uint32_t lb, uint32_t col, bool one_pass, float* v) {
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    if (p > 0 && one_pass) break;
+    float u[N];
+    const uint32_t ta = tc::taddr(tbase, lb, col_part(p) + col);
+    if (N == 16) {
+      tc::tmem_ld16(ta, u);
+    } else if (N == 8) {
+      tc::tmem_ld8(ta, u);
+    } else {
+      tc::tmem_ld4(ta, u);
+    }
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = p == 0 ? u[i] : v[i] + u[i];
   }
 }
 
@@ -519,11 +563,11 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
     st_smem_u32(b3_lo, off, 0u);
   }
   if (warp == 0) {
-    tc::tmem_alloc(slot, kCols);
+    tc::tmem_alloc(slot, kBwdCols);
     tc::tmem_relinquish();
   }
   if (t == 0) {
-    tc::mbar_init(bar, 1);
+    tc::mbar_init(bar, 3);   // one commit from each of the three pass threads
     tc::mbar_init(bar3, 1);
   }
   tc::fence_proxy_async_smem();
@@ -594,9 +638,10 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
       ok = false;
       break;
     }
-    if (t == 0) {
+    if (t == 0 || t == 32 || t == 64) {
+      const int part = t >> 5;
       tc::fence_after_sync();
-      issue_mma1(tbase, s_b1_hi, s_b1_lo, a.one_pass);
+      if (part == 0 || !a.one_pass) issue_mma1_part(tbase, s_b1_hi, s_b1_lo, part);
       tc::mma_commit(bar);
     }
     bool got = tc::mbar_wait_bounded(bar, phase);
@@ -609,12 +654,7 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
     // ---- dH for this member's hidden units kHpm g .. kHpm g + kHpm - 1 ----
     {
       float h[kHpm];
-      if (kHpm == 16) {
-        tc::tmem_ld16(tc::taddr(tbase, lb, kColH + kHpm * g), h);
-      } else {
-        tc::tmem_ld8(tc::taddr(tbase, lb, kColH + kHpm * g), h);
-      }
-      tc::tmem_wait_ld();
+      ld_parts<kHpm>(tbase, lb, kHpm * g, a.one_pass, h);
       float dh[kHpm], act[kHpm];
 #pragma unroll
       for (int i = 0; i < kHpm; ++i) {
@@ -671,11 +711,12 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
     // dIN (needed next) and the weight-gradient MMAs are issued by two threads
     // of different warps, each committing its own to its own mbarrier, so the
     // dIN chain is queued without waiting behind the longer dW0 issue
-    if (t == 0) {
+    if (t == 0 || t == 32 || t == 64) {
+      const int part = t >> 5;
       tc::fence_after_sync();
-      issue_mma2(tbase, sm, a.one_pass);
+      if (part == 0 || !a.one_pass) issue_mma2_part(tbase, sm, part);
       tc::mma_commit(bar);
-    } else if (t == 32) {
+    } else if (t == 96) {
       tc::fence_after_sync();
       issue_mma3(tbase, sm, first, a.one_pass);
       tc::mma_commit(bar3);
@@ -692,17 +733,9 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
     // ---- dIN: table-gradient scatter for this member's levels, dL/dx ----
     {
       float din[kFpm];
-      if (kFpm == 8) {
-        tc::tmem_ld8(tc::taddr(tbase, lb, kColH + kFpm * g), din);
-      } else {
-        tc::tmem_ld4(tc::taddr(tbase, lb, kColH + kFpm * g), din);
-      }
-      tc::tmem_wait_ld();
+      ld_parts<kFpm>(tbase, lb, kFpm * g, a.one_pass, din);
       float dxl[8];
-      if (g == 0) {
-        tc::tmem_ld8(tc::taddr(tbase, lb, kColH + kXCol), dxl);
-        tc::tmem_wait_ld();
-      }
+      if (g == 0) ld_parts<8>(tbase, lb, kXCol, a.one_pass, dxl);
       float dx[3] = {0.0f, 0.0f, 0.0f};
       if (g == 0) {
         dx[0] = dxl[0];
@@ -783,7 +816,7 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
   }
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tbase, kCols);
+  if (warp == 0) tc::tmem_dealloc(tbase, kBwdCols);
 }
 
 
