@@ -395,8 +395,13 @@ struct MarchArgs {
 // skip (or the marcher stops), and the warp restarts from the broadcast state.
 // Modes: count only (num_steps), fill at packed_info offsets, or fill into
 // fixed slots ray*slot_stride (padded; num_steps written too).
-template <int MODE>  // 0 count, 1 fill packed, 2 fill padded
+// CONE false: cone_angle == 0, where calc_dt(t) = clamp(t * 0, dt_min, dt_max)
+// is dt_min for every t, so each speculative step is one addition.
+template <int MODE, bool CONE>  // MODE: 0 count, 1 fill packed, 2 fill padded
 __global__ void __launch_bounds__(128) march_warp_kernel(MarchArgs a, int64_t slot_stride) {
+  const auto step_dt = [&](float t, float cone, float lo, float hi) {
+    return CONE ? calc_dt(t, cone, lo, hi) : lo;
+  };
   const int lane = threadIdx.x & 31;
   const int64_t ray = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   if (ray >= a.n_rays) return;  // whole warp exits together
@@ -423,7 +428,7 @@ __global__ void __launch_bounds__(128) march_warp_kernel(MarchArgs a, int64_t sl
   const float dt_min = a.step, dt_max = 1e10f;
   int64_t j = 0, iters = 0;
   float t0 = near;
-  float dt = calc_dt(t0, a.cone, dt_min, dt_max);
+  float dt = step_dt(t0, a.cone, dt_min, dt_max);
   float t1 = __fadd_rn(t0, dt);
   // t_mid of the current state: (t0 + t1) / 2 after an occupied step, but the
   // skip's own result after a DDA skip (the sequential loop tests that value)
@@ -434,7 +439,7 @@ __global__ void __launch_bounds__(128) march_warp_kernel(MarchArgs a, int64_t sl
     float l0 = t0, l1 = t1;
     for (int s = 0; s < lane; ++s) {
       l0 = l1;
-      l1 = __fadd_rn(l0, calc_dt(l0, a.cone, dt_min, dt_max));
+      l1 = __fadd_rn(l0, step_dt(l0, a.cone, dt_min, dt_max));
     }
     const float tm = lane == 0 ? tm0 : __fmul_rn(__fadd_rn(l0, l1), 0.5f);
     float p[3];
@@ -458,7 +463,7 @@ __global__ void __launch_bounds__(128) march_warp_kernel(MarchArgs a, int64_t sl
     iters += m + 1;
     if (m == 32) {  // the whole warp was occupied: continue after lane 31
       t0 = __shfl_sync(0xffffffffu, l1, 31);
-      t1 = __fadd_rn(t0, calc_dt(t0, a.cone, dt_min, dt_max));
+      t1 = __fadd_rn(t0, step_dt(t0, a.cone, dt_min, dt_max));
       tm0 = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
     } else {
       // lane m holds the sequential state at the first non-occupied position
@@ -468,12 +473,12 @@ __global__ void __launch_bounds__(128) march_warp_kernel(MarchArgs a, int64_t sl
       if (lane == m) {
         if (g.ctype == SN_CONTRACTION_AABB) {
           ntm = advance_voxel(g, tm, dt_min, p, d, inv, far);
-          const float ndt = calc_dt(ntm, a.cone, dt_min, dt_max);
+          const float ndt = step_dt(ntm, a.cone, dt_min, dt_max);
           n0 = __fsub_rn(ntm, __fmul_rn(ndt, 0.5f));
           n1 = __fadd_rn(ntm, __fmul_rn(ndt, 0.5f));
         } else {
           n0 = l1;
-          n1 = __fadd_rn(n0, calc_dt(n0, a.cone, dt_min, dt_max));
+          n1 = __fadd_rn(n0, step_dt(n0, a.cone, dt_min, dt_max));
           ntm = __fmul_rn(__fadd_rn(n0, n1), 0.5f);
         }
       }
@@ -855,7 +860,10 @@ int sn_march_count(int64_t n_rays, const float* rays_o, const float* rays_d, con
                       contraction_type, step_size, cone_angle, max_iters, status));
   if (n_rays == 0) return SN_OK;
   a.num_steps = num_steps;
-  march_warp_kernel<0><<<div_up(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(a, 0);
+  if (a.cone == 0.0f)
+    march_warp_kernel<0, false><<<div_up(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(a, 0);
+  else
+    march_warp_kernel<0, true><<<div_up(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(a, 0);
   return check_launch("march_count");
 }
 
@@ -876,7 +884,10 @@ int sn_march_padded(int64_t n_rays, const float* rays_o, const float* rays_d, co
   a.ray_indices = ray_indices;
   a.t_starts = t_starts;
   a.t_ends = t_ends;
-  march_warp_kernel<2><<<div_up(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(a, slot_stride);
+  if (a.cone == 0.0f)
+    march_warp_kernel<2, false><<<div_up(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(a, slot_stride);
+  else
+    march_warp_kernel<2, true><<<div_up(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(a, slot_stride);
   return check_launch("march_padded");
 }
 
@@ -909,7 +920,10 @@ int sn_march_fill(int64_t n_rays, const float* rays_o, const float* rays_d, cons
   a.ray_indices = ray_indices;
   a.t_starts = t_starts;
   a.t_ends = t_ends;
-  march_warp_kernel<1><<<div_up(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(a, 0);
+  if (a.cone == 0.0f)
+    march_warp_kernel<1, false><<<div_up(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(a, 0);
+  else
+    march_warp_kernel<1, true><<<div_up(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(a, 0);
   return check_launch("march_fill");
 }
 
