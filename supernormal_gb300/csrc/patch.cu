@@ -201,18 +201,16 @@ __global__ void __launch_bounds__(MAXT) patch_block_kernel(PatchArgs a) {
   const int steps = a.packed[2 * p + 1];
   const float inv_s = inv_s_from(a.variance);
   if (MODE != kFwd && lane == 0) a.carry[p * P + k] = 0.0f;
-  // the first chunks' samples stay in registers across the passes (as many
-  // as the register budget of the block size allows)
-  constexpr int kCache = MAXT <= 288 ? 3 : (MAXT <= 512 ? 1 : 0);
-  Sample cache[kCache > 0 ? kCache : 1];
 
   // ---------------- forward ----------------
   float Tc = 1.0f, cp0 = 0.0f, cp1 = 0.0f, cp2 = 0.0f, ws = 0.0f, eik = 0.0f;
   if (MODE != kBwd) {
-    auto fwd_body = [&](int j0, const Sample& s) {
+    for (int j0 = 0; j0 < steps; j0 += 32) {
       const int j = j0 + lane;
       const bool ok = j < steps && base + j < S;  // S clamps a packed table past capacity
       const int64_t i = base + j;
+      Sample s;
+      chunk_sample(a, R, i, S, inv_s, ok, lane, sm_s0, sm_pos, s);
       const float T = transmittance(ok ? __fsub_rn(1.0f, s.alpha) : 1.0f, Tc, lane);
       const float w = ok ? __fmul_rn(s.alpha, T) : 0.0f;
       ws = __fadd_rn(ws, w);
@@ -231,20 +229,6 @@ __global__ void __launch_bounds__(MAXT) patch_block_kernel(PatchArgs a) {
         const float nr = sqrtf(s.g[0] * s.g[0] + s.g[1] * s.g[1] + s.g[2] * s.g[2]);
         eik += (nr - 1.0f) * (nr - 1.0f);
       }
-    };
-#pragma unroll
-    for (int c = 0; c < kCache; ++c) {
-      if (32 * c < steps) {
-        const int j = 32 * c + lane;
-        chunk_sample(a, R, base + j, S, inv_s, j < steps && base + j < S, lane, sm_s0, sm_pos, cache[c]);
-        fwd_body(32 * c, cache[c]);
-      }
-    }
-    for (int j0 = 32 * kCache; j0 < steps; j0 += 32) {
-      const int j = j0 + lane;
-      Sample s;
-      chunk_sample(a, R, base + j, S, inv_s, j < steps && base + j < S, lane, sm_s0, sm_pos, s);
-      fwd_body(j0, s);
     }
     ws = warp_sum(ws);
     cp0 = warp_sum(cp0);
@@ -301,29 +285,15 @@ __global__ void __launch_bounds__(MAXT) patch_block_kernel(PatchArgs a) {
   // ---------------- adjoint: total = sum_j g_w_j w_j ----------------
   float total = 0.0f;
   Tc = 1.0f;
-  auto total_body = [&](int j0, const Sample& s) {
+  for (int j0 = 0; j0 < steps; j0 += 32) {
     const int j = j0 + lane;
     const bool ok = j < steps && base + j < S;  // S clamps a packed table past capacity
+    Sample s;
+    chunk_sample(a, R, base + j, S, inv_s, ok, lane, sm_s0, sm_pos, s);
     const float T = transmittance(ok ? __fsub_rn(1.0f, s.alpha) : 1.0f, Tc, lane);
     const float w = ok ? __fmul_rn(s.alpha, T) : 0.0f;
     const float gw = gc[0] * s.g[0] + gc[1] * s.g[1] + gc[2] * s.g[2] + gws;
     total = __fmaf_rn(gw, w, total);
-  };
-#pragma unroll
-  for (int c = 0; c < kCache; ++c) {
-    if (32 * c < steps) {
-      if (MODE == kBwd) {  // no forward pass ran: load the cached chunks here
-        const int j = 32 * c + lane;
-        chunk_sample(a, R, base + j, S, inv_s, j < steps && base + j < S, lane, sm_s0, sm_pos, cache[c]);
-      }
-      total_body(32 * c, cache[c]);
-    }
-  }
-  for (int j0 = 32 * kCache; j0 < steps; j0 += 32) {
-    const int j = j0 + lane;
-    Sample s;
-    chunk_sample(a, R, base + j, S, inv_s, j < steps && base + j < S, lane, sm_s0, sm_pos, s);
-    total_body(j0, s);
   }
   total = warp_sum(total);
 
@@ -333,10 +303,12 @@ __global__ void __launch_bounds__(MAXT) patch_block_kernel(PatchArgs a) {
   const int ku = R.r > 0 ? k - W : k, kd = R.r < H - 1 ? k + W : k;
   float d_inv = 0.0f, prefix = 0.0f, carry_in = 0.0f;
   Tc = 1.0f;
-  auto adj_body = [&](int j0, const Sample& s) {
+  for (int j0 = 0; j0 < steps; j0 += 32) {
     const int j = j0 + lane;
     const bool ok = j < steps && base + j < S;  // S clamps a packed table past capacity
     const int64_t i = base + j;
+    Sample s;
+    chunk_sample(a, R, i, S, inv_s, ok, lane, sm_s0, sm_pos, s);
     const float T = transmittance(ok ? __fsub_rn(1.0f, s.alpha) : 1.0f, Tc, lane);
     const float w = ok ? __fmul_rn(s.alpha, T) : 0.0f;
     const float gw = ok ? gc[0] * s.g[0] + gc[1] * s.g[1] + gc[2] * s.g[2] + gws : 0.0f;
@@ -447,15 +419,6 @@ __global__ void __launch_bounds__(MAXT) patch_block_kernel(PatchArgs a) {
       }
       a.d_sdf[i * P + k] = ds0;
     }
-  };
-#pragma unroll
-  for (int c = 0; c < kCache; ++c)
-    if (32 * c < steps) adj_body(32 * c, cache[c]);
-  for (int j0 = 32 * kCache; j0 < steps; j0 += 32) {
-    const int j = j0 + lane;
-    Sample s;
-    chunk_sample(a, R, base + j, S, inv_s, j < steps && base + j < S, lane, sm_s0, sm_pos, s);
-    adj_body(j0, s);
   }
   d_inv = warp_sum(d_inv);
   if (lane == 0) red[k][0] = d_inv;
