@@ -236,12 +236,14 @@ def poisson_trace(n_objects: int, duration: float, rate: float, seed: int = 0,
 class Server:
     """Runs a request trace over ServedObjects under an HBM budget."""
 
-    def __init__(self, objects: list, budget_bytes: int, query_res: int = 256, slice_iters: int = 10):
+    def __init__(self, objects: list, budget_bytes: int, query_res: int = 256, slice_iters: int = 10,
+                 sync=None):
         self.objects = objects
         self.budget = budget_bytes
         self.query_res = query_res
         self.slice_iters = slice_iters
         self.swaps = 0
+        self.sync = torch.cuda.synchronize if sync is None else sync
 
     def resident_bytes(self) -> int:
         return sum(o.nbytes() for o in self.objects if o.resident)
@@ -292,7 +294,7 @@ class Server:
                     short_q.append(r)
 
         def finish(r):
-            torch.cuda.synchronize()
+            self.sync()
             r.done_at = now()
 
         while pending or recon_q or short_q or fifo:
