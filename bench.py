@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--cpu-sample-patches", type=int, default=8)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-clocks", action="store_true")
+    p.add_argument("--no-encoding-cache", action="store_true",
+                   help="field backward recomputes the encoding instead of reading the forward's")
     p.add_argument("--serve", choices=["small", "full", "off"], default="small",
                    help="serving-loop trace after the training measurement (p50/p99 latency)")
     p.add_argument("--quality", action="store_true",
@@ -174,7 +176,8 @@ def build_workload(args, device, seed):
                      input_concat=True).to(device)
     var = SingleVarianceNetwork(0.5).to(device)
     cfg = TrainConfig(batch_size=args.batch, step_size=2.0 / 1024, occ_update_freq=8,
-                      occ_threshold=0.1, increase_bandwidth_every=0, end_iter=5000, seed=seed)
+                      occ_threshold=0.1, increase_bandwidth_every=0, end_iter=5000, seed=seed,
+                      encoding_cache=not getattr(args, "no_encoding_cache", False))
     tr = FusedTrainer(net, var, cfg, device=device)
     net.bindwidth = ENC["n_levels"]
     return scene, rig, net, var, tr
@@ -261,7 +264,7 @@ def run_ours(args, world, rank, local):
                    "rays_per_step": args.batch * tr.P, "views": args.views,
                    "resolution": [args.height, args.width], "hash_levels": 16, "log2_table": 19,
                    "active_levels": net.active_levels(), "step_size": 2.0 / 1024,
-                   "occupancy_update_every": 8,
+                   "occupancy_update_every": 8, "encoding_cache": tr.enc_cache is not None,
                    "samples_per_ray": float(tr.S.item()) / args.batch,
                    "l2": "step working set > L2: table + Adam state 4 x 64 MiB streamed every step",
                    "parallelism": f"replicas{world}"},

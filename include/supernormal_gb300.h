@@ -241,6 +241,7 @@ typedef struct sn_mlp_desc {
   const float* b1;
   int32_t* status;   /* nullable device word: SN_STATUS_TIMEOUT is OR-ed here */
   uint32_t flags;    /* SN_FIELD_* precision options of the fused field kernels */
+  float* enc_cache;  /* nullable: encoding cache of the fused field kernels (below) */
 } sn_mlp_desc;
 
 /* sn_mlp_desc.flags (fused field forward / backward only):
@@ -250,6 +251,15 @@ typedef struct sn_mlp_desc {
  *   instead of the FP32-accurate three. */
 #define SN_FIELD_TABLE_FP16 1u
 #define SN_FIELD_MLP_TF32 2u
+
+/* sn_mlp_desc.enc_cache (no reference counterpart; the reference's autograd
+ * keeps tcnn's encoding output alive between forward and backward in the
+ * same way): n_levels * 2 floats per point of capacity n, 8-byte aligned,
+ * level l of point p at enc_cache[2 * (l * n + p)].  sn_field_fwd writes the levels
+ * below active_levels of its points there; sn_field_bwd reads them instead of
+ * gathering the table again.  The backward must see the same n, count, x,
+ * table and active_levels as the forward that filled the cache; results are
+ * identical to the recomputing backward.  sn_field_grad_fwd/bwd ignore it. */
 
 /* Level offsets, resolutions and scales of tcnn's GridEncoding for
  * {otype: HashGrid, n_levels, n_features_per_level, log2_hashmap_size,

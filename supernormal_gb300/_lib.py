@@ -56,6 +56,7 @@ class MlpDesc(C.Structure):
         ("b1", C.c_void_p),
         ("status", C.c_void_p),
         ("flags", C.c_uint32),
+        ("enc_cache", C.c_void_p),
     ]
 
 

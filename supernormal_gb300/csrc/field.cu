@@ -590,6 +590,10 @@ int sn_field_fwd(int64_t n, const int32_t* count, const float* x, const float* t
   SN_TRY(fill_field_args(a, n, count, x, table, grid, active_levels, mlp, out_cols));
   SN_REQUIRE(out != nullptr, "field_fwd: out is null");
   a.out = out;
+  if (mlp->enc_cache) {
+    SN_REQUIRE((reinterpret_cast<uintptr_t>(mlp->enc_cache) & 7u) == 0, "field_fwd: enc_cache not 8-byte aligned");
+    a.enc_out = reinterpret_cast<float2*>(mlp->enc_cache);
+  }
   if (n == 0) return SN_OK;
   return field_fwd_tc(a, as_stream(stream));
 }
@@ -609,6 +613,10 @@ int sn_field_bwd(int64_t n, const int32_t* count, const float* x, const float* g
   a.grad_b1 = grad_b1;
   a.grad_x = grad_x;
   a.pair16 = (reinterpret_cast<uintptr_t>(grad_table) & 15u) == 0;
+  if (mlp->enc_cache) {
+    SN_REQUIRE((reinterpret_cast<uintptr_t>(mlp->enc_cache) & 7u) == 0, "field_bwd: enc_cache not 8-byte aligned");
+    a.enc_in = reinterpret_cast<const float2*>(mlp->enc_cache);
+  }
   if (n == 0) return SN_OK;
   return field_bwd_tc(a, as_stream(stream));
 }

@@ -190,6 +190,21 @@ __device__ __forceinline__ void load_grad(const FieldArgs& a, int64_t p, int64_t
   for (int o = 0; o < OC; ++o) go[o] = (p < n && o < a.out_cols) ? a.grad_out[p * a.out_cols + o] : 0.0f;
 }
 
+// Member g's levels of point p from the encoding cache (zeros past n or the
+// active levels, as encode_group gives).  Read once, so streamed past L2.
+template <int M>
+__device__ __forceinline__ void load_enc(const FieldArgs& a, int g, int64_t p, int64_t n,
+                                         float e[2 * (16 / M)]) {
+#pragma unroll
+  for (int i = 0; i < 16 / M; ++i) {
+    const int l = level_of<M>(g, i);
+    float2 v = make_float2(0.0f, 0.0f);
+    if (p < n && l < a.active) v = __ldcs(a.enc_in + (int64_t)l * a.cap + p);
+    e[2 * i] = v.x;
+    e[2 * i + 1] = v.y;
+  }
+}
+
 // Encoding of member g's levels of point x: e[2i + f] for level level_of(g, i).
 // PAIRED: two levels at a time, all 16 corner gathers issued before any is
 // used (about two L2 round trips per phase instead of four; the backward,
@@ -371,6 +386,13 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
     {
       float e[8];
       encode_group<false, 4>(a, g, live, x, e);
+      if (a.enc_out && live) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int l = level_of<4>(g, i);
+          if (l < a.active) __stcs(a.enc_out + (int64_t)l * a.cap + p, make_float2(e[2 * i], e[2 * i + 1]));
+        }
+      }
       st_split8(tc::taddr(tbase, lb, kFwdColInHi + 8 * g), tc::taddr(tbase, lb, kFwdColInLo + 8 * g), e);
       if (g == 0) {
         const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
@@ -583,9 +605,12 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
   const int64_t n = effective_n(a);
   const int64_t n_tiles = (n + kTile - 1) / kTile;
   // this point's coordinates and output gradient one tile ahead
-  float xn[3] = {0.0f, 0.0f, 0.0f}, gon[kOc];
+  // (and, with the encoding cache, its member levels)
+  const bool cached = a.enc_in != nullptr;
+  float xn[3] = {0.0f, 0.0f, 0.0f}, gon[kOc], en[kFpm];
   load_point(a, (int64_t)blockIdx.x * kTile + pt, n, xn);
   load_grad<kOc>(a, (int64_t)blockIdx.x * kTile + pt, n, gon);
+  if (cached) load_enc<M>(a, g, (int64_t)blockIdx.x * kTile + pt, n, en);
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const int64_t p = tile * kTile + pt;
     const bool live = p < n;
@@ -593,13 +618,18 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
     float go[kOc];
 #pragma unroll
     for (int o = 0; o < kOc; ++o) go[o] = gon[o];
+    float e[kFpm];
+    if (cached) {
+#pragma unroll
+      for (int i = 0; i < kFpm; ++i) e[i] = en[i];
+      load_enc<M>(a, g, (tile + gridDim.x) * kTile + pt, n, en);
+    }
     load_point(a, (tile + gridDim.x) * kTile + pt, n, xn);
     load_grad<kOc>(a, (tile + gridDim.x) * kTile + pt, n, gon);
     // ---- input rows: TMEM (A of the first MMA) and IN^T (B of the third) ----
     bool ok3 = true;
     {
-      float e[kFpm];
-      encode_group<(M == 4), M>(a, g, live, x, e);
+      if (!cached) encode_group<(M == 4), M>(a, g, live, x, e);
       st_split<kFpm>(tc::taddr(tbase, lb, kColInHi + kFpm * g), tc::taddr(tbase, lb, kColInLo + kFpm * g), e);
       // the previous tile's weight-gradient MMAs still read IN^T and dH^T:
       // wait for them only now, so they overlap its scatter and these gathers

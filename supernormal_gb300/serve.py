@@ -77,8 +77,11 @@ class ServedObject:
         torch.manual_seed(spec.seed)
         net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=enc, input_concat=True).to(dev)
         var = SingleVarianceNetwork(0.3).to(dev)
+        # no encoding cache: its n_levels x 8 bytes per point of step capacity
+        # would more than double an object's device footprint
         cfg = TrainConfig(batch_size=batch, step_size=step_size, occ_update_freq=8, occ_warmup_steps=16,
-                          increase_bandwidth_every=100, end_iter=5000, seed=spec.seed)
+                          increase_bandwidth_every=100, end_iter=5000, seed=spec.seed,
+                          encoding_cache=False)
         self.tr = FusedTrainer(net, var, cfg, device=dev)
         self.graph = GraphStep(self.tr)
         self.renderer = NeuSRenderer(net, var)

@@ -50,6 +50,7 @@ class TrainConfig:
     loss_type: str = "l2"
     gradient_method: str = "dfd"            # 'dfd' (shipped) or 'ad' (second-order adjoint)
     precision: str = "fp32"                 # 'fp32' or 'mixed' (FP16 table copy, one-pass TF32 MLP)
+    encoding_cache: bool = True             # field forward keeps the encoding for the backward
     normal_weight: float = 1.0
     eikonal_weight: float = 1.0
     mask_weight: float = 1.0
@@ -205,6 +206,9 @@ class FusedTrainer:
         self.tpe = torch.empty((C0, P), device=dev)
         self.sdf1 = torch.empty((2 * C0 * P, 1), device=dev)
         self.d_sdf = torch.empty((2 * C0 * P, 1), device=dev)
+        # encoding of the training points, level-major (n_levels x 2 x capacity floats)
+        self.enc_cache = (torch.empty((self.net.encoding.n_levels * 2 * 2 * C0 * P,), device=dev)
+                          if self.cfg.encoding_cache else None)
         self.partials = torch.zeros((B, 4), device=dev)
         self.carry = torch.empty((B, P), device=dev)
         if self.cfg.gradient_method == "ad":
@@ -324,6 +328,10 @@ class FusedTrainer:
         self._mark("step_begin")
         self.weight_norm_forward(st)
         mlp = C.byref(self._mlp())
+        mlp_pts = self._mlp()      # training points: the forward fills the encoding cache
+        if self.enc_cache is not None:
+            mlp_pts.enc_cache = self.enc_cache.data_ptr()
+        mlp_pts = C.byref(mlp_pts)
         # --- inputs: mask binarisation, near/far and jitter of the centre rays ---
         call("sn_mask_prep", B * P, mask, self.mask_bin, self.mask_sum, st)
         call("sn_near_far_sphere", B, _center_ptr(rays_o, kc), _center_ptr(rays_d, kc), 3 * P,
@@ -356,7 +364,7 @@ class FusedTrainer:
              plane_n, self.endp1, self.n_ends1, self.xyz1, self.tps, self.tpe, self.q1, st)
         cap1 = 2 * C0 * P
         self._mark("field_fwd_begin")
-        call("sn_field_fwd", cap1, self.q1, self.xyz1, self._table(), gd, active, mlp, 1, self.sdf1, st)
+        call("sn_field_fwd", cap1, self.q1, self.xyz1, self._table(), gd, active, mlp_pts, 1, self.sdf1, st)
         self._mark("field_fwd_end")
         if self.profile:
             self.q_hist.append(self.q1.clone())   # field points of this step (device copy)
@@ -382,7 +390,7 @@ class FusedTrainer:
         self.dw0.zero_()
         self.dw1.zero_()
         self._mark("field_bwd_begin")
-        call("sn_field_bwd", cap1, self.q1, self.xyz1, self.d_sdf, 1, self._table(), gd, active, mlp,
+        call("sn_field_bwd", cap1, self.q1, self.xyz1, self.d_sdf, 1, self._table(), gd, active, mlp_pts,
              g["table"], self.dw0, g["b0"], self.dw1, g["b1"], None, st)
         if ad:  # second-order adjoint of the gradients
             call("sn_field_grad_bwd", C0 * P, self.sp_count, self.xyz1, self.d_ext, None, v["table"],

@@ -87,6 +87,58 @@ def test_field_backward_matches_oracle(built_lib, enc, d_out, active, cols):
         assert rel_err(g.cpu().numpy(), r.numpy()) < 1e-3, n
 
 
+@pytest.mark.parametrize("enc,d_out,active,count,flags", [(ENC1, 1, 16, None, 0), (ENC_SHIPPED, 1, 9, 1700, 0),
+                                                          (ENC2, 1, 16, 0, 0), (ENC1, 16, 12, 2100, 0),
+                                                          (ENC1, 1, 16, 2300, 3)])
+def test_encoding_cache_gives_the_recomputed_backward(built_lib, enc, d_out, active, count, flags):
+    """sn_field_fwd with an encoding cache writes the encoding of its points
+    (level-major) and nothing else; sn_field_bwd reading it gives the
+    recomputing backward's gradients (atomics order aside)."""
+    import ctypes as C
+
+    from supernormal_gb300._lib import call, stream_handle
+
+    net = make_net(enc, d_out=d_out, table_scale=1e3)
+    n, L = 2500, net.encoding.n_levels
+    x = torch.rand((n, 3), device="cuda") * 2 - 1
+    cnt = None if count is None else torch.tensor([count], dtype=torch.int32, device="cuda")
+    m = n if count is None else count
+    w0, b0, w1, b1 = (t.detach().contiguous() for t in net.mlp_tensors())
+    table32 = net.encoding.params.detach()
+    table = table32.half().contiguous() if flags & 1 else table32
+    cache = torch.full((L * 2 * n,), float("nan"), device="cuda")
+    cached, plain = net._mlp_desc(w0, b0, w1, b1), net._mlp_desc(w0, b0, w1, b1)
+    cached.flags = plain.flags = flags
+    cached.enc_cache = cache.data_ptr()
+    gd, st = C.byref(net.encoding.desc), stream_handle()
+    out_c, out_p = torch.zeros((n, d_out), device="cuda"), torch.zeros((n, d_out), device="cuda")
+    call("sn_field_fwd", n, cnt, x, table, gd, active, C.byref(cached), d_out, out_c, st)
+    call("sn_field_fwd", n, cnt, x, table, gd, active, C.byref(plain), d_out, out_p, st)
+    assert torch.equal(out_c, out_p)
+    c3 = cache.view(L, n, 2)
+    assert torch.isnan(c3[active:]).all() and torch.isnan(c3[:, m:]).all()   # nothing else written
+    if m:
+        ref = net.encoding(x, active_levels=active).detach()
+        if flags & 1:   # FP16 table: the oracle encoding of the rounded table
+            ref = torch.from_numpy(OF.encode(x.cpu(), table.float().cpu(), OF.geometry_from_module(net)).numpy())
+            ref[:, 2 * active:] = 0
+            ref = ref.cuda().float()
+        got = c3[:active, :m].permute(1, 0, 2).reshape(m, 2 * active)
+        assert rel_err(got.cpu(), ref[:m, :2 * active].cpu()) < 1e-6
+    go = torch.randn((n, d_out), device="cuda")
+
+    def bwd(desc):
+        gs = [torch.zeros_like(table32), torch.zeros_like(w0), torch.zeros_like(b0), torch.zeros_like(w1),
+              torch.zeros_like(b1), torch.zeros_like(x)]
+        call("sn_field_bwd", n, cnt, x, go, d_out, table, gd, active, C.byref(desc), *gs, st)
+        return gs
+
+    for u, v in zip(bwd(cached), bwd(plain)):
+        assert torch.isfinite(u).all()
+        scale = max(float(v.abs().max()), 1e-30)
+        assert float((u - v).abs().max()) <= 1e-5 * scale
+
+
 @pytest.mark.parametrize("spread", [1e-3, 3e-2])
 def test_field_backward_clustered_points(built_lib, spread):
     """Warps of 32 neighbouring points (as a patch's samples are): coarse levels
