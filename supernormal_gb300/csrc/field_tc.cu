@@ -28,13 +28,11 @@ namespace sn {
 namespace {
 
 constexpr int kTile = 128;
-constexpr int kWarps = 16;
-constexpr int kThreads = 32 * kWarps;
 constexpr int kK1 = 40;        // MLP input width inside the kernels (35 used)
 constexpr int kN2 = 48;        // dIN columns (N of the second MMA; 35 used)
 constexpr int kXCol = 32;      // first column of x in the permuted input
 constexpr int kOnesRow = 35;   // row of ones in IN^T (gives db0)
-constexpr uint32_t kCols = 256;      // forward: two CTAs per SM
+constexpr uint32_t kCols = 256;      // forward: up to two CTAs per SM
 constexpr uint32_t kBwdCols = 512;   // backward: one CTA per SM
 // IN^T and [dH_hi; dH_lo] (K = the tile's points, written one point per
 // thread): core matrices 144 bytes apart along K so a warp's 32 stores of one
@@ -213,7 +211,7 @@ template <bool PAIRED, int M = 4>
 __device__ __forceinline__ void encode_group(const FieldArgs& a, int g, bool live, const float x[3],
                                              float e[2 * (16 / M)]) {
   constexpr int kLpm = 16 / M;  // levels per member
-  if (!PAIRED) {
+  if constexpr (!PAIRED) {
 #pragma unroll
     for (int i = 0; i < kLpm; ++i) {
       const int l = level_of<M>(g, i);
@@ -222,8 +220,7 @@ __device__ __forceinline__ void encode_group(const FieldArgs& a, int g, bool liv
       e[2 * i] = e0;
       e[2 * i + 1] = e1;
     }
-    return;
-  }
+  } else {
 #pragma unroll
   for (int i0 = 0; i0 < kLpm; i0 += 2) {
     const int la = level_of<M>(g, i0), lb = level_of<M>(g, i0 + 1);
@@ -259,6 +256,7 @@ __device__ __forceinline__ void encode_group(const FieldArgs& a, int g, bool liv
     e[2 * i0 + 1] = live ? a1 : 0.0f;
     e[2 * i0 + 2] = live ? b0 : 0.0f;
     e[2 * i0 + 3] = live ? b1 : 0.0f;
+  }
   }
 }
 
@@ -329,33 +327,52 @@ __device__ __forceinline__ void st_split(uint32_t ta_hi, uint32_t ta_lo, const f
 // ---------------------------------------------------------------------------
 // forward
 // ---------------------------------------------------------------------------
+// M members per TMEM lane quadrant: 128 M threads; member g owns levels
+// level_of<M>(g, i), input columns (32/M)g .. and hidden units (64/M)g ...
+// M = 4: 512 threads, two CTAs per SM; M = 8: 1024 threads, one CTA per SM.
+constexpr int kFwdMembers = 4;
+
+template <int M>
 struct FwdSmem {
   static constexpr uint32_t b1_hi = 0, b1_lo = 10240, w1 = 20480, b0 = 24576, b1 = 24832,
-                            part = 24896, bar = part + 4 * kTile * kDoutMax * 4, slot = bar + 8,
+                            part = 24896, bar = part + M * kTile * kDoutMax * 4, slot = bar + 8,
                             end = slot + 8;
+  // M = 4: more than 228/3 KB, so at most two CTAs (2 x 256 TMEM columns) per SM
+  static constexpr size_t bytes = M == 4 ? 80 * 1024 : end;
 };
-constexpr size_t kFwdSmemBytes = 80 * 1024;  // > 228/3 KB: at most two CTAs (2 x 256 TMEM columns) per SM
-static_assert(FwdSmem::end <= kFwdSmemBytes, "forward shared memory map");
+static_assert(FwdSmem<4>::end <= FwdSmem<4>::bytes, "forward shared memory map");
+
+template <int N>
+__device__ __forceinline__ void tmem_ld_n(uint32_t ta, float* v) {
+  if constexpr (N == 16) tc::tmem_ld16(ta, v);
+  else if constexpr (N == 8) tc::tmem_ld8(ta, v);
+  else tc::tmem_ld4(ta, v);
+}
 
 // ONE: a single output column (the sdf; every training call), else up to kDoutMax.
-template <bool ONE>
-__global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) {
+template <bool ONE, int M>
+__global__ void __launch_bounds__(128 * M, M == 4 ? 2 : 1) field_fwd_tc_kernel(FieldArgs a) {
   constexpr int kOc = ONE ? 1 : kDoutMax;
+  constexpr int kNt = 128 * M;      // threads
+  constexpr int kLpm = 16 / M;      // levels per member
+  constexpr int kFpm = 2 * kLpm;    // input features per member
+  constexpr int kHpm = kH / M;      // hidden units per member
+  using Sm = FwdSmem<M>;
   extern __shared__ __align__(1024) uint8_t sm[];
-  float* s_w1 = reinterpret_cast<float*>(sm + FwdSmem::w1);
-  float* s_b0 = reinterpret_cast<float*>(sm + FwdSmem::b0);
-  float* s_b1 = reinterpret_cast<float*>(sm + FwdSmem::b1);
-  float* s_part = reinterpret_cast<float*>(sm + FwdSmem::part);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + FwdSmem::bar);
-  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + FwdSmem::slot);
+  float* s_w1 = reinterpret_cast<float*>(sm + Sm::w1);
+  float* s_b0 = reinterpret_cast<float*>(sm + Sm::b0);
+  float* s_b1 = reinterpret_cast<float*>(sm + Sm::b1);
+  float* s_part = reinterpret_cast<float*>(sm + Sm::part);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + Sm::bar);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + Sm::slot);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int q = warp & 3, g = warp >> 2;
   const int pt = 32 * q + lane;  // point within the tile == TMEM lane
   const int oc = a.out_cols;
   const float inv_beta = 1.0f / a.beta;
 
-  stage_w0<4>(a, sm + FwdSmem::b1_hi, sm + FwdSmem::b1_lo, nullptr, nullptr);
-  for (int e = t; e < kDoutMax * kH; e += kThreads) s_w1[e] = e / kH < oc ? a.w1[e] : 0.0f;
+  stage_w0<M>(a, sm + Sm::b1_hi, sm + Sm::b1_lo, nullptr, nullptr);
+  for (int e = t; e < kDoutMax * kH; e += kNt) s_w1[e] = e / kH < oc ? a.w1[e] : 0.0f;
   if (t < kH) s_b0[t] = a.b0[t];
   if (t < kDoutMax) s_b1[t] = t < oc ? a.b1[t] : 0.0f;
   if (warp == 0) {
@@ -369,7 +386,7 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
   tc::fence_after_sync();
   const uint32_t tbase = *slot;
   const uint32_t lb = (uint32_t)(32 * q);
-  const uint32_t s_b1_hi = tc::smem_u32(sm + FwdSmem::b1_hi), s_b1_lo = tc::smem_u32(sm + FwdSmem::b1_lo);
+  const uint32_t s_b1_hi = tc::smem_u32(sm + Sm::b1_hi), s_b1_lo = tc::smem_u32(sm + Sm::b1_lo);
   uint32_t phase = 0;
   bool ok = true;
 
@@ -384,16 +401,16 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
     const float x[3] = {xn[0], xn[1], xn[2]};
     load_point(a, (tile + gridDim.x) * kTile + pt, n, xn);
     {
-      float e[8];
-      encode_group<false, 4>(a, g, live, x, e);
+      float e[kFpm];
+      encode_group<(M == 8), M>(a, g, live, x, e);
       if (a.enc_out && live) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int l = level_of<4>(g, i);
+        for (int i = 0; i < kLpm; ++i) {
+          const int l = level_of<M>(g, i);
           if (l < a.active) __stcs(a.enc_out + (int64_t)l * a.cap + p, make_float2(e[2 * i], e[2 * i + 1]));
         }
       }
-      st_split8(tc::taddr(tbase, lb, kFwdColInHi + 8 * g), tc::taddr(tbase, lb, kFwdColInLo + 8 * g), e);
+      st_split<kFpm>(tc::taddr(tbase, lb, kFwdColInHi + kFpm * g), tc::taddr(tbase, lb, kFwdColInLo + kFpm * g), e);
       if (g == 0) {
         const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         st_split8(tc::taddr(tbase, lb, kFwdColInHi + kXCol), tc::taddr(tbase, lb, kFwdColInLo + kXCol), xv);
@@ -422,23 +439,23 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
       break;
     }
     tc::fence_after_sync();
-    // hidden units 16g..16g+15 of this point -> partial outputs
-    float h[16];
-    tc::tmem_ld16(tc::taddr(tbase, lb, kFwdColH0 + 16 * g), h);
+    // hidden units kHpm g .. kHpm g + kHpm - 1 of this point -> partial outputs
+    float h[kHpm];
+    tmem_ld_n<kHpm>(tc::taddr(tbase, lb, kFwdColH0 + kHpm * g), h);
     if (!a.one_pass) {
-      float h1[16];
-      tc::tmem_ld16(tc::taddr(tbase, lb, kFwdColH1 + 16 * g), h1);
+      float h1[kHpm];
+      tmem_ld_n<kHpm>(tc::taddr(tbase, lb, kFwdColH1 + kHpm * g), h1);
       tc::tmem_wait_ld();
 #pragma unroll
-      for (int i = 0; i < 16; ++i) h[i] += h1[i];
+      for (int i = 0; i < kHpm; ++i) h[i] += h1[i];
     }
     tc::tmem_wait_ld();
     float part[kOc];
 #pragma unroll
     for (int o = 0; o < kOc; ++o) part[o] = 0.0f;
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const int j = 16 * g + i;
+    for (int i = 0; i < kHpm; ++i) {
+      const int j = kHpm * g + i;
       float act, sg_unused;
       softplus_fwd_grad_fast(h[i] + s_b0[j], a.beta, inv_beta, a.thresh, act, sg_unused);
 #pragma unroll
@@ -454,7 +471,7 @@ __global__ void __launch_bounds__(kThreads, 2) field_fwd_tc_kernel(FieldArgs a) 
       for (int o = 0; o < oc; ++o) {
         float s = s_b1[o];
 #pragma unroll
-        for (int m = 0; m < 4; ++m) s += s_part[(m * kTile + pt) * kDoutMax + o];
+        for (int m = 0; m < M; ++m) s += s_part[(m * kTile + pt) * kDoutMax + o];
         a.out[p * oc + o] = s;
       }
     }
@@ -854,16 +871,18 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
 
 // Launchers used by sn_field_fwd / sn_field_bwd (field.cu).
 int field_fwd_tc(const FieldArgs& a, cudaStream_t st) {
-  const void* fn = a.out_cols == 1 ? reinterpret_cast<const void*>(field_fwd_tc_kernel<true>)
-                                   : reinterpret_cast<const void*>(field_fwd_tc_kernel<false>);
-  SN_TRY(ensure_smem_limit(fn, kFwdSmemBytes, "field_fwd"));
+  constexpr int M = kFwdMembers;
+  constexpr size_t smem = FwdSmem<M>::bytes;
+  const void* fn = a.out_cols == 1 ? reinterpret_cast<const void*>(field_fwd_tc_kernel<true, M>)
+                                   : reinterpret_cast<const void*>(field_fwd_tc_kernel<false, M>);
+  SN_TRY(ensure_smem_limit(fn, smem, "field_fwd"));
   const int64_t n_tiles = (a.cap + kTile - 1) / kTile;
-  const int64_t cap = 2LL * num_sms();
+  const int64_t cap = (M == 4 ? 2LL : 1LL) * num_sms();
   const unsigned grid = (unsigned)(n_tiles < cap ? n_tiles : cap);
   if (a.out_cols == 1)
-    field_fwd_tc_kernel<true><<<grid, kThreads, kFwdSmemBytes, st>>>(a);
+    field_fwd_tc_kernel<true, M><<<grid, 128 * M, smem, st>>>(a);
   else
-    field_fwd_tc_kernel<false><<<grid, kThreads, kFwdSmemBytes, st>>>(a);
+    field_fwd_tc_kernel<false, M><<<grid, 128 * M, smem, st>>>(a);
   return check_launch("field_fwd");
 }
 
