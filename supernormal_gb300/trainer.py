@@ -416,6 +416,64 @@ def _center_ptr(t: Tensor, kc: int) -> int:
     return t.data_ptr() + kc * 3 * t.element_size()
 
 
+class HostPrefetcher:
+    """Feeds a FusedTrainer from batches in pinned host memory.
+
+    Two device slots: while step i runs on the current stream, batch i+1 is
+    copied host -> device on a side stream, so the copies of every step stay
+    inside the loop but overlap the previous step's kernels.  The side stream
+    waits until the step that last read a slot has run before refilling it,
+    and each step waits for its own batch's copies.
+
+        pf = HostPrefetcher(trainer, host_batches[0])
+        pf.put(host_batches[0])
+        for i in range(n):
+            loss = pf.step(host_batches[i + 1] if i + 1 < n else None)
+    """
+
+    def __init__(self, trainer: FusedTrainer, example: tuple):
+        dev = trainer.device
+        self.tr = trainer
+        self.slots = [tuple(torch.empty(t.shape, dtype=t.dtype, device=dev) for t in example) for _ in range(2)]
+        self.copy_stream = torch.cuda.Stream(device=dev)
+        self.ready = [torch.cuda.Event(), torch.cuda.Event()]
+        self.free = [torch.cuda.Event(), torch.cuda.Event()]
+        self.used = [False, False]   # a step has read the slot (its free event is recorded)
+        self.next_slot = 0
+        self.queue: list[int] = []   # slots holding (or receiving) put() batches, oldest first
+
+    def put(self, host_batch: tuple) -> None:
+        """Start copying a pinned host batch into the next slot (at most two batches ahead)."""
+        if len(self.queue) == 2:
+            raise RuntimeError("HostPrefetcher.put: both slots hold batches no step has consumed")
+        slot = self.next_slot
+        self.next_slot ^= 1
+        start = torch.cuda.Event()
+        start.record(torch.cuda.current_stream(self.tr.device))   # the copy follows its caller's point
+        self.copy_stream.wait_event(start)
+        if self.used[slot]:
+            self.copy_stream.wait_event(self.free[slot])          # the step that read the slot has run
+        with torch.cuda.stream(self.copy_stream):
+            for dst, src in zip(self.slots[slot], host_batch):
+                dst.copy_(src, non_blocking=True)
+        self.ready[slot].record(self.copy_stream)
+        self.queue.append(slot)
+
+    def step(self, next_host_batch: tuple | None = None) -> Tensor:
+        """One training step on the oldest put() batch; starts copying next_host_batch."""
+        if not self.queue:
+            raise RuntimeError("HostPrefetcher.step: no batch was put()")
+        slot = self.queue.pop(0)
+        main = torch.cuda.current_stream(self.tr.device)
+        main.wait_event(self.ready[slot])
+        if next_host_batch is not None:
+            self.put(next_host_batch)
+        loss = self.tr.train_step(*self.slots[slot])
+        self.free[slot].record(main)
+        self.used[slot] = True
+        return loss
+
+
 class GraphStep:
     """A training iteration of a FusedTrainer as CUDA-graph replays.
 

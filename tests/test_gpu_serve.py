@@ -43,6 +43,47 @@ def test_graph_step_matches_eager(built_lib):
     assert gs._step is not None and gs._occ is not None
 
 
+def test_host_prefetcher_matches_device_batches(built_lib):
+    """Batches fed from pinned host memory through HostPrefetcher (copies on a
+    side stream, two device slots) give the losses of device-resident batches."""
+    from supernormal_gb300 import scenes
+    from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
+    from supernormal_gb300.trainer import FusedTrainer, HostPrefetcher, TrainConfig
+
+    ds = scenes.SyntheticDataset(scenes.sphere(0.5), scenes.ring_cameras(6, 96, 96, elevation_deg=20),
+                                 torch.device("cuda"))
+    enc = dict(otype="HashGrid", n_levels=16, n_features_per_level=2, log2_hashmap_size=15,
+               base_resolution=16, per_level_scale=1.447)
+
+    def make():
+        torch.manual_seed(0)
+        net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=enc, input_concat=True).cuda()
+        var = SingleVarianceNetwork(0.3).cuda()
+        cfg = TrainConfig(batch_size=128, step_size=1.0 / 96, occ_update_freq=4, occ_warmup_steps=4,
+                          increase_bandwidth_every=0, end_iter=100, seed=3)
+        net.bindwidth = 16
+        return FusedTrainer(net, var, cfg)
+
+    g = torch.Generator(device="cuda").manual_seed(1)
+    batches = [ds.gen_random_patches(128, generator=g) for _ in range(7)]
+    host = [tuple(t.cpu().pin_memory() for t in b) for b in batches]
+    direct, fed = make(), make()
+    pf = HostPrefetcher(fed, host[0])
+    pf.put(host[0])
+    ld, lf = [], []
+    for i, b in enumerate(batches):
+        ld.append(direct.train_step(*b).clone())
+        lf.append(pf.step(host[i + 1] if i + 1 < len(host) else None).clone())
+    torch.cuda.synchronize()
+    direct.check_status()
+    fed.check_status()
+    assert torch.equal(ld[0], lf[0])
+    for a, b in zip(ld, lf):
+        assert torch.allclose(a, b, rtol=2e-3, atol=1e-6), (a, b)
+    with pytest.raises(RuntimeError):
+        pf.step()                      # every put() batch was consumed
+
+
 def test_serving_loop_small_trace(built_lib):
     from supernormal_gb300.serve import ServedObject, Server, object_specs, poisson_trace
 
