@@ -435,11 +435,32 @@ __global__ void __launch_bounds__(128) march_warp_kernel(MarchArgs a, int64_t sl
   float tm0 = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
   bool overflow = false, limit = false;
   while (true) {
-    // state after `lane` occupied steps, formed with the sequential additions
+    // state after `lane` occupied steps, as the sequential additions form it:
+    // l1 = s_lane, l0 = s_(lane-1) (t0 for lane 0) with s_0 = t1 and
+    // s_(k+1) = fl(s_k + dt).  With a constant dt, s_k is guessed in closed
+    // form (t1 + k delta, one rounding) and every lane checks its own step
+    // against the sequential rule; all steps agreeing makes every guess the
+    // sequential value (induction from s_0).  Otherwise (a binade crossing
+    // that rounds, a tie, cone > 0) the additions are replayed one by one.
     float l0 = t0, l1 = t1;
-    for (int s = 0; s < lane; ++s) {
-      l0 = l1;
-      l1 = __fadd_rn(l0, step_dt(l0, a.cone, dt_min, dt_max));
+    bool exact = false;
+    if (!CONE) {
+      const float delta = __fsub_rn(__fadd_rn(t1, dt_min), t1);
+      if (lane > 0) {
+        l0 = __fmaf_rn((float)(lane - 1), delta, t1);
+        l1 = __fmaf_rn((float)lane, delta, t1);
+      }
+      exact = __all_sync(0xffffffffu, lane == 0 || __fadd_rn(l0, dt_min) == l1);
+      if (!exact) {
+        l0 = t0;
+        l1 = t1;
+      }
+    }
+    if (!exact) {
+      for (int s = 0; s < lane; ++s) {
+        l0 = l1;
+        l1 = __fadd_rn(l0, step_dt(l0, a.cone, dt_min, dt_max));
+      }
     }
     const float tm = lane == 0 ? tm0 : __fmul_rn(__fadd_rn(l0, l1), 0.5f);
     float p[3];
