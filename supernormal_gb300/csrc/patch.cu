@@ -175,8 +175,10 @@ __device__ __forceinline__ float transmittance(float v, float& carry, int lane) 
   return T;
 }
 
+// 3x3 patches (288 threads): at least three blocks per SM (72 registers);
+// unbounded, the kernel takes 96 registers and only two blocks fit.
 template <int MODE, int MAXT>
-__global__ void __launch_bounds__(MAXT) patch_block_kernel(PatchArgs a) {
+__global__ void __launch_bounds__(MAXT, MAXT == 288 ? 3 : 1) patch_block_kernel(PatchArgs a) {
   extern __shared__ float sm[];
   const int P = a.P;
   float* sm_s0 = sm;             // [32][P]
