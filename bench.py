@@ -36,6 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+import numpy as np  # noqa: E402
 import torch  # noqa: E402
 
 METRIC = "train_rays_per_s"
@@ -59,6 +60,8 @@ def parse():
     p.add_argument("--cpu-sample-patches", type=int, default=8)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-clocks", action="store_true")
+    p.add_argument("--eager", action="store_true",
+                   help="time eager launches instead of CUDA-graph replays of each iteration")
     p.add_argument("--no-encoding-cache", action="store_true",
                    help="field backward recomputes the encoding instead of reading the forward's")
     p.add_argument("--serve", choices=["small", "full", "off"], default="small",
@@ -186,7 +189,7 @@ def build_workload(args, device, seed):
 def run_ours(args, world, rank, local):
     from supernormal_gb300 import scenes
     from supernormal_gb300._lib import lib
-    from supernormal_gb300.trainer import HostPrefetcher
+    from supernormal_gb300.trainer import GraphStep, HostPrefetcher
 
     dev = torch.device("cuda", local)
     scene, rig, net, var, tr = build_workload(args, dev, seed=1234 + rank)
@@ -198,36 +201,58 @@ def run_ours(args, world, rank, local):
     for i in range(args.pretrain):
         tr.train_step(*pool[i % len(pool)])
     tr.iter_step = max(tr.iter_step, tr.cfg.occ_warmup_steps)   # post-warm-up occupancy regime
+    # iterations as CUDA-graph replays carrying the stage events (captured
+    # before the warm-up), or eager launches with --eager
+    gs = None if args.eager else GraphStep(tr, profile=True)
+    if gs is not None:
+        gs.prepare()
     for i in range(args.warmup):
-        tr.train_step(*pool[i % len(pool)])
+        if gs is not None:
+            gs.step(pool[i % len(pool)])
+        else:
+            tr.train_step(*pool[i % len(pool)])
     torch.cuda.synchronize()
     tr.check_status()
+    if gs is not None:
+        gs.flush()
+        gs.stage_marks.clear()
+        gs.points.clear()
 
     # ---------------- device-resident timed region ----------------
     K = args.steps
-    tr.profile = True
-    tr.marks.clear()
-    tr.q_hist.clear()
+    if gs is None:
+        tr.profile = True
+        tr.marks.clear()
+        tr.q_hist.clear()
     clocks = ClockSampler(local, not args.no_clocks and rank == 0)
-    launches0 = lib().sn_kernel_launches()
+    launches0 = gs.launches if gs is not None else lib().sn_kernel_launches()
     barrier(world)
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.nvtx.range_push("timed")      # profiler filter: the timed steps only
     start.record()
     for i in range(K):
-        tr.train_step(*pool[i % len(pool)])
+        if gs is not None:
+            gs.step(pool[i % len(pool)])
+        else:
+            tr.train_step(*pool[i % len(pool)])
     end.record()
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     barrier(world)
-    launches = lib().sn_kernel_launches() - launches0
     clk = clocks.stop()
     ms = start.elapsed_time(end)
     tr.check_status()
-    stages = stage_times(tr.marks)
-    q = torch.cat(tr.q_hist).double().cpu().numpy() if tr.q_hist else None
-    tr.profile = False
+    if gs is not None:
+        gs.flush()
+        launches = gs.launches - launches0
+        stages = stage_times([m for step in gs.stage_marks for m in step])
+        q = np.asarray(gs.points, dtype=np.float64)
+    else:
+        launches = lib().sn_kernel_launches() - launches0
+        stages = stage_times(tr.marks)
+        q = torch.cat(tr.q_hist).double().cpu().numpy() if tr.q_hist else None
+        tr.profile = False
     ms_max = max_over_ranks(ms, world)
     rays = args.batch * tr.P * K * world
     value = rays / (ms_max / 1e3)
@@ -237,7 +262,11 @@ def run_ours(args, world, rank, local):
     loss_host = torch.empty((5,), dtype=torch.float32).pin_memory()
     h2d = sum(t.numel() * t.element_size() for t in host[0])
     d2h = loss_host.numel() * loss_host.element_size()
-    pf = HostPrefetcher(tr, host[0])
+    pf = HostPrefetcher(tr, host[0], graph=None if args.eager else GraphStep(tr))
+    if pf.graph is not None:
+        pf.graph.prepare()
+        for i in range(3):              # replays of the fresh captures, untimed
+            pf.graph.step(pool[i % len(pool)])
     barrier(world)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -278,7 +307,7 @@ def run_ours(args, world, rank, local):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, tr, scene, rig, budget_s=20.0)
     if args.serve != "off":
-        del tr, ds, pool, host, dev_in
+        del tr, ds, pool, host, pf, gs
         torch.cuda.empty_cache()
         out["serve"] = run_serve(args.serve, dev)
     return out
@@ -378,12 +407,13 @@ def stage_times(marks):
              "occupancy": ("occ_begin", "occ_end")}
     tot = {k: 0.0 for k in pairs}
     open_ev = {}
-    for tag, ev in marks:
+    for tag, ev in marks:   # ev: a CUDA event, or ms from the step's first mark (graph replays)
         for k, (b, e) in pairs.items():
             if tag == b:
                 open_ev[k] = ev
             elif tag == e and k in open_ev:
-                tot[k] += open_ev.pop(k).elapsed_time(ev)
+                b_ev = open_ev.pop(k)
+                tot[k] += ev - b_ev if isinstance(ev, float) else b_ev.elapsed_time(ev)
     return tot
 
 
@@ -391,11 +421,13 @@ def roofline(stages, q, tr, peaks, peak_kind, K):
     """Dominant kernel's achieved algorithmic bandwidth vs the measured HBM peak."""
     L = tr.net.active_levels()
     F = 2
+    enc = L * F * 4 if tr.enc_cache is not None else 0   # encoding cache, per point
     bytes_per = {
-        # xyz + d sdf in, recomputed gather of 8 corners x F fp32 per level, float2 gradient scatter
-        "field_bwd": lambda: float(q.sum()) * (12 + 4 + 2 * L * 8 * F * 4),
-        # xyz in, gather, sdf out
-        "field_fwd": lambda: float(q.sum()) * (12 + L * 8 * F * 4 + 4),
+        # xyz + d sdf in, the encoding (cached: read back; else the gather of 8
+        # corners x F fp32 per level recomputed), float2 gradient scatter
+        "field_bwd": lambda: float(q.sum()) * (12 + 4 + (enc if enc else L * 8 * F * 4) + L * 8 * F * 4),
+        # xyz in, gather, sdf out, encoding cache written
+        "field_fwd": lambda: float(q.sum()) * (12 + L * 8 * F * 4 + 4 + enc),
         # p, g, m, v read; p, m, v, g(=0) written
         "adam": lambda: float(tr.n_params) * 32 * K,
     }

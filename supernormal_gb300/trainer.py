@@ -22,7 +22,7 @@ import torch
 from torch import Tensor
 
 from ._lib import (SN_FIELD_MLP_TF32, SN_FIELD_TABLE_FP16, SN_STATUS_CAPACITY, SN_STATUS_MARCH_LIMIT,
-                   SN_STATUS_TIMEOUT, call, stream_handle)
+                   SN_STATUS_TIMEOUT, call, lib, stream_handle)
 from .fields import SDFNetwork, SingleVarianceNetwork
 
 __all__ = ["TrainConfig", "FusedTrainer"]
@@ -148,11 +148,13 @@ class FusedTrainer:
         self.profile = False        # when True, CUDA events mark the stages of each step
         self.marks: list = []       # [(tag, torch.cuda.Event)] of the steps run while profiling
         self.q_hist: list = []      # device copies of the training field-point count per step
+        self._capturing = False
         self._alloc_step_buffers(self._max_step_size_for_capacity())
 
     def _mark(self, tag: str) -> None:
         if self.profile:
-            ev = torch.cuda.Event(enable_timing=True)
+            # under graph capture the event becomes a node of the graph
+            ev = torch.cuda.Event(enable_timing=True, external=self._capturing)
             ev.record(torch.cuda.current_stream())
             self.marks.append((tag, ev))
 
@@ -366,7 +368,7 @@ class FusedTrainer:
         self._mark("field_fwd_begin")
         call("sn_field_fwd", cap1, self.q1, self.xyz1, self._table(), gd, active, mlp_pts, 1, self.sdf1, st)
         self._mark("field_fwd_end")
-        if self.profile:
+        if self.profile and not self._capturing:
             self.q_hist.append(self.q1.clone())   # field points of this step (device copy)
         ad = c.gradient_method == "ad"
         if ad:  # gradients = d sdf / dx at the start points (models/renderer.py:225-226)
@@ -431,9 +433,10 @@ class HostPrefetcher:
             loss = pf.step(host_batches[i + 1] if i + 1 < n else None)
     """
 
-    def __init__(self, trainer: FusedTrainer, example: tuple):
+    def __init__(self, trainer: FusedTrainer, example: tuple, graph: "GraphStep | None" = None):
         dev = trainer.device
         self.tr = trainer
+        self.graph = graph            # steps as CUDA-graph replays (the batch is copied into its inputs)
         self.slots = [tuple(torch.empty(t.shape, dtype=t.dtype, device=dev) for t in example) for _ in range(2)]
         self.copy_stream = torch.cuda.Stream(device=dev)
         self.ready = [torch.cuda.Event(), torch.cuda.Event()]
@@ -468,7 +471,10 @@ class HostPrefetcher:
         main.wait_event(self.ready[slot])
         if next_host_batch is not None:
             self.put(next_host_batch)
-        loss = self.tr.train_step(*self.slots[slot])
+        if self.graph is not None:
+            loss = self.graph.step(self.slots[slot])
+        else:
+            loss = self.tr.train_step(*self.slots[slot])
         self.free[slot].record(main)
         self.used[slot] = True
         return loss
@@ -481,35 +487,110 @@ class GraphStep:
     input buffers; the post-warm-up occupancy update is captured too.  Both
     are re-captured when the step size or the bandwidth changes, and after
     the trainer's storages were reallocated (``invalidate``).  During the
-    occupancy warm-up the update runs eagerly."""
+    occupancy warm-up the update runs eagerly.
 
-    def __init__(self, trainer: FusedTrainer):
+    ``profile=True`` captures the trainer's stage events into the graphs
+    (event-record nodes) plus a copy of the step's field-point count into
+    pinned memory, in three graph copies replayed in turn: a copy's events
+    are read when it comes round again, after waiting for its previous
+    replay while the two later steps are still queued, so profiling adds no
+    gap between replays.  ``stage_marks`` then holds, per replayed step, the
+    marks as (tag, ms from the first mark), ``points`` the field points, and
+    ``launches`` counts the library kernels replayed."""
+
+    def __init__(self, trainer: FusedTrainer, profile: bool = False):
         self.tr = trainer
         c, dev = trainer.cfg, trainer.device
         B, H, W = trainer.B, c.patch_h, c.patch_w
         self.inputs = (torch.empty((B, H, W, 3), device=dev), torch.empty((B, H, W, 3), device=dev),
                        torch.empty((B, 3), device=dev), torch.empty((B, H, W, 3, 3), device=dev),
                        torch.empty((B, H, W, 3), device=dev), torch.empty((B, H, W, 1), device=dev))
-        self._step = None
-        self._step_key = None
-        self._occ = None
+        self.profile = profile
+        self.n_copies = 3 if profile else 1
+        self.stage_marks: list = []
+        self.points: list = []
+        self.launches = 0
+        self.invalidate()
 
     def invalidate(self) -> None:
-        self._step = self._step_key = self._occ = None
+        self._steps = [None] * self.n_copies
+        self._step_key = None
+        self._next = 0
+        self._occ = None
 
-    def _capture(self, fn):
+    def _capture(self, fn, snap_points: bool = False) -> dict:
+        tr = self.tr
         torch.cuda.synchronize()
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g):
-            fn()
-        return g
+        self.flush()
+        rec = {"graph": torch.cuda.CUDAGraph(), "pending": False,
+               "q_host": torch.zeros((1,), dtype=torch.int32).pin_memory() if snap_points else None}
+        prof = tr.profile
+        tr.marks.clear()
+        tr.profile, tr._capturing = self.profile, True
+        n0 = lib().sn_kernel_launches()
+        try:
+            with torch.cuda.graph(rec["graph"]):
+                fn()
+                if snap_points and self.profile:
+                    rec["q_host"].copy_(tr.q1, non_blocking=True)
+        finally:
+            tr.profile, tr._capturing = prof, False
+        rec["launches"] = lib().sn_kernel_launches() - n0
+        rec["marks"] = list(tr.marks)
+        tr.marks.clear()
+        return rec
+
+    def _replay(self, rec: dict) -> None:
+        self._harvest(rec)
+        rec["graph"].replay()
+        rec["pending"] = True
+        self.launches += rec["launches"]
+
+    def _harvest(self, rec) -> None:
+        """Read a finished replay's marks (waits for that replay only)."""
+        if rec is None or not rec["pending"]:
+            return
+        rec["pending"] = False
+        if not self.profile or not rec["marks"]:
+            return
+        marks = rec["marks"]
+        marks[-1][1].synchronize()
+        t0 = marks[0][1]
+        self.stage_marks.append([(tag, t0.elapsed_time(ev)) for tag, ev in marks])
+        if rec["q_host"] is not None:
+            self.points.append(int(rec["q_host"][0]))
+
+    def flush(self) -> None:
+        """Wait for every replay and read the marks of those not read yet."""
+        torch.cuda.synchronize()
+        for rec in self._steps + [self._occ]:
+            self._harvest(rec)
+
+    def prepare(self) -> None:
+        """Capture, ahead of the first replays, the graphs the coming
+        iterations need at the current step size and bandwidth (the step
+        copies and, past the occupancy warm-up, the occupancy update)."""
+        tr, c = self.tr, self.tr.cfg
+        it = tr.iter_step
+        key = (tr.step_size(it), tr.net.active_levels())
+        if key != self._step_key:
+            self.flush()
+            self._steps = [None] * self.n_copies
+            self._step_key = key
+            self._next = 0
+        for k in range(self.n_copies):
+            if self._steps[k] is None:
+                self._steps[k] = self._capture(lambda: tr.run_step(*self.inputs, key[0], key[1]),
+                                               snap_points=True)
+        if c.occ_update_freq > 0 and it >= c.occ_warmup_steps and self._occ is None:
+            self._occ = self._capture(lambda: tr.occupancy_update(c.occ_warmup_steps))
 
     def step(self, batch=None) -> Tensor:
         """One iteration; ``batch`` (6 tensors as from gen_random_patches) is
         copied into the static inputs, or the caller filled ``inputs``."""
         tr, c = self.tr, self.tr.cfg
         if tr.profile:
-            raise RuntimeError("GraphStep does not record stage events")
+            raise RuntimeError("GraphStep replaces the trainer's eager stage events (profile=True here)")
         it = tr.iter_step
         if c.occ_update_freq > 0 and it % c.occ_update_freq == 0:
             if it < c.occ_warmup_steps:
@@ -517,16 +598,22 @@ class GraphStep:
             else:
                 if self._occ is None:
                     self._occ = self._capture(lambda: tr.occupancy_update(c.occ_warmup_steps))
-                self._occ.replay()
+                self._replay(self._occ)
         if c.increase_bandwidth_every > 0 and it % c.increase_bandwidth_every == 0:
             tr.net.increase_bandwidth()
         if batch is not None:
             for dst, src in zip(self.inputs, batch):
                 dst.copy_(src, non_blocking=True)
         key = (tr.step_size(it), tr.net.active_levels())
-        if self._step is None or key != self._step_key:
-            self._step = self._capture(lambda: tr.run_step(*self.inputs, key[0], key[1]))
+        if key != self._step_key:
+            self.flush()
+            self._steps = [None] * self.n_copies
             self._step_key = key
-        self._step.replay()
+            self._next = 0
+        k = self._next
+        self._next = (k + 1) % self.n_copies
+        if self._steps[k] is None:
+            self._steps[k] = self._capture(lambda: tr.run_step(*self.inputs, key[0], key[1]), snap_points=True)
+        self._replay(self._steps[k])
         tr.iter_step += 1
         return tr.loss_out

@@ -40,7 +40,57 @@ def test_graph_step_matches_eager(built_lib):
     assert torch.equal(le[0], lg[0])
     for a, b in zip(le, lg):
         assert torch.allclose(a, b, rtol=2e-3, atol=1e-6), (a, b)
-    assert gs._step is not None and gs._occ is not None
+    assert gs._steps[0] is not None and gs._occ is not None
+
+
+def test_graph_step_profile_marks(built_lib):
+    """Profiled graph replays (three copies with captured stage events) report
+    every step's stage marks in order, its field-point count and the kernels
+    replayed, and train like the eager iteration."""
+    from supernormal_gb300 import scenes
+    from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
+    from supernormal_gb300.trainer import FusedTrainer, GraphStep, TrainConfig
+
+    ds = scenes.SyntheticDataset(scenes.sphere(0.5), scenes.ring_cameras(6, 96, 96, elevation_deg=20),
+                                 torch.device("cuda"))
+    enc = dict(otype="HashGrid", n_levels=16, n_features_per_level=2, log2_hashmap_size=15,
+               base_resolution=16, per_level_scale=1.447)
+
+    def make():
+        torch.manual_seed(0)
+        net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=enc, input_concat=True).cuda()
+        var = SingleVarianceNetwork(0.3).cuda()
+        cfg = TrainConfig(batch_size=128, step_size=1.0 / 96, occ_update_freq=4, occ_warmup_steps=4,
+                          increase_bandwidth_every=0, end_iter=100, seed=3)
+        net.bindwidth = 16
+        return FusedTrainer(net, var, cfg)
+
+    g = torch.Generator(device="cuda").manual_seed(1)
+    batches = [ds.gen_random_patches(128, generator=g) for _ in range(10)]
+    eager, graphed = make(), make()
+    for b in batches[:4]:                      # occupancy warm-up runs eagerly in both
+        eager.train_step(*b)
+        graphed.train_step(*b)
+    gs = GraphStep(graphed, profile=True)
+    gs.prepare()
+    le, lg = [], []
+    for b in batches[4:]:
+        le.append(eager.train_step(*b).clone())
+        lg.append(gs.step(b).clone())
+    gs.flush()
+    eager.check_status()
+    graphed.check_status()
+    for a, b in zip(le, lg):
+        assert torch.allclose(a, b, rtol=2e-3, atol=1e-6), (a, b)
+    steps = [m for m in gs.stage_marks if m[0][0] == "step_begin"]
+    assert len(steps) == 6 and len(gs.points) == 6 and all(p > 0 for p in gs.points)
+    tags = [t for t, _ in steps[0]]
+    assert tags.index("field_fwd_begin") < tags.index("field_bwd_begin") < tags.index("adam_end")
+    for m in steps:
+        ts = [t for _, t in m]
+        assert all(b >= a for a, b in zip(ts, ts[1:])) and ts[-1] > 0.0
+    assert any(m[0][0] == "occ_begin" for m in gs.stage_marks)   # the occupancy graph's own marks
+    assert gs.launches > 6 * 10
 
 
 def test_host_prefetcher_matches_device_batches(built_lib):
