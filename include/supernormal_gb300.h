@@ -430,6 +430,22 @@ int sn_near_far_sphere(int64_t n, const float* rays_o, const float* rays_d,
                        int64_t stride, float* near, float* far, float* jitter,
                        uint64_t seed, const int32_t* stream_counter,
                        float* rays_o_out, float* rays_d_out, void* stream);
+/* Training patches on the device (models/dataset_loader.py:223-277) with the
+ * rays and V^-1 formed per pixel instead of read from per-view (H, W, 3) and
+ * (H, W, 3, 3) tables (:112-145): for patch b of view img[b] centred at
+ * (cx[b], cy[b]), pixel (x, y) gets d = R normalize(K^-1 [x, y, 1]), origin t
+ * and V^-1 with V = rows (d, R[:,0], R[:,1]); plane_n[b] = R[:,2].  kinv
+ * (n_views, 3, 3) and pose (n_views, 3, 4) = [R | t] are double; normals
+ * (n_views, H, W, 3) and masks (n_views, H, W) are gathered when given.
+ * Outputs: rays_o / rays_d / normal_out (n, ph, pw, 3), vinv (n, ph, pw, 3, 3),
+ * mask_out (n, ph, pw), plane_n (n, 3).  Centres must keep the patch inside
+ * the view. */
+int sn_gen_patches(int64_t n_patches, int patch_h, int patch_w,
+                   const int32_t* cx, const int32_t* cy, const int32_t* img,
+                   int n_views, int H, int W, const double* kinv,
+                   const double* pose, const float* normals, const float* masks,
+                   float* rays_o, float* rays_d, float* plane_n, float* vinv,
+                   float* normal_out, float* mask_out, void* stream);
 /* *out = *in * mul + add on the device (counts derived without a host sync). */
 int sn_scale_count(const int32_t* in, int32_t mul, int32_t add, int32_t* out,
                    void* stream);

@@ -119,6 +119,7 @@ SIGNATURES: dict[str, tuple] = {
     "sn_patch_carry_fixup": (_I, [_I64, _I, _P, _P, _I64, _P, _P, _P, _P]),
     "sn_patch_finalize": (_I, [_I64, _I, _P, _P, _I64, _P, _P, _F, _F, _F, _P, _P, _P]),
     "sn_scale_count": (_I, [_P, C.c_int32, C.c_int32, _P, _P]),
+    "sn_gen_patches": (_I, [_I64, _I, _I, _P, _P, _P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sn_mask_prep": (_I, [_I64, _P, _P, _P, _P]),
     "sn_lr_schedule": (_I, [_P, _P, _P, _F, _I, _I, _F, _P]),
     "sn_adam_step": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _F, _I, _F, _F, _F, _I, _P]),

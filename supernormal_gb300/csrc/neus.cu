@@ -204,6 +204,67 @@ mask_prep_kernel(int64_t n, const float* __restrict__ mask_in, float* __restrict
   }
 }
 
+// One thread per patch pixel: world ray direction R normalize(K^-1 [x, y, 1]),
+// V = rows (d, camera right, camera down) and V^-1 by the adjugate, in double
+// and rounded once (models/dataset_loader.py:112-137), plus the ground-truth
+// gathers and per-patch origin / plane normal (models/dataset_loader.py:223-277).
+__global__ void gen_patches_kernel(int64_t n_patches, int ph, int pw, const int32_t* __restrict__ cx,
+                                   const int32_t* __restrict__ cy, const int32_t* __restrict__ img, int H,
+                                   int W, const double* __restrict__ kinv, const double* __restrict__ pose,
+                                   const float* __restrict__ normals, const float* __restrict__ masks,
+                                   float* __restrict__ rays_o, float* __restrict__ rays_d,
+                                   float* __restrict__ plane_n, float* __restrict__ vinv,
+                                   float* __restrict__ normal_out, float* __restrict__ mask_out) {
+  const int P = ph * pw;
+  const int64_t n = n_patches * P;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / P;
+    const int r = (int)(i - b * P), yy = r / pw, xx = r - yy * pw;
+    const int v = img[b];
+    const int px = cx[b] + xx - pw / 2, py = cy[b] + yy - ph / 2;
+    const double* K = kinv + 9 * v;
+    const double* T = pose + 12 * v;   // rows of [R | t]
+    double q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) q[k] = K[3 * k] * px + K[3 * k + 1] * py + K[3 * k + 2];
+    const double inv_norm = 1.0 / sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+    double rw[3][3];   // rows d, right, down
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      rw[0][k] = (T[4 * k] * q[0] + T[4 * k + 1] * q[1] + T[4 * k + 2] * q[2]) * inv_norm;
+      rw[1][k] = T[4 * k];
+      rw[2][k] = T[4 * k + 1];
+    }
+    double c[3][3];    // c[j] = r(j+1) x r(j+2): column j of the adjugate
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double* a = rw[(j + 1) % 3];
+      const double* e = rw[(j + 2) % 3];
+      c[j][0] = a[1] * e[2] - a[2] * e[1];
+      c[j][1] = a[2] * e[0] - a[0] * e[2];
+      c[j][2] = a[0] * e[1] - a[1] * e[0];
+    }
+    const double det = rw[0][0] * c[0][0] + rw[0][1] * c[0][1] + rw[0][2] * c[0][2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      rays_d[3 * i + k] = (float)rw[0][k];
+      rays_o[3 * i + k] = (float)T[4 * k + 3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) vinv[9 * i + 3 * k + j] = (float)(c[j][k] / det);
+    }
+    const int64_t pix = ((int64_t)v * H + py) * W + px;
+    if (normals) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) normal_out[3 * i + k] = normals[3 * pix + k];
+    }
+    if (masks) mask_out[i] = masks[pix];
+    if (r == 0) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) plane_n[3 * b + k] = (float)T[4 * k + 2];
+    }
+  }
+}
+
 }  // namespace sn
 
 using namespace sn;
@@ -285,6 +346,22 @@ int sn_near_far_sphere(int64_t n, const float* rays_o, const float* rays_d, int6
   near_far_kernel<<<stride_grid(n, 256, 8), 256, 0, as_stream(stream)>>>(
       n, rays_o, rays_d, stride, near, far, jitter, seed, stream_counter, rays_o_out, rays_d_out);
   return check_launch("near_far_sphere");
+}
+
+int sn_gen_patches(int64_t n_patches, int patch_h, int patch_w, const int32_t* cx, const int32_t* cy,
+                   const int32_t* img, int n_views, int H, int W, const double* kinv, const double* pose,
+                   const float* normals, const float* masks, float* rays_o, float* rays_d, float* plane_n,
+                   float* vinv, float* normal_out, float* mask_out, void* stream) {
+  SN_REQUIRE(n_patches >= 0 && patch_h >= 1 && patch_w >= 1 && n_views >= 1 && H >= patch_h && W >= patch_w,
+             "gen_patches: bad sizes");
+  SN_REQUIRE(cx && cy && img && kinv && pose && rays_o && rays_d && plane_n && vinv, "gen_patches: null buffer");
+  SN_REQUIRE(!normals || normal_out, "gen_patches: normals given without normal_out");
+  SN_REQUIRE(!masks || mask_out, "gen_patches: masks given without mask_out");
+  if (n_patches == 0) return SN_OK;
+  gen_patches_kernel<<<stride_grid(n_patches * patch_h * patch_w, 256, 8), 256, 0, as_stream(stream)>>>(
+      n_patches, patch_h, patch_w, cx, cy, img, H, W, kinv, pose, normals, masks, rays_o, rays_d, plane_n, vinv,
+      normal_out, mask_out);
+  return check_launch("gen_patches");
 }
 
 int sn_scale_count(const int32_t* in, int32_t mul, int32_t add, int32_t* out, void* stream) {

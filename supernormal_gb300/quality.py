@@ -26,8 +26,9 @@ def render_view(renderer: NeuSRenderer, ds: scenes.SyntheticDataset, view: int, 
     ph, pw = H // 3, W // 3
     blk = lambda t: t[: 3 * ph, : 3 * pw].reshape(ph, 3, pw, 3, *t.shape[2:]).transpose(1, 2).reshape(
         ph * pw, 3, 3, *t.shape[2:]).contiguous()
-    rays_d = blk(ds.rays_all[view])
-    vinv = blk(ds.V_inverse_all[view])
+    d, vi = scenes.view_rays(ds.rig, view, ds.device)
+    rays_d = blk(d)
+    vinv = blk(vi)
     pose = ds.pose_all[view]
     rays_o = pose[:3, 3].expand(rays_d.shape).contiguous()
     plane_n = pose[:3, 2].expand(rays_d.shape[0], 3).contiguous()

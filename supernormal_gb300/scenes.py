@@ -202,23 +202,26 @@ def sphere_trace(scene: SDFScene, o: Tensor, d: Tensor, near: Tensor, far: Tenso
 
 @dataclass
 class SyntheticDataset:
-    """Views of an analytic scene with GT normals / masks and per-pixel V^-1,
-    resident on `device`; gen_random_patches mirrors the reference sampler."""
+    """Views of an analytic scene with GT normals / masks, resident on
+    `device`; gen_random_patches mirrors the reference sampler.  On a GPU the
+    patches' rays and V^-1 are formed per pixel by `sn_gen_patches`, so no
+    per-pixel (H, W, 3) ray or (H, W, 3, 3) V^-1 table is kept (48 B per
+    pixel); `rays_all` / `V_inverse_all` build those tables on first use."""
 
     scene: SDFScene
     rig: CameraRig
     device: torch.device
     normals: Tensor = field(init=False)      # (n, H, W, 3) float32
     masks: Tensor = field(init=False)        # (n, H, W) float32
-    V_inverse_all: Tensor = field(init=False)  # (n, H, W, 3, 3) float32
-    rays_all: Tensor = field(init=False)     # (n, H, W, 3) float32
+    kinv: Tensor = field(init=False)         # (n, 3, 3) float64 K^-1
+    pose34: Tensor = field(init=False)       # (n, 3, 4) float64 [R | t]
 
     def __post_init__(self):
         n, H, W = self.rig.poses.shape[0], self.rig.H, self.rig.W
         dev = self.device
         ys, xs = torch.meshgrid(torch.arange(H, device=dev, dtype=torch.float64),
                                 torch.arange(W, device=dev, dtype=torch.float64), indexing="ij")
-        normals, masks, vinvs, rays = [], [], [], []
+        normals, masks = [], []
         for v in range(n):
             d = pixel_rays(self.rig, v, xs, ys)                         # (H, W, 3)
             o = self.rig.poses[v, :3, 3].to(dev).expand_as(d)
@@ -229,18 +232,30 @@ class SyntheticDataset:
             nrm = self.scene.normal(pts) * hit[:, None]
             normals.append(nrm.reshape(H, W, 3).float())
             masks.append(hit.reshape(H, W).float())
-            right = self.rig.poses[v, :3, 0].to(dev).expand_as(d)
-            down = self.rig.poses[v, :3, 1].to(dev).expand_as(d)
-            V = torch.stack([d, right, down], dim=-2)                  # rows: d, right, down
-            vinvs.append(inv3x3(V).float())
-            rays.append(d.float())
         self.normals = torch.stack(normals)
         self.masks = torch.stack(masks)
-        self.V_inverse_all = torch.stack(vinvs)
-        self.rays_all = torch.stack(rays)
         self.pose_all = self.rig.poses.to(dev).float()
         self.intrinsics_all = self.rig.intrinsics.to(dev).float()
+        self.kinv = inv3x3(self.rig.intrinsics[:, :3, :3].double()).to(dev).contiguous()
+        self.pose34 = self.rig.poses[:, :3, :4].double().to(dev).contiguous()
         self.n_images, self.H, self.W = n, H, W
+        self._tables = None
+
+    def _build_tables(self):
+        if self._tables is None:
+            views = [view_rays(self.rig, v, self.device) for v in range(self.n_images)]
+            self._tables = (torch.stack([d for d, _ in views]), torch.stack([vi for _, vi in views]))
+        return self._tables
+
+    @property
+    def rays_all(self) -> Tensor:
+        """(n, H, W, 3) float32 ray directions, built on first use."""
+        return self._build_tables()[0]
+
+    @property
+    def V_inverse_all(self) -> Tensor:
+        """(n, H, W, 3, 3) float32 V^-1 (models/dataset_loader.py:112-137), built on first use."""
+        return self._build_tables()[1]
 
     def gen_random_patches(self, num_patch: int, patch_H: int = 3, patch_W: int = 3,
                            generator: Optional[torch.Generator] = None):
@@ -250,6 +265,20 @@ class SyntheticDataset:
         cx = torch.randint(patch_W // 2, self.W - 1 - patch_W // 2, (num_patch,), device=dev, generator=g)
         cy = torch.randint(patch_H // 2, self.H - 1 - patch_H // 2, (num_patch,), device=dev, generator=g)
         img = torch.randint(0, self.n_images, (num_patch,), device=dev, generator=g)
+        if self.device.type == "cuda":
+            from ._lib import call, stream_handle
+
+            shp = (num_patch, patch_H, patch_W)
+            rays_o = torch.empty(shp + (3,), device=dev)
+            rays_d = torch.empty(shp + (3,), device=dev)
+            plane_n = torch.empty((num_patch, 3), device=dev)
+            vinv = torch.empty(shp + (3, 3), device=dev)
+            normal = torch.empty(shp + (3,), device=dev)
+            mask = torch.empty(shp + (1,), device=dev)
+            call("sn_gen_patches", num_patch, patch_H, patch_W, cx.int(), cy.int(), img.int(), self.n_images,
+                 self.H, self.W, self.kinv, self.pose34, self.normals, self.masks, rays_o, rays_d, plane_n,
+                 vinv, normal, mask, stream_handle())
+            return rays_o, rays_d, plane_n, vinv, normal, mask
         ox = torch.arange(-(patch_W // 2), patch_W // 2 + 1, device=dev)
         oy = torch.arange(-(patch_H // 2), patch_H // 2 + 1, device=dev)
         px = cx[:, None, None] + ox[None, None, :].expand(1, patch_H, patch_W)

@@ -100,8 +100,7 @@ class ServedObject:
         """Storages holding persistent state (copied on offload) vs workspace."""
         tr, ds = self.tr, self.ds
         state_t = [tr.params, tr.exp_avg, tr.exp_avg_sq, tr.iter_dev, tr.lr_dev, tr.adam_step_dev,
-                   tr.status, ds.normals, ds.masks, ds.V_inverse_all, ds.rays_all, ds.pose_all,
-                   ds.intrinsics_all]
+                   tr.status, ds.normals, ds.masks, ds.kinv, ds.pose34, ds.pose_all, ds.intrinsics_all]
         state_t += list(tr.grid.buffers()) + list(tr.net.buffers())
         if tr.params_half is not None:
             state_t.append(tr.params_half)
