@@ -248,7 +248,9 @@ def run_ours(args, world, rank, local):
         launches = gs.launches - launches0
         stages = stage_times([m for step in gs.stage_marks for m in step])
         q = np.asarray(gs.points, dtype=np.float64)
+        samples = np.asarray(gs.samples, dtype=np.float64)
     else:
+        samples = None
         launches = lib().sn_kernel_launches() - launches0
         stages = stage_times(tr.marks)
         q = torch.cat(tr.q_hist).double().cpu().numpy() if tr.q_hist else None
@@ -301,6 +303,7 @@ def run_ours(args, world, rank, local):
         "gpu_launches": int(launches),
         "roofline": rl,
         "stages_ms_per_step": {k: v / K for k, v in stages.items()},
+        "stage_roofline": stage_rooflines(stages, q, samples, tr, rl["peak"], K),
     }
     if clk:
         out["clocks"] = clk
@@ -415,6 +418,33 @@ def stage_times(marks):
                 b_ev = open_ev.pop(k)
                 tot[k] += ev - b_ev if isinstance(ev, float) else b_ev.elapsed_time(ev)
     return tot
+
+
+def stage_rooflines(stages, q, samples, tr, peak, K):
+    """Achieved algorithmic GB/s of the other stages (per-unit bytes as in the
+    survey's measurement table): marcher 16 B per marched centre sample + 8 B
+    per ray; patch render 36 B per patch-pixel sample + 16 B per pixel; Adam
+    32 B per parameter; field kernels as in roofline()."""
+    if samples is None or q is None or len(samples) == 0:
+        return None
+    L, F = tr.net.active_levels(), 2
+    enc = L * F * 4 if tr.enc_cache is not None else 0
+    marched, kept = samples[:, 0].sum(), samples[:, 1].sum()
+    steps = len(samples)
+    nbytes = {
+        "march": marched * 16 + steps * tr.B * 8,
+        "render": kept * tr.P * 36 + steps * tr.B * tr.P * 16,
+        "adam": float(tr.n_params) * 32 * steps,
+        "field_fwd": float(q.sum()) * (12 + L * 8 * F * 4 + 4 + enc),
+        "field_bwd": float(q.sum()) * (12 + 4 + (enc if enc else L * 8 * F * 4) + L * 8 * F * 4),
+    }
+    out = {}
+    for k, b in nbytes.items():
+        ms = stages[k] * steps / K
+        gbs = b / (ms / 1e3) / 1e9 if ms > 0 else None
+        out[k] = {"achieved_gbs": gbs, "frac": gbs / peak if gbs else None,
+                  "bytes_per_step": b / steps}
+    return out
 
 
 def roofline(stages, q, tr, peaks, peak_kind, K):

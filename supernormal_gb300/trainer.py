@@ -495,8 +495,9 @@ class GraphStep:
     are read when it comes round again, after waiting for its previous
     replay while the two later steps are still queued, so profiling adds no
     gap between replays.  ``stage_marks`` then holds, per replayed step, the
-    marks as (tag, ms from the first mark), ``points`` the field points, and
-    ``launches`` counts the library kernels replayed."""
+    marks as (tag, ms from the first mark), ``points`` the field points,
+    ``samples`` the marched and kept centre samples, and ``launches`` counts
+    the library kernels replayed."""
 
     def __init__(self, trainer: FusedTrainer, profile: bool = False):
         self.tr = trainer
@@ -509,6 +510,7 @@ class GraphStep:
         self.n_copies = 3 if profile else 1
         self.stage_marks: list = []
         self.points: list = []
+        self.samples: list = []    # per replayed step: (marched centre samples, kept samples)
         self.launches = 0
         self.invalidate()
 
@@ -523,7 +525,7 @@ class GraphStep:
         torch.cuda.synchronize()
         self.flush()
         rec = {"graph": torch.cuda.CUDAGraph(), "pending": False,
-               "q_host": torch.zeros((1,), dtype=torch.int32).pin_memory() if snap_points else None}
+               "q_host": torch.zeros((3,), dtype=torch.int32).pin_memory() if snap_points else None}
         prof = tr.profile
         tr.marks.clear()
         tr.profile, tr._capturing = self.profile, True
@@ -532,7 +534,9 @@ class GraphStep:
             with torch.cuda.graph(rec["graph"]):
                 fn()
                 if snap_points and self.profile:
-                    rec["q_host"].copy_(tr.q1, non_blocking=True)
+                    rec["q_host"][0:1].copy_(tr.q1, non_blocking=True)
+                    rec["q_host"][1:2].copy_(tr.total0, non_blocking=True)
+                    rec["q_host"][2:3].copy_(tr.S, non_blocking=True)
         finally:
             tr.profile, tr._capturing = prof, False
         rec["launches"] = lib().sn_kernel_launches() - n0
@@ -558,7 +562,9 @@ class GraphStep:
         t0 = marks[0][1]
         self.stage_marks.append([(tag, t0.elapsed_time(ev)) for tag, ev in marks])
         if rec["q_host"] is not None:
-            self.points.append(int(rec["q_host"][0]))
+            q = rec["q_host"].tolist()
+            self.points.append(q[0])
+            self.samples.append((q[1], q[2]))
 
     def flush(self) -> None:
         """Wait for every replay and read the marks of those not read yet."""
