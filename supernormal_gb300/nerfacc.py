@@ -318,11 +318,13 @@ def ray_marching(rays_o: Tensor, rays_d: Tensor, t_min: Optional[Tensor] = None,
                  alpha_fn: Optional[Callable] = None, early_stop_eps: float = 1e-4,
                  alpha_thre: float = 0.0, near_plane: Optional[float] = None,
                  far_plane: Optional[float] = None, render_step_size: float = 1e-3,
-                 stratified: bool = False, cone_angle: float = 0.0
+                 stratified: bool = False, cone_angle: float = 0.0,
+                 generator: Optional[torch.Generator] = None
                  ) -> Tuple[Tensor, Tensor, Tensor]:
     """Ray marching with occupancy-grid skipping and visibility culling
     (NA/nerfacc/ray_marching.py:13-222): returns ray_indices (N,) int64,
-    t_starts (N, 1), t_ends (N, 1)."""
+    t_starts (N, 1), t_ends (N, 1).  ``generator`` (an addition) draws the
+    stratified jitter, so that a render can be reproduced."""
     _need_cuda(rays_o)
     if alpha_fn is not None and sigma_fn is not None:
         raise ValueError("Only one of `alpha_fn` and `sigma_fn` should be provided.")
@@ -340,7 +342,8 @@ def ray_marching(rays_o: Tensor, rays_d: Tensor, t_min: Optional[Tensor] = None,
     rays_d = rays_d.contiguous().float()
     t_min = t_min.contiguous().float()
     t_max = t_max.contiguous().float()
-    jitter = torch.rand_like(t_min) if stratified else None
+    jitter = (torch.rand(t_min.shape, dtype=t_min.dtype, device=t_min.device, generator=generator)
+              if stratified else None)
     packed, ray_indices, t_starts, t_ends = march_packed(
         rays_o, rays_d, t_min, t_max, grid, render_step_size, cone_angle, jitter)
     if sigma_fn is not None or alpha_fn is not None:

@@ -138,7 +138,7 @@ class NeuSRenderer:
         return alpha_fn
 
     def render(self, rays_o_patch_all, rays_d_patch_all, marching_plane_normal, near, far,
-               V_inverse_patch_all, val_gradient_method="dfd", mode="train"):
+               V_inverse_patch_all, val_gradient_method="dfd", mode="train", generator=None):
         patch_H, patch_W = rays_o_patch_all.shape[1], rays_o_patch_all.shape[2]
         num_patch = rays_o_patch_all.shape[0]
         P = patch_H * patch_W
@@ -155,7 +155,7 @@ class NeuSRenderer:
             patch_indices, t_s, t_e = ray_marching(
                 ro_c, rd_c, t_min=near, t_max=far, grid=self.occupancy_grid,
                 render_step_size=self.sampling_step_size, stratified=True, cone_angle=0.0,
-                early_stop_eps=1e-8, alpha_fn=self._center_alpha_fn(ro_c, rd_c))
+                early_stop_eps=1e-8, alpha_fn=self._center_alpha_fn(ro_c, rd_c), generator=generator)
         self.last_samples = (patch_indices, t_s, t_e)
         return self.render_samples(ro, rd, marching_plane_normal, V_inverse_patch_all, patch_indices,
                                    t_s, t_e, gradient_method)

@@ -127,11 +127,10 @@ class ServedObject:
         if not self.resident:
             return
         torch.cuda.synchronize()
-        self._host = {}
         for i, st in enumerate(self._state):
-            h = torch.empty(st.nbytes(), dtype=torch.uint8, pin_memory=True)
-            h.untyped_storage().copy_(st)
-            self._host[i] = h
+            if i not in self._host:     # pinned once per object, reused by every offload
+                self._host[i] = torch.empty(st.nbytes(), dtype=torch.uint8, pin_memory=True)
+            self._host[i].untyped_storage().copy_(st)
         for st in self._state + self._work:
             st.resize_(0)
         self.graph.invalidate()
@@ -148,7 +147,6 @@ class ServedObject:
         for i, st in enumerate(self._state):
             st.copy_(self._host[i].untyped_storage(), non_blocking=True)
         self.tr.grads.zero_()          # zero at rest (Adam consumes and clears them)
-        self._host = {}
         self.graph.invalidate()
         self.resident = True
 
@@ -185,11 +183,12 @@ class ServedObject:
         plane_n = pose[:3, 2].expand(rays_d.shape[0], 3).contiguous()
         out = torch.empty_like(rays_d)
         self.renderer.gradient_method = "dfd"
+        jit = torch.Generator(device=dev).manual_seed(pose_seed)   # the request's own stratified jitter
         for a in range(0, rays_d.shape[0], chunk):
             b = min(a + chunk, rays_d.shape[0])
             near, far = near_far_from_sphere(rays_o[a:b, 1, 1].contiguous(), rays_d[a:b, 1, 1].contiguous())
             r = self.renderer.render(rays_o[a:b], rays_d[a:b], plane_n[a:b], near, far, vinv[a:b],
-                                     mode="eval")
+                                     mode="eval", generator=jit)
             out[a:b] = r["comp_normal"]
         return out.reshape(ph, pw, 3, 3, 3).transpose(1, 2).reshape(H, W, 3)
 
@@ -246,6 +245,18 @@ class Server:
         self.slice_iters = slice_iters
         self.swaps = 0
         self.sync = torch.cuda.synchronize if sync is None else sync
+        if sync is None:
+            self.mark = self._record_event
+            self.wait = lambda ev: ev.synchronize()
+        else:                     # host-only tests: no device work to wait for
+            self.mark = lambda: None
+            self.wait = lambda ev: None
+
+    @staticmethod
+    def _record_event():
+        ev = torch.cuda.Event()
+        ev.record()
+        return ev
 
     def resident_bytes(self) -> int:
         return sum(o.nbytes() for o in self.objects if o.resident)
@@ -284,6 +295,7 @@ class Server:
         now = lambda: time.perf_counter() - t0
         busy = 0.0
         train_rays = render_rays = 0
+        slice_done: list = []     # completion marks of queued reconstruction slices
 
         def arrive():
             while pending and pending[0].arrival <= now():
@@ -320,8 +332,13 @@ class Server:
                     finish(r)
                     if policy != "plain":
                         recon_q.popleft()
-                # (a slice ends without a device sync: the host looks at new
-                # arrivals while the GPU works through the queued iterations)
+                elif policy != "plain":
+                    # a slice ends without a device sync (the host looks at new
+                    # arrivals while the GPU works), but at most two slices are
+                    # queued: a short request never waits behind a longer backlog
+                    slice_done.append(self.mark())
+                    if len(slice_done) > 2:
+                        self.wait(slice_done.pop(0))
             elif r.kind == "render":
                 img = obj.render(pose_seed=r.rid)
                 render_rays += img.shape[0] * img.shape[1]

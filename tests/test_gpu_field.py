@@ -126,17 +126,21 @@ def test_encoding_cache_gives_the_recomputed_backward(built_lib, enc, d_out, act
         got = c3[:active, :m].permute(1, 0, 2).reshape(m, 2 * active)
         assert rel_err(got.cpu(), ref[:m, :2 * active].cpu()) < 1e-6
     go = torch.randn((n, d_out), device="cuda")
+    cache_fwd = cache.clone()
 
-    def bwd(desc):
+    def bwd(desc, with_x):
         gs = [torch.zeros_like(table32), torch.zeros_like(w0), torch.zeros_like(b0), torch.zeros_like(w1),
-              torch.zeros_like(b1), torch.zeros_like(x)]
+              torch.zeros_like(b1), torch.zeros_like(x) if with_x else None]
         call("sn_field_bwd", n, cnt, x, go, d_out, table, gd, active, C.byref(desc), *gs, st)
-        return gs
+        return [t for t in gs if t is not None]
 
-    for u, v in zip(bwd(cached), bwd(plain)):
-        assert torch.isfinite(u).all()
-        scale = max(float(v.abs().max()), 1e-30)
-        assert float((u - v).abs().max()) <= 1e-5 * scale
+    # with and without grad_x (the table gradient alone is the training call)
+    for with_x in (True, False):
+        cache.copy_(cache_fwd)
+        for u, v in zip(bwd(cached, with_x), bwd(plain, with_x)):
+            assert torch.isfinite(u).all()
+            scale = max(float(v.abs().max()), 1e-30)
+            assert float((u - v).abs().max()) <= 1e-5 * scale, with_x
 
 
 @pytest.mark.parametrize("spread", [1e-3, 3e-2])

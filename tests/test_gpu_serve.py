@@ -162,3 +162,35 @@ def test_serving_loop_small_trace(built_lib):
     o.offload()
     o.onload()
     assert torch.equal(p, o.tr.params)
+
+
+def test_requests_same_alone_and_in_the_mix(built_lib):
+    """A render (its stratified jitter seeded by the request) and an SDF query
+    give bit-identical results alone and interleaved with another object's
+    training slices, as the served policy runs them; training with those
+    requests interleaved matches training alone (atomics order aside)."""
+    from supernormal_gb300.serve import ServedObject, object_specs
+
+    specs = object_specs(2, seed=3, views=(6, 6), res=(96, 96), log2_table=(15, 15))
+    a, b, b_alone = (ServedObject(s, "cuda", batch=128, step_size=1.0 / 96) for s in (specs[0], specs[1], specs[1]))
+    for o in (a, b, b_alone):
+        o.train_iterations(6, False)          # past the occupancy warm-up
+    torch.cuda.synchronize()
+    img_alone = a.render(pose_seed=7).clone()
+    q_alone = a.query(48).clone()
+    la, lb = [], []
+    for _ in range(3):
+        b_alone.train_iterations(4, True)
+        la.append(b_alone.tr.loss_out.clone())
+    for i in range(3):                        # slices of b with a's requests between them
+        b.train_iterations(4, True)
+        lb.append(b.tr.loss_out.clone())
+        if i == 0:
+            img_mix = a.render(pose_seed=7)
+            q_mix = a.query(48)
+    torch.cuda.synchronize()
+    assert torch.equal(img_alone, img_mix)
+    assert torch.equal(q_alone, q_mix)
+    assert torch.equal(a.render(pose_seed=7), img_alone)
+    for x, y in zip(la, lb):
+        assert torch.allclose(x, y, rtol=2e-3, atol=1e-6), (x, y)
