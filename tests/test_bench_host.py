@@ -1,0 +1,44 @@
+"""Host-side helpers of bench.py: stage intervals from graph-replay marks and
+the per-stage algorithmic byte model."""
+import numpy as np
+
+import bench
+
+
+class _Net:
+    def active_levels(self):
+        return 16
+
+
+class _Tr:
+    B, P, n_params = 2048, 9, 1000
+    net = _Net()
+    enc_cache = object()
+
+
+def test_stage_times_from_replay_offsets():
+    step = [("step_begin", 0.0), ("march_end", 0.2), ("cull_end", 0.35), ("field_fwd_begin", 0.4),
+            ("field_fwd_end", 0.8), ("render_end", 1.0), ("field_bwd_begin", 1.0), ("field_bwd_end", 2.1),
+            ("adam_begin", 2.15), ("adam_end", 2.25)]
+    occ = [("occ_begin", 0.0), ("occ_end", 0.4)]
+    t = bench.stage_times(step + step + occ)
+    assert np.isclose(t["march"], 0.4) and np.isclose(t["field_bwd"], 2.2)
+    assert np.isclose(t["expand"], 0.1) and np.isclose(t["occupancy"], 0.4)
+    assert np.isclose(t["adam"], 0.2) and np.isclose(t["render"], 0.4)
+
+
+def test_stage_rooflines_byte_model():
+    stages = {"march": 1.0, "render": 1.0, "adam": 1.0, "field_fwd": 2.0, "field_bwd": 4.0}
+    q = np.array([1000.0, 1000.0])
+    samples = np.array([[500.0, 100.0], [500.0, 100.0]])
+    out = bench.stage_rooflines(stages, q, samples, _Tr(), 1000.0, 2)
+    # 16 B per marched sample + 8 B per ray; 36 B per patch-pixel sample + 16 B per pixel
+    assert np.isclose(out["march"]["bytes_per_step"], 500 * 16 + 2048 * 8)
+    assert np.isclose(out["render"]["bytes_per_step"], 100 * 9 * 36 + 2048 * 9 * 16)
+    assert np.isclose(out["adam"]["bytes_per_step"], 1000 * 32)
+    # with the encoding cache both field kernels move 1,168 B per point at L=16
+    assert np.isclose(out["field_fwd"]["bytes_per_step"], 1000 * 1168)
+    assert np.isclose(out["field_bwd"]["bytes_per_step"], 1000 * 1168)
+    gbs = out["field_bwd"]["achieved_gbs"]
+    assert np.isclose(gbs, 2000 * 1168 / (4.0 / 1e3) / 1e9) and np.isclose(out["field_bwd"]["frac"], gbs / 1000.0)
+    assert bench.stage_rooflines(stages, None, None, _Tr(), 1000.0, 2) is None
