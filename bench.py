@@ -14,9 +14,15 @@ adjoint, field backward, learning-rate schedule and Adam, plus the amortised
 occupancy update.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--precision fp32|mixed] [--eager] [--serve small|full|off] [--quality]
 
-N > 1 runs as independent replicas (one process per GPU via torchrun; the
-path has no exchange step), value = all ranks' rays / max rank time.
+The timed region replays each iteration as a CUDA graph whose captured copies
+carry the stage events (per-stage times and the roofline's kernel durations
+come from those events; --eager times eager launches instead).  The
+end-to-end figure feeds every iteration from pinned host memory through the
+trainer's prefetcher and reads its loss back.  N > 1 runs as independent
+replicas (one process per GPU via torchrun; the path has no exchange step),
+value = all ranks' rays / max rank time.
 --impl reference times the reference's CPU implementation of the path (the
 float64 restatement in oracle/, the reference having no CPU path of its own)
 on host cores over a bounded, proportional sample of the same workload.
