@@ -42,3 +42,23 @@ def test_stage_rooflines_byte_model():
     gbs = out["field_bwd"]["achieved_gbs"]
     assert np.isclose(gbs, 2000 * 1168 / (4.0 / 1e3) / 1e9) and np.isclose(out["field_bwd"]["frac"], gbs / 1000.0)
     assert bench.stage_rooflines(stages, None, None, _Tr(), 1000.0, 2) is None
+
+
+def test_reference_arm_prints_its_line():
+    """bench.py --impl reference (the CPU restatement on host cores) prints one
+    JSON line with the contract's keys."""
+    import json
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0", "--cpu-sample-patches", "2"], capture_output=True, text=True,
+                       timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+    assert line["impl"] == "reference" and line["metric"] == "train_rays_per_s" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    assert line["higher_is_better"] is True and line["vs_baseline"] > 0
