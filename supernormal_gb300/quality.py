@@ -10,8 +10,6 @@ analytic surface.
 """
 from __future__ import annotations
 
-import math
-
 import torch
 
 from . import scenes

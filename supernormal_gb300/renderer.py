@@ -10,7 +10,6 @@ back-propagate through the custom kernels.
 """
 from __future__ import annotations
 
-import ctypes as C
 
 import torch
 from torch import Tensor
