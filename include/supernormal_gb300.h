@@ -69,8 +69,10 @@ int sn_pack_counts(int64_t n, const int32_t* counts, int32_t* packed_info,
  * allocator of their own (a C or FFI binding handed tensors by its framework).
  * Limit: n <= 16,777,216 entries (larger n -> SN_ERR_INVALID with a message).
  * The first call on each device looks up the scratch address with that device
- * current; make it before any stream capture.  The scratch is one per device:
- * calls that overlap on a device (other streams or threads) race. */
+ * current; make it before any stream capture.  The address is kept for the
+ * life of the process: after cudaDeviceReset on a device, do not call this
+ * entry point on that device again.  The scratch is one per device: calls
+ * that overlap on a device (other streams or threads) race. */
 int sn_pack_counts_static(int64_t n, const int32_t* counts, int32_t* packed_info,
                           int32_t* total, void* stream);
 /* counts[r] = number of samples with ray_indices == r (counts zeroed here).
@@ -140,9 +142,15 @@ int sn_occ_points(int64_t n, const int64_t* cells, const float* jitter,
                   int rx, int ry, int rz, const float* roi,
                   int contraction_type, float* x_out, void* stream);
 /* occs[c] = max(occs[c]*ema_decay, occ[i]) for c = cells[i]
- * (NA/nerfacc/grid.py:229-230); duplicate cells resolve to the max. */
+ * (NA/nerfacc/grid.py:229-230).  cells == NULL: cell i for i < n, updated
+ * in place.  Sampled cells may repeat: every candidate is formed from the
+ * cell's value before the update, and a repeated cell ends at the largest
+ * candidate, max(occs[c]*ema_decay, max_i occ[i]) (the reference's index_put
+ * stores an unspecified one of them); workspace holds n floats and is
+ * required when cells != NULL. */
 int sn_occ_ema_update(int64_t n, const int64_t* cells, const float* occ,
-                      float ema_decay, float* occs, void* stream);
+                      float ema_decay, float* occs, float* workspace,
+                      void* stream);
 size_t sn_occ_binarize_workspace_bytes(int64_t n_cells);
 /* binary[c] = occs[c] > min(mean(occs), occ_thre) (NA/nerfacc/grid.py:235-237);
  * mean_out (nullable, device) receives the mean. */
@@ -156,11 +164,13 @@ int sn_occ_points_n(int64_t cap, const int32_t* count, const int64_t* cells,
                     uint64_t seed, const int32_t* stream_counter, int rx,
                     int ry, int rz, const float* roi, int contraction_type,
                     float* x_out, void* stream);
-/* occs[c] = max(occs[c]*ema_decay, sigmoid(-sigmoid_k * sdf[i])): the
- * renderer's occ_eval_fn (models/renderer.py:56-60) fused with the EMA. */
+/* occs[c] = max(occs[c]*ema_decay, sigmoid(-sigmoid_k * sdf[i])) for
+ * i < min(*count, cap): the renderer's occ_eval_fn (models/renderer.py:56-60)
+ * fused with the EMA, repeated cells resolved as in sn_occ_ema_update
+ * (workspace: cap floats, required when cells != NULL). */
 int sn_occ_ema_sdf(int64_t cap, const int32_t* count, const int64_t* cells,
                    const float* sdf, float sigmoid_k, float ema_decay,
-                   float* occs, void* stream);
+                   float* occs, float* workspace, void* stream);
 size_t sn_occ_sample_workspace_bytes(int64_t n_cells);
 /* Post-warm-up cell sampling (NA/nerfacc/grid.py:168-182): n_uniform
  * uniform cells followed by min(n_occupied, n_uniform) occupied cells (all,

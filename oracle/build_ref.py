@@ -1,6 +1,6 @@
 """ORACLE (test infrastructure only): build the reference's own CUDA kernels as a checker.
 
-Compiles nerfacc 0.3.5's ``ray_marching.cu`` and ``render_weight.cu`` from the
+Compiles nerfacc 0.3.5's ``ray_marching.cu``, ``render_weight.cu`` and ``contraction.cu`` from the
 read-only SuperNormal tree (third_parties/nerfacc-0.3.5/nerfacc-0.3.5/nerfacc/cuda/csrc)
 to sm_103a cubins in ``oracle/_ref/``, and records the exported kernel symbol
 names (read with ``nm`` from host objects of the same sources) in
@@ -23,11 +23,12 @@ HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 REF_ROOT = Path(os.environ.get("SUPERNORMAL_REFERENCE", "/root/reference"))
 CSRC = REF_ROOT / "third_parties" / "nerfacc-0.3.5" / "nerfacc-0.3.5" / "nerfacc" / "cuda" / "csrc"
-SOURCES = ["ray_marching.cu", "render_weight.cu"]
+SOURCES = ["ray_marching.cu", "render_weight.cu", "contraction.cu"]
 KERNELS = {
     "ray_marching.cu": ["ray_marching_kernel"],
     "render_weight.cu": ["weight_from_alpha_patch_based_forward_kernel",
                          "weight_from_alpha_patch_based_backward_kernel"],
+    "contraction.cu": ["contract_inv_kernel"],
 }
 
 

@@ -135,3 +135,29 @@ int oracle_march_fill(int64_t n_rays, const float* rays_o, const float* rays_d, 
   }
   return 0;
 }
+
+/* Occupancy-grid query points (NA/nerfacc/grid.py:210-225).  grid_coords is
+ * the "ij" meshgrid of the resolution (grid.py:296-312), so cell
+ * c = (x * ry + y) * rz + z; u = (coords + jitter) / resolution in float32
+ * (an exact int -> float conversion, then one addition and one division),
+ * then unit_to_roi, u * (hi - lo) + lo
+ * (NA/nerfacc/cuda/csrc/include/helpers_contraction.h:23-28), whose multiply
+ * and add nvcc contracts into one FMA.  cells == NULL: cell i.  AABB only. */
+void oracle_occ_points(int64_t n, const int64_t* cells, const float* jitter, int rx, int ry,
+                       int rz, const float* roi, float* x) {
+  const float res[3] = {(float)rx, (float)ry, (float)rz};
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t c = cells ? cells[i] : i;
+    const int64_t co[3] = {c / ((int64_t)ry * rz), (c / rz) % ry, c % rz};
+    for (int d = 0; d < 3; ++d) {
+      const float u = ((float)co[d] + jitter[3 * i + d]) / res[d];
+      x[3 * i + d] = fmaf(u, roi[3 + d] - roi[d], roi[d]);
+    }
+  }
+}
+
+/* unit_to_roi alone (helpers_contraction.h:23-28): x = fma(u, hi - lo, lo). */
+void oracle_unit_to_roi(int64_t n, const float* u, const float* roi, float* x) {
+  for (int64_t i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d) x[3 * i + d] = fmaf(u[3 * i + d], roi[3 + d] - roi[d], roi[d]);
+}

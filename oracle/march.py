@@ -21,6 +21,10 @@ def _load():
         L.oracle_march_count.restype = C.c_int
         L.oracle_march_fill.argtypes = common + [P, P, P, P]
         L.oracle_march_fill.restype = C.c_int
+        L.oracle_occ_points.argtypes = [C.c_int64, P, P, C.c_int, C.c_int, C.c_int, P, P]
+        L.oracle_occ_points.restype = None
+        L.oracle_unit_to_roi.argtypes = [C.c_int64, P, P, P]
+        L.oracle_unit_to_roi.restype = None
         _lib = L
     return _lib
 
@@ -55,3 +59,25 @@ def ray_marching(rays_o, rays_d, t_min, t_max, roi, binary, step_size, jitter=No
     offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int32)
     packed = np.stack([offs, counts], axis=1).astype(np.int32)
     return packed, ridx, ts, te
+
+
+def occ_points(cells, jitter, resolution, roi):
+    """Occupancy query points of grid cells (NA/nerfacc/grid.py:210-225, AABB):
+    float32 (n, 3); cells None = every cell in order."""
+    jitter = np.ascontiguousarray(jitter, dtype=np.float32)
+    n = jitter.shape[0]
+    cells = None if cells is None else np.ascontiguousarray(cells, dtype=np.int64)
+    roi = np.ascontiguousarray(roi, dtype=np.float32)
+    rx, ry, rz = (int(r) for r in resolution)
+    out = np.zeros((n, 3), dtype=np.float32)
+    _load().oracle_occ_points(n, _p(cells), _p(jitter), rx, ry, rz, _p(roi), _p(out))
+    return out
+
+
+def unit_to_roi(u, roi):
+    """[0,1]^3 -> roi (helpers_contraction.h:23-28, AABB contract_inv), float32."""
+    u = np.ascontiguousarray(u, dtype=np.float32).reshape(-1, 3)
+    roi = np.ascontiguousarray(roi, dtype=np.float32)
+    out = np.zeros_like(u)
+    _load().oracle_unit_to_roi(u.shape[0], _p(u), _p(roi), _p(out))
+    return out

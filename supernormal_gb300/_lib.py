@@ -82,11 +82,11 @@ SIGNATURES: dict[str, tuple] = {
     "sn_compact_padded": (_I, [_I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sn_grid_query": (_I, [_I64, _P, _P, _P, _I, _I, _I, _I, _P, _P]),
     "sn_occ_points": (_I, [_I64, _P, _P, _I, _I, _I, _P, _I, _P, _P]),
-    "sn_occ_ema_update": (_I, [_I64, _P, _P, _F, _P, _P]),
+    "sn_occ_ema_update": (_I, [_I64, _P, _P, _F, _P, _P, _P]),
     "sn_occ_binarize_workspace_bytes": (_SZ, [_I64]),
     "sn_occ_binarize": (_I, [_I64, _P, _F, _P, _P, _P, _P]),
     "sn_occ_points_n": (_I, [_I64, _P, _P, C.c_uint64, _P, _I, _I, _I, _P, _I, _P, _P]),
-    "sn_occ_ema_sdf": (_I, [_I64, _P, _P, _P, _F, _F, _P, _P]),
+    "sn_occ_ema_sdf": (_I, [_I64, _P, _P, _P, _F, _F, _P, _P, _P]),
     "sn_occ_sample_workspace_bytes": (_SZ, [_I64]),
     "sn_occ_sample_cells": (_I, [_I64, _P, _I64, C.c_uint64, _P, _P, _P, _P, _P]),
     "sn_near_far_sphere": (_I, [_I64, _P, _P, _I64, _P, _P, _P, C.c_uint64, _P, _P, _P, _P]),

@@ -204,7 +204,10 @@ int ensure_smem_limit(const void* fn, size_t bytes, const char* what) {
 
 // Static scratch of sn_pack_counts_static: tile sums of up to kPackStaticMaxTiles
 // tiles.  Its device address is looked up once per device (with that device
-// current) and cached.
+// current) and cached for the life of the process.  cudaDeviceReset destroys
+// the module that holds the array, and a later call would write through the
+// stale address, so a process that resets a device must not call the entry
+// point on that device again.
 constexpr int64_t kPackStaticMaxTiles = 4096;
 constexpr int64_t kPackStaticMaxEntries = kPackStaticMaxTiles * kScanTile;
 static __device__ __align__(256) int32_t g_pack_scratch[kPackStaticMaxTiles];
@@ -606,20 +609,6 @@ __global__ void occ_points_kernel(int64_t n, const int64_t* __restrict__ cells,
   }
 }
 
-// occs >= 0 always (EMA of sigmoid values), so float order == int bit order.
-__global__ void occ_ema_kernel(int64_t n, const int64_t* __restrict__ cells,
-                               const float* __restrict__ occ, float decay, float* __restrict__ occs) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = cells ? cells[i] : i;
-    const float v = fmaxf(__fmul_rn(occs[c], decay), occ[i]);
-    if (cells)
-      atomicMax(reinterpret_cast<int*>(occs) + c, __float_as_int(fmaxf(v, 0.0f)));
-    else
-      occs[c] = v;
-  }
-}
-
 constexpr int kReduceThreads = 512;
 
 __global__ void __launch_bounds__(kReduceThreads)
@@ -689,22 +678,70 @@ __global__ void occ_points_n_kernel(int64_t cap, const int32_t* __restrict__ cou
   }
 }
 
-// occs[c] = max(occs[c]*decay, sigmoid(-k*sdf)) (renderer occ_eval_fn,
-// models/renderer.py:56-60, fused with NA/nerfacc/grid.py:229-230).
-__global__ void occ_ema_sdf_kernel(int64_t cap, const int32_t* __restrict__ count,
-                                   const int64_t* __restrict__ cells, const float* __restrict__ sdf,
-                                   float k, float decay, float* __restrict__ occs) {
+// EMA update of the occupancy values (NA/nerfacc/grid.py:229-230:
+// occs[indices] = max(occs[indices] * decay, occ)).  With cells == nullptr
+// every cell appears once (the warm-up sweep) and one pass updates it in
+// place.  Sampled cells may repeat, and every candidate must be formed from
+// the cell's value before the update, so the sampled form takes three passes:
+//   (1) vals[i] = max(occs[c] * decay, occ_i)       (reads occs only)
+//   (2) occs[c] = vals[i]                            (a repeated cell keeps any one)
+//   (3) atomicMax(occs[c], vals[i])                  (... then the largest)
+// A repeated cell ends at max(old * decay, max_i occ_i): one of the values
+// the reference's unordered index_put can store, and the one the scatter-max
+// it names as intended gives.  occs >= 0 (an EMA of sigmoid values), so the
+// float order equals the int order of the bit patterns.
+__device__ __forceinline__ float occ_from_sdf(float sdf, float k) {
+  // torch.sigmoid(-sdf * k) (models/renderer.py:56-60): 1 / (1 + exp(sdf * k))
+  return 1.0f / (1.0f + expf(__fmul_rn(sdf, k)));
+}
+
+template <bool kFromSdf>
+__global__ void occ_ema_value_kernel(int64_t cap, const int32_t* __restrict__ count,
+                                     const int64_t* __restrict__ cells, const float* __restrict__ in,
+                                     float k, float decay, float* __restrict__ occs,
+                                     float* __restrict__ vals) {
   const int64_t n = count ? min((int64_t)*count, cap) : cap;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = cells ? cells[i] : i;
-    const float occ = 1.0f / (1.0f + expf(__fmul_rn(sdf[i], k)));
+    const float occ = kFromSdf ? occ_from_sdf(in[i], k) : in[i];
     const float v = fmaxf(__fmul_rn(occs[c], decay), occ);
     if (cells)
-      atomicMax(reinterpret_cast<int*>(occs) + c, __float_as_int(fmaxf(v, 0.0f)));
+      vals[i] = v;
     else
       occs[c] = v;
   }
+}
+
+__global__ void occ_ema_store_kernel(int64_t cap, const int32_t* __restrict__ count,
+                                     const int64_t* __restrict__ cells, const float* __restrict__ vals,
+                                     float* __restrict__ occs) {
+  const int64_t n = count ? min((int64_t)*count, cap) : cap;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    occs[cells[i]] = vals[i];
+}
+
+__global__ void occ_ema_max_kernel(int64_t cap, const int32_t* __restrict__ count,
+                                   const int64_t* __restrict__ cells, const float* __restrict__ vals,
+                                   float* __restrict__ occs) {
+  const int64_t n = count ? min((int64_t)*count, cap) : cap;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    atomicMax(reinterpret_cast<int*>(occs) + cells[i], __float_as_int(fmaxf(vals[i], 0.0f)));
+}
+
+// Launches the one-pass (all cells) or three-pass (sampled cells) update.
+template <bool kFromSdf>
+static int occ_ema_launch(int64_t cap, const int32_t* count, const int64_t* cells, const float* in,
+                          float k, float decay, float* occs, float* vals, cudaStream_t st,
+                          const char* what) {
+  const unsigned g = stride_grid(cap, 256, 8);
+  occ_ema_value_kernel<kFromSdf><<<g, 256, 0, st>>>(cap, count, cells, in, k, decay, occs, vals);
+  if (!cells) return check_launch(what);
+  occ_ema_store_kernel<<<g, 256, 0, st>>>(cap, count, cells, vals, occs);
+  occ_ema_max_kernel<<<g, 256, 0, st>>>(cap, count, cells, vals, occs);
+  return check_launch(what, 3);
 }
 
 __global__ void __launch_bounds__(kScanThreads)
@@ -972,13 +1009,14 @@ int sn_occ_points(int64_t n, const int64_t* cells, const float* jitter, int rx, 
 }
 
 int sn_occ_ema_update(int64_t n, const int64_t* cells, const float* occ, float ema_decay,
-                      float* occs, void* stream) {
+                      float* occs, float* workspace, void* stream) {
   SN_REQUIRE(n >= 0, "occ_ema_update: n < 0");
   SN_REQUIRE(ema_decay >= 0.0f, "occ_ema_update: ema_decay < 0");
+  SN_REQUIRE(occ && occs, "occ_ema_update: null buffer");
+  SN_REQUIRE(!cells || workspace, "occ_ema_update: sampled cells need a workspace of n floats");
   if (n == 0) return SN_OK;
-  occ_ema_kernel<<<stride_grid(n, 256, 8), 256, 0, as_stream(stream)>>>(n, cells, occ, ema_decay,
-                                                                        occs);
-  return check_launch("occ_ema_update");
+  return occ_ema_launch<false>(n, nullptr, cells, occ, 0.0f, ema_decay, occs, workspace,
+                               as_stream(stream), "occ_ema_update");
 }
 
 size_t sn_occ_binarize_workspace_bytes(int64_t n_cells) {
@@ -1018,13 +1056,13 @@ int sn_occ_points_n(int64_t cap, const int32_t* count, const int64_t* cells, uin
 }
 
 int sn_occ_ema_sdf(int64_t cap, const int32_t* count, const int64_t* cells, const float* sdf,
-                   float sigmoid_k, float ema_decay, float* occs, void* stream) {
+                   float sigmoid_k, float ema_decay, float* occs, float* workspace, void* stream) {
   SN_REQUIRE(cap >= 0, "occ_ema_sdf: cap < 0");
   SN_REQUIRE(sdf && occs, "occ_ema_sdf: null buffer");
+  SN_REQUIRE(!cells || workspace, "occ_ema_sdf: sampled cells need a workspace of cap floats");
   if (cap == 0) return SN_OK;
-  occ_ema_sdf_kernel<<<stride_grid(cap, 256, 8), 256, 0, as_stream(stream)>>>(
-      cap, count, cells, sdf, sigmoid_k, ema_decay, occs);
-  return check_launch("occ_ema_sdf");
+  return occ_ema_launch<true>(cap, count, cells, sdf, sigmoid_k, ema_decay, occs, workspace,
+                              as_stream(stream), "occ_ema_sdf");
 }
 
 size_t sn_occ_sample_workspace_bytes(int64_t n_cells) {

@@ -209,20 +209,30 @@ class OccupancyGrid(Grid):
         _need_cuda(self.occs)
         if step < warmup_steps:
             cells = None
-            n = self.num_cells
         else:
             cells = self._sample_uniform_and_occupied_cells(self.num_cells // 4).contiguous()
-            n = cells.numel()
-        rx, ry, rz = (int(r) for r in self.resolution.tolist())
+        n = self.num_cells if cells is None else cells.numel()
         jitter = torch.rand((n, 3), device=self.device)
-        x = torch.empty((n, 3), device=self.device)
-        st = stream_handle()
+        self._update_cells(cells, jitter, occ_eval_fn, occ_thre, ema_decay)
+
+    @torch.no_grad()
+    def _update_cells(self, cells: Optional[Tensor], jitter: Tensor, occ_eval_fn: Callable,
+                      occ_thre: float, ema_decay: float) -> None:
+        """The body of ``_update`` for given cells (None = every cell) and
+        jitter (n, 3) in [0, 1): query points, occupancy, EMA, binarisation."""
+        _need_cuda(self.occs)
         if self._contraction_type == ContractionType.UN_BOUNDED_SPHERE:
             raise NotImplementedError("UN_BOUNDED_SPHERE occupancy updates are not on SuperNormal's path")
+        n = self.num_cells if cells is None else cells.numel()
+        rx, ry, rz = (int(r) for r in self.resolution.tolist())
+        jitter = jitter.contiguous().float()
+        x = torch.empty((n, 3), device=self.device)
+        st = stream_handle()
         call("sn_occ_points", n, cells, jitter, rx, ry, rz, self._roi_aabb.contiguous().float(),
              self._contraction_type.value, x, st)
         occ = occ_eval_fn(x).squeeze(-1).contiguous().float()
-        call("sn_occ_ema_update", n, cells, occ, float(ema_decay), self.occs, st)
+        vals = torch.empty((n,), device=self.device) if cells is not None else None
+        call("sn_occ_ema_update", n, cells, occ, float(ema_decay), self.occs, vals, st)
         ws = _ws(int(call("sn_occ_binarize_workspace_bytes", self.num_cells)), self.device)
         binary = torch.empty_like(self._binary)
         call("sn_occ_binarize", self.num_cells, self.occs, float(occ_thre), binary.view(torch.uint8),

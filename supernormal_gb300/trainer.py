@@ -133,6 +133,7 @@ class FusedTrainer:
         self.occ_count = torch.zeros((1,), dtype=torch.int32, device=dev)
         self.occ_xyz = torch.empty((self.n_cells, 3), device=dev)
         self.occ_sdf = torch.empty((self.n_cells, 1), device=dev)
+        self.occ_vals = torch.empty((2 * (self.n_cells // 4),), device=dev)
         self.occ_ws = torch.empty(int(call("sn_occ_sample_workspace_bytes", self.n_cells)),
                                   dtype=torch.uint8, device=dev)
         self.bin_ws = torch.empty(int(call("sn_occ_binarize_workspace_bytes", self.n_cells)),
@@ -274,7 +275,7 @@ class FusedTrainer:
         call("sn_field_fwd", cap, count, self.occ_xyz, self._table(), self._grid_desc(), active,
              C.byref(self._mlp()), 1, self.occ_sdf, st)
         call("sn_occ_ema_sdf", cap, count, cells, self.occ_sdf, float(c.occ_sigmoid_k),
-             float(c.occ_ema_decay), g.occs, st)
+             float(c.occ_ema_decay), g.occs, self.occ_vals, st)
         call("sn_occ_binarize", self.n_cells, g.occs, float(c.occ_threshold),
              g._binary.view(torch.uint8), None, self.bin_ws, st)
         self._mark("occ_end")

@@ -1,6 +1,6 @@
 """Checker: launch the reference's own CUDA kernels (oracle/_ref cubins) on the GPU.
 
-The cubins are nerfacc 0.3.5's ray_marching.cu / render_weight.cu compiled
+The cubins are nerfacc 0.3.5's ray_marching.cu / render_weight.cu / contraction.cu compiled
 from source for sm_103a by oracle/build_ref.py.  They are loaded with the
 CUDA driver API into the current (torch) context and launched with the
 reference's own launch shapes (ray_marching.cu:227-228,
@@ -101,6 +101,15 @@ class RefKernels:
                      [C.c_uint32(n_patches), C.c_uint32(P), vp(packed), vp(alphas), vp(weights),
                       vp(grad_weights), vp(ga)])
         return ga
+
+    def contract_inv(self, x_unit, roi, ctype=0):
+        """contract_inv_kernel (NA/nerfacc/cuda/csrc/contraction.cu:36-61,89-113)."""
+        n = x_unit.shape[0]
+        out = torch.empty_like(x_unit)
+        vp = lambda t: C.c_void_p(t.data_ptr())
+        self._launch("contract_inv_kernel", ((n + 255) // 256, 1, 1), (256, 1, 1),
+                     [C.c_uint32(n), vp(x_unit), vp(roi), C.c_int(ctype), vp(out)])
+        return out
 
 
 def load():

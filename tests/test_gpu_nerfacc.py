@@ -245,7 +245,9 @@ def test_ray_marching_api_culling_matches_oracle(nf):
     np.testing.assert_array_equal(te.cpu().numpy().ravel(), te_r[vis])
 
 
-def test_occupancy_grid_update_matches_oracle(nf):
+def test_occupancy_grid_every_n_step_properties(nf):
+    """every_n_step end to end with torch's own draws (the bit-exact replay of the
+    reference's draws is tests/test_gpu_occupancy.py)."""
     grid = nf.OccupancyGrid(roi_aabb=[-1.0, -1.0, -1.0, 1.0, 1.0, 1.0], resolution=32).cuda()
     occ_fn = lambda x: torch.sigmoid((0.5 - x.norm(dim=-1, keepdim=True)) * 80.0)
     torch.manual_seed(0)

@@ -1,0 +1,236 @@
+"""GPU parity of the occupancy-grid update (NA/nerfacc/grid.py:196-239).
+
+Replays the draws recorded from nerfacc's own ``OccupancyGrid._update``
+(tests/golden/reference_occupancy.npz) through the C ABI and the drop-in
+``OccupancyGrid``.  Bars: query points bit-exact (also against the
+reference's own ``contract_inv_kernel`` built from source); EMA values
+bit-exact with a repeated cell at its largest candidate (the reference's
+index_put keeps an unspecified one); the fused sigmoid bit-exact against
+torch.sigmoid on the device; the binary grid bit-exact except cells within a
+few ulp of the mean threshold (torch's float32 mean has its own reduction
+order)."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import occupancy as OO
+
+pytestmark = pytest.mark.gpu
+FIX = np.load(Path(__file__).parent / "golden" / "reference_occupancy.npz")
+STEPS = [str(s) for s in FIX["steps"]]
+
+
+@pytest.fixture(scope="module")
+def nf(built_lib):
+    from supernormal_gb300 import nerfacc
+
+    return nerfacc
+
+
+def D(a, dtype=None):
+    t = torch.as_tensor(np.asarray(a), device="cuda")
+    return t.to(dtype) if dtype is not None else t
+
+
+def _call(*a):
+    from supernormal_gb300._lib import call, stream_handle
+
+    return call(*a, stream_handle())
+
+
+def _near_threshold(occs, thr):
+    return np.abs(occs - thr) <= 4 * np.spacing(np.float32(thr))
+
+
+@pytest.mark.parametrize("tag", STEPS)
+def test_query_points_bit_exact(nf, tag):
+    f = lambda k: FIX[f"{tag}/{k}"]
+    cells = None if int(f("step")) < 256 else D(f("cells"), torch.int64)
+    n = f("jitter").shape[0]
+    x = torch.empty((n, 3), device="cuda")
+    _call("sn_occ_points", n, cells, D(f("jitter")), 16, 16, 16, D(FIX["roi"]), 0, x)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(x.cpu().numpy(), f("x"))
+
+
+def test_query_points_vs_reference_kernel(nf):
+    from tests import refkernels
+
+    ref = refkernels.load()
+    if isinstance(ref, Exception):
+        pytest.skip(f"reference checker kernels unavailable: {ref}")
+    if "contract_inv_kernel" not in ref.funcs:
+        pytest.skip("reference contract_inv_kernel not built")
+    f = lambda k: FIX[f"sampled/{k}"]
+    cells = D(f("cells"), torch.int64)
+    jitter = D(f("jitter"))
+    res = torch.tensor([16, 16, 16], dtype=torch.int32, device="cuda")
+    # grid.py:210-212 on the device, then the reference's own contract_inv kernel
+    coords = torch.stack(torch.meshgrid([torch.arange(16, device="cuda")] * 3, indexing="ij"),
+                         -1).reshape(-1, 3)[cells]
+    x_unit = ((coords + jitter) / res).contiguous()
+    want = ref.contract_inv(x_unit, D(FIX["roi"]))
+    got = torch.empty_like(want)
+    _call("sn_occ_points", cells.numel(), cells, jitter, 16, 16, 16, D(FIX["roi"]), 0, got)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(x_unit.cpu().numpy(), f("x_unit"))
+    np.testing.assert_array_equal(got.cpu().numpy(), want.cpu().numpy())
+
+
+@pytest.mark.parametrize("tag", STEPS)
+def test_ema_update_and_binarize(nf, tag):
+    f = lambda k: FIX[f"{tag}/{k}"]
+    cells_np = None if int(f("step")) < 256 else f("cells")
+    want, repeated = OO.ema_update(f("occs_before"), cells_np, f("occ"), 0.95)
+    for twice in range(2):   # the workspace keeps the previous call's values: no effect
+        occs = D(f("occs_before")).clone()
+        n = f("occ").size
+        ws = torch.full((n,), float("nan"), device="cuda") if cells_np is not None else None
+        _call("sn_occ_ema_update", n, None if cells_np is None else D(cells_np, torch.int64), D(f("occ")),
+              0.95, occs, ws)
+        got = occs.cpu().numpy()
+        np.testing.assert_array_equal(got, want)
+    ref = f("occs_after")
+    for c, cand in repeated.items():
+        assert got[c] == cand.max() and ref[c] in cand
+    from supernormal_gb300._lib import call
+
+    wsb = torch.empty(int(call("sn_occ_binarize_workspace_bytes", 4096)), dtype=torch.uint8, device="cuda")
+    binary = torch.empty(4096, dtype=torch.uint8, device="cuda")
+    mean = torch.empty(1, device="cuda")
+    _call("sn_occ_binarize", 4096, D(ref), float(f("occ_thre")), binary, mean, wsb)
+    b_want, thr = OO.binarize(ref, float(f("occ_thre")))
+    near = _near_threshold(ref, thr)
+    np.testing.assert_array_equal(binary.cpu().numpy().astype(bool)[~near], b_want.reshape(-1)[~near])
+    np.testing.assert_array_equal(binary.cpu().numpy().astype(bool)[~near],
+                                  f("binary_after").reshape(-1)[~near])
+    assert abs(mean.item() - float(ref.astype(np.float64).mean())) <= 1e-6 * max(1.0, abs(ref.mean()))
+
+
+def test_sampled_cells_decay(nf):
+    """A sampled cell whose occupancy the field no longer has decays by 0.95."""
+    f = lambda k: FIX[f"sampled/{k}"]
+    occs = D(f("occs_before")).clone()
+    cells = D(f("cells"), torch.int64)
+    ws = torch.empty(cells.numel(), device="cuda")
+    _call("sn_occ_ema_update", cells.numel(), cells, D(f("occ")), 0.95, occs, ws)
+    hit = np.intersect1d(FIX["planted"], f("cells"))
+    got = occs.cpu().numpy()[hit]
+    before = f("occs_before")[hit]
+    assert hit.size > 10 and (got < before).all()
+    np.testing.assert_array_equal(got, f("occs_after")[hit])
+
+
+@pytest.mark.parametrize("with_count", [False, True])
+def test_ema_sdf_matches_torch_sigmoid(nf, with_count):
+    """The fused occ_eval_fn + EMA against torch.sigmoid(-sdf * 80) (models/renderer.py:56-60)
+    on the device, with repeated sampled cells and a device count below the capacity."""
+    g = torch.Generator(device="cuda").manual_seed(3)
+    n_cells, cap = 8192, 6000
+    occs0 = torch.rand(n_cells, device="cuda", generator=g)
+    cells = torch.randint(0, n_cells, (cap,), device="cuda", generator=g)   # many repeats
+    sdf = (torch.rand(cap, device="cuda", generator=g) - 0.5) * 0.2
+    n = 4321 if with_count else cap
+    count = torch.tensor([n], dtype=torch.int32, device="cuda") if with_count else None
+    occs = occs0.clone()
+    ws = torch.empty(cap, device="cuda")
+    _call("sn_occ_ema_sdf", cap, count, cells, sdf, 80.0, 0.95, occs, ws)
+    occ_ref = torch.sigmoid(-sdf[:n] * 80)          # the reference's own op, on the same device
+    want, _ = OO.ema_update(occs0.cpu().numpy(), cells[:n].cpu().numpy(), occ_ref.cpu().numpy(), 0.95)
+    np.testing.assert_array_equal(occs.cpu().numpy(), want)
+    # every cell: the warm-up sweep form (cells = NULL)
+    occs = occs0.clone()
+    sdf_all = (torch.rand(n_cells, device="cuda", generator=g) - 0.5) * 0.2
+    _call("sn_occ_ema_sdf", n_cells, None, None, sdf_all, 80.0, 0.95, occs, None)
+    want = torch.maximum(occs0 * 0.95, torch.sigmoid(-sdf_all * 80))
+    np.testing.assert_array_equal(occs.cpu().numpy(), want.cpu().numpy())
+
+
+@pytest.mark.parametrize("tag", STEPS)
+def test_occupancy_grid_api_replays_reference(nf, tag):
+    """The drop-in OccupancyGrid, given the reference's recorded cells and jitter."""
+    f = lambda k: FIX[f"{tag}/{k}"]
+    grid = nf.OccupancyGrid(roi_aabb=[-1.0, -1.0, -1.0, 1.0, 1.0, 1.0], resolution=16).cuda()
+    grid.occs.copy_(D(f("occs_before")))
+    grid._binary = D(f("binary_before"))
+    seen = {}
+
+    def occ_eval_fn(x):
+        seen["x"] = x.clone()
+        return D(f("occ"))[:, None]
+
+    cells = None if int(f("step")) < 256 else D(f("cells"), torch.int64)
+    grid._update_cells(cells, D(f("jitter")), occ_eval_fn, float(f("occ_thre")), 0.95)
+    np.testing.assert_array_equal(seen["x"].cpu().numpy(), f("x"))
+    want, _ = OO.ema_update(f("occs_before"), None if cells is None else f("cells"), f("occ"), 0.95)
+    np.testing.assert_array_equal(grid.occs.cpu().numpy(), want)
+    _, thr = OO.binarize(want, float(f("occ_thre")))
+    near = _near_threshold(want, thr)
+    got_b = grid.binary.cpu().numpy().reshape(-1)
+    np.testing.assert_array_equal(got_b[~near], f("binary_after").reshape(-1)[~near])
+
+
+def test_sample_cells(nf):
+    """Post-warm-up draws (grid.py:181-194): n uniform cells, then every
+    occupied cell in order when there are at most n, else n of them."""
+    from supernormal_gb300._lib import call
+
+    for frac in (0.05, 0.6):
+        g = torch.Generator(device="cuda").manual_seed(1)
+        n_cells = 32 ** 3
+        binary = (torch.rand(n_cells, device="cuda", generator=g) < frac).to(torch.uint8)
+        n_u = n_cells // 4
+        cells = torch.full((2 * n_u,), -1, dtype=torch.int64, device="cuda")
+        count = torch.zeros(1, dtype=torch.int32, device="cuda")
+        ws = torch.empty(int(call("sn_occ_sample_workspace_bytes", n_cells)), dtype=torch.uint8, device="cuda")
+        it = torch.zeros(1, dtype=torch.int32, device="cuda")
+        _call("sn_occ_sample_cells", n_cells, binary, n_u, 7, it, cells, count, ws)
+        occ = OO.occupied_cells(binary.cpu().numpy())
+        c = cells.cpu().numpy()
+        assert int(count.item()) == n_u + min(len(occ), n_u)
+        assert ((c[:n_u] >= 0) & (c[:n_u] < n_cells)).all()
+        if len(occ) <= n_u:
+            np.testing.assert_array_equal(c[n_u:n_u + len(occ)], occ)
+        else:
+            assert np.isin(c[n_u:], occ).all()
+
+
+def test_trainer_occupancy_update_matches_oracle(nf):
+    """FusedTrainer's device-side update (sampling, query points, field, fused
+    sigmoid + EMA, binarisation) after the warm-up, checked per sampled cell."""
+    from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
+    from supernormal_gb300.trainer import FusedTrainer, TrainConfig
+
+    torch.manual_seed(0)
+    enc = dict(otype="HashGrid", n_levels=8, n_features_per_level=2, log2_hashmap_size=15,
+               base_resolution=16, per_level_scale=1.447)
+    net = SDFNetwork(3, 1, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=enc, input_concat=True).cuda()
+    var = SingleVarianceNetwork(0.3).cuda()
+    cfg = TrainConfig(batch_size=16, step_size=1.0 / 64, occ_update_freq=8, occ_threshold=0.1)
+    tr = FusedTrainer(net, var, cfg, device="cuda")
+    tr.occupancy_update(0)                       # warm-up sweep from the initial field
+    g = tr.grid
+    # plant stale occupancy far outside the initial surface (|x| - 0.5)
+    far_cells = torch.nonzero(g.occs < 1e-4)[:, 0]
+    g.occs[far_cells[::7]] = 0.8
+    from supernormal_gb300._lib import call
+
+    call("sn_occ_binarize", tr.n_cells, g.occs, 0.1, g._binary.view(torch.uint8), None, tr.bin_ws,
+         torch.cuda.current_stream().cuda_stream)
+    before = g.occs.cpu().numpy().copy()
+    tr.occupancy_update(cfg.occ_warmup_steps)    # sampled regime
+    torch.cuda.synchronize()
+    n = int(tr.occ_count.item())
+    cells = tr.occ_cells[:n].cpu().numpy()
+    sdf = tr.occ_sdf[:n, 0]
+    occ = torch.sigmoid(-sdf * 80).cpu().numpy()
+    want, repeated = OO.ema_update(before, cells, occ, cfg.occ_ema_decay)
+    got = g.occs.cpu().numpy()
+    np.testing.assert_array_equal(got, want)
+    planted_hit = np.intersect1d(far_cells[::7].cpu().numpy(), cells)
+    assert planted_hit.size > 0 and (got[planted_hit] < before[planted_hit]).all()
+    b_want, thr = OO.binarize(want, cfg.occ_threshold)
+    near = _near_threshold(want, thr)
+    np.testing.assert_array_equal(g.binary.cpu().numpy().reshape(-1)[~near], b_want.reshape(-1)[~near])
