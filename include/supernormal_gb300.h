@@ -114,14 +114,18 @@ int sn_march_fill(int64_t n_rays, const float* rays_o, const float* rays_d,
 /* Single-pass marcher: ray i writes its samples to slots
  * [i*slot_stride, i*slot_stride + num_steps[i]) (num_steps written too;
  * SN_STATUS_CAPACITY if a ray has more than slot_stride samples).  Same
- * samples as count + fill; used with sn_pack_counts + sn_compact_padded. */
+ * samples as count + fill; used with sn_pack_counts + sn_compact_padded.
+ * step_size_dev (nullable) holds the step size in device memory and then
+ * replaces step_size, so a captured launch follows a step-size schedule
+ * (sn_step_size_schedule). */
 int sn_march_padded(int64_t n_rays, const float* rays_o, const float* rays_d,
                     const float* t_min, const float* t_max, const float* jitter,
                     const float* roi, const uint8_t* grid_binary, int rx, int ry,
                     int rz, int contraction_type, float step_size,
-                    float cone_angle, int64_t max_iters, int64_t slot_stride,
-                    int32_t* num_steps, int64_t* ray_indices, float* t_starts,
-                    float* t_ends, int32_t* status, void* stream);
+                    const float* step_size_dev, float cone_angle,
+                    int64_t max_iters, int64_t slot_stride, int32_t* num_steps,
+                    int64_t* ray_indices, float* t_starts, float* t_ends,
+                    int32_t* status, void* stream);
 /* Copies padded per-ray samples to their packed_info offsets. */
 int sn_compact_padded(int64_t n_rays, int64_t slot_stride,
                       const int32_t* packed_info, const int64_t* ray_indices_in,
@@ -464,11 +468,55 @@ int sn_scale_count(const int32_t* in, int32_t mul, int32_t add, int32_t* out,
 int sn_mask_prep(int64_t n, const float* mask_in, float* mask_out,
                  float* mask_sum, void* stream);
 
+/* ---- synthetic analytic scenes (benchmark and test data) ------------------- */
+/* No reference counterpart: the reference trains on captured normal maps
+ * (models/dataset_loader.py); the benchmarks here render multi-view normal
+ * maps and masks of analytic SDF scenes instead.  A scene is the union (min)
+ * of up to SN_SCENE_MAX_PRIMS primitives minus a displacement
+ * disp_amp * sin(f x) sin(f y) sin(f z); a torus lies around z with ring
+ * radius size[0], tube radius size[1] and a radial displacement
+ * amp * sin(freq theta) sin(freq phi); a box has half extents size[];
+ * lipschitz bounds the SDF's slope (sphere-tracing step sdf / lipschitz * 0.9). */
+#define SN_SCENE_MAX_PRIMS 4
+enum { SN_PRIM_SPHERE = 0, SN_PRIM_TORUS = 1, SN_PRIM_BOX = 2 };
+typedef struct {
+  int32_t kind;
+  int32_t reserved;
+  double center[3];
+  double size[3];
+  double amp, freq;
+} sn_prim;
+typedef struct {
+  int32_t n_prims;
+  int32_t reserved;
+  sn_prim prims[SN_SCENE_MAX_PRIMS];
+  double disp_amp, disp_freq;
+  double lipschitz;
+} sn_scene_desc;
+/* Ground-truth normal maps and masks of n_views pinhole views: pixel (x, y)
+ * of view v looks along R_v normalize(K_v^-1 [x, y, 1]) from t_v (kinv
+ * (n_views, 3, 3) and pose (n_views, 3, 4) = [R | t], double), is clipped to
+ * the unit sphere and sphere-traced in double (at most max_iters steps, hit
+ * when |sdf| < eps); normals (n_views, H, W, 3) get the unit SDF gradient at
+ * the hit (zero on a miss), masks (n_views, H, W) 1 or 0. */
+int sn_scene_render_gt(const sn_scene_desc* scene, int n_views, int H, int W,
+                       const double* kinv, const double* pose, int max_iters,
+                       double eps, float* normals, float* masks, void* stream);
+/* out[i] = the scene's SDF at x[i] (n, 3) (evaluated in double). */
+int sn_scene_sdf(const sn_scene_desc* scene, int64_t n, const float* x,
+                 float* out, void* stream);
+
 /* ---- optimiser (exp_runner.py:97, 205-210, 270-279) ------------------------ */
 /* Reads iteration k from *iter, writes lr(k) of the warm-up + cosine schedule
  * and adam_step = k + 1, then stores k + 1 in *iter. */
 int sn_lr_schedule(int32_t* iter, float* lr, int32_t* adam_step, float base_lr,
                    int warm_up_end, int end_iter, float alpha, void* stream);
+/* Marching step of iteration *iter on the log schedule of exp_runner.py:81-83,
+ * 149 (renderer.sampling_step_size = 10 ** (log10(start) - slop * iter), slop =
+ * (log10(start) - log10(end)) / end_iter), formed in double and rounded once
+ * to float into *step; *iter is read, not changed. */
+int sn_step_size_schedule(const int32_t* iter, double start_step, double end_step,
+                          int end_iter, float* step, void* stream);
 /* torch.optim.Adam step over a flat buffer (16-byte aligned).  lr_dev /
  * step_dev (nullable) override lr / step; zero_grad clears grad after use;
  * param_half (nullable) receives an fp16 copy of the updated parameters. */

@@ -65,18 +65,19 @@ def corner_indices(x32: np.ndarray, level: int, offsets, res, scales):
 
 
 def encode(x: torch.Tensor, table: torch.Tensor, geom, n_features=2, active_levels=None,
-           cache: dict | None = None):
-    """(N, L*F) float64 encoding, differentiable w.r.t. table and x.  ``cache``
+           cache: dict | None = None, dtype=torch.float64):
+    """(N, L*F) encoding in ``dtype`` (float64 for the parity checks; float32
+    for a timed host baseline), differentiable w.r.t. table and x.  ``cache``
     (optional dict) keeps the per-level cell data of a fixed x across calls."""
     offsets, res, scales = geom
     L = len(res)
     active = L if active_levels is None else active_levels
     x32 = x.detach().cpu().numpy().astype(np.float32) if cache is None or not cache else None
-    xd = x.double()
+    xd = x.to(dtype)
     outs = []
     for l in range(L):
         if l >= active:
-            outs.append(torch.zeros((x.shape[0], n_features), dtype=torch.float64))
+            outs.append(torch.zeros((x.shape[0], n_features), dtype=dtype))
             continue
         if cache is not None and l in cache:
             cell, frac32, idx = cache[l]
@@ -89,8 +90,8 @@ def encode(x: torch.Tensor, table: torch.Tensor, geom, n_features=2, active_leve
         # value: the float32 fraction tcnn forms (pos rounded to float32 before
         # floor/subtract); derivative: d frac / dx = scale
         xs = xd * float(scales[l])
-        frac = torch.from_numpy(frac32.astype(np.float64)) + (xs - xs.detach())
-        feat = table.double().reshape(-1, n_features)[torch.from_numpy(idx)]      # (N, 8, F)
+        frac = torch.from_numpy(frac32).to(dtype) + (xs - xs.detach())
+        feat = table.to(dtype).reshape(-1, n_features)[torch.from_numpy(idx)]      # (N, 8, F)
         acc = 0.0
         for k in range(8):
             w = 1.0
@@ -110,13 +111,13 @@ def softplus(h, beta=100.0, threshold=20.0):
 
 
 def sdf_network(x, table, v0, g0, b0, v1, g1, b1, geom, active_levels=None, out_cols=None,
-                cache=None):
-    """SDFNetwork.forward with n_layers=1, input_concat=True (float64)."""
-    enc = encode(x, table, geom, active_levels=active_levels, cache=cache)
-    inp = torch.cat([x.double(), enc], dim=1)
-    h = inp @ weight_norm(v0.double(), g0.double()).T + b0.double()
+                cache=None, dtype=torch.float64):
+    """SDFNetwork.forward with n_layers=1, input_concat=True (in ``dtype``)."""
+    enc = encode(x, table, geom, active_levels=active_levels, cache=cache, dtype=dtype)
+    inp = torch.cat([x.to(dtype), enc], dim=1)
+    h = inp @ weight_norm(v0.to(dtype), g0.to(dtype)).T + b0.to(dtype)
     a = softplus(h)
-    y = a @ weight_norm(v1.double(), g1.double()).T + b1.double()
+    y = a @ weight_norm(v1.to(dtype), g1.to(dtype)).T + b1.to(dtype)
     return y if out_cols is None else y[:, :out_cols]
 
 

@@ -1,8 +1,9 @@
-"""ORACLE (test infrastructure only): float64 restatement of the patch renderer and losses.
+"""ORACLE (test infrastructure only): restatement of the patch renderer and losses.
 
 Follows models/renderer.py:80-122 (culling alpha), :142-267 (patch expansion,
 NeuS alpha, patch weights, dfd normals, accumulation) and exp_runner.py:169-203
-(losses) with torch float64 CPU tensors, so autograd gives the reference
+(losses) with torch CPU tensors, float64 for the parity checks (``dtype``
+float32 for a timed host baseline), so autograd gives the reference
 gradients.  The field is passed in as a callable (N,3) -> (N,1).
 """
 from __future__ import annotations
@@ -14,8 +15,8 @@ import torch.nn.functional as F
 from . import nerfacc_ref
 
 
-def inv_s_of(variance):
-    return torch.exp(variance.double() * 10.0).clip(1e-6, 1e6)
+def inv_s_of(variance, dtype=torch.float64):
+    return torch.exp(variance.to(dtype) * 10.0).clip(1e-6, 1e6)
 
 
 def neus_alpha(s0, s1, inv_s):
@@ -35,13 +36,13 @@ def diff_mask_of(ts, te):
     return (te - nxt) != 0
 
 
-def center_alpha(field, ridx, ts, te, rays_o_c, rays_d_c, variance):
-    """alpha_fn_patch_center (models/renderer.py:80-122), float64."""
+def center_alpha(field, ridx, ts, te, rays_o_c, rays_d_c, variance, dtype=torch.float64):
+    """alpha_fn_patch_center (models/renderer.py:80-122)."""
     ridx = np.asarray(ridx)
-    o = torch.as_tensor(np.asarray(rays_o_c, np.float32)[ridx]).double()
-    d = torch.as_tensor(np.asarray(rays_d_c, np.float32)[ridx]).double()
-    tsd = torch.as_tensor(np.asarray(ts, np.float32)).double().reshape(-1, 1)
-    ted = torch.as_tensor(np.asarray(te, np.float32)).double().reshape(-1, 1)
+    o = torch.as_tensor(np.asarray(rays_o_c, np.float32)[ridx]).to(dtype)
+    d = torch.as_tensor(np.asarray(rays_d_c, np.float32)[ridx]).to(dtype)
+    tsd = torch.as_tensor(np.asarray(ts, np.float32)).to(dtype).reshape(-1, 1)
+    ted = torch.as_tensor(np.asarray(te, np.float32)).to(dtype).reshape(-1, 1)
     diff = torch.as_tensor(diff_mask_of(ts, te))
     ps, pe = o + d * tsd, o + d * ted
     sdf = field(torch.cat([ps, pe[diff]], 0))
@@ -49,20 +50,22 @@ def center_alpha(field, ridx, ts, te, rays_o_c, rays_d_c, variance):
     s0 = sdf[:n]
     s1 = torch.cat([s0[1:], s0[-1:]], 0).clone()
     s1[diff] = sdf[n:]
-    return neus_alpha(s0, s1, inv_s_of(variance)).reshape(-1)
+    return neus_alpha(s0, s1, inv_s_of(variance, dtype)).reshape(-1)
 
 
-def cull(field, packed, ridx, ts, te, rays_o_c, rays_d_c, variance, early_stop_eps=1e-8):
+def cull(field, packed, ridx, ts, te, rays_o_c, rays_d_c, variance, early_stop_eps=1e-8,
+         dtype=torch.float64):
     """Visibility culling inside nerfacc.ray_marching (NA/nerfacc/ray_marching.py:193-220)."""
     with torch.no_grad():
-        alpha = center_alpha(field, ridx, ts, te, rays_o_c, rays_d_c, variance).numpy()
+        alpha = center_alpha(field, ridx, ts, te, rays_o_c, rays_d_c, variance, dtype).numpy()
     vis = nerfacc_ref.visibility(alpha, packed, early_stop_eps)
     return vis, alpha
 
 
 def patch_forward(field, patch_idx, ts, te, rays_o_all, rays_d_all, plane_n, vinv, variance,
-                  points=None, gradient_method="dfd", ext_gradients=None):
-    """models/renderer.py:142-267 for gradient_method='dfd' (float64).
+                  points=None, gradient_method="dfd", ext_gradients=None, dtype=torch.float64):
+    """models/renderer.py:142-267 for gradient_method='dfd' (float64 unless
+    ``dtype`` says otherwise).
 
     patch_idx/ts/te are the culled centre samples; rays_* are (B, H, W, 3).
     ``points`` (optional, ((S + E) * H * W, 3) float32) are the field query
@@ -70,14 +73,14 @@ def patch_forward(field, patch_idx, ts, te, rays_o_all, rays_d_all, plane_n, vin
     float32); the field is then evaluated exactly there, so hash-grid cell
     choices match and only arithmetic precision differs."""
     pidx = torch.as_tensor(np.asarray(patch_idx, np.int64))
-    ro = torch.as_tensor(np.asarray(rays_o_all, np.float32)).double()
-    rd = torch.as_tensor(np.asarray(rays_d_all, np.float32)).double()
-    pn = torch.as_tensor(np.asarray(plane_n, np.float32)).double()
-    vi = torch.as_tensor(np.asarray(vinv, np.float32)).double()
+    ro = torch.as_tensor(np.asarray(rays_o_all, np.float32)).to(dtype)
+    rd = torch.as_tensor(np.asarray(rays_d_all, np.float32)).to(dtype)
+    pn = torch.as_tensor(np.asarray(plane_n, np.float32)).to(dtype)
+    vi = torch.as_tensor(np.asarray(vinv, np.float32)).to(dtype)
     B, H, W, _ = ro.shape
     S = pidx.shape[0]
-    tsc = torch.as_tensor(np.asarray(ts, np.float32)).double().reshape(S, 1, 1, 1)
-    tec = torch.as_tensor(np.asarray(te, np.float32)).double().reshape(S, 1, 1, 1)
+    tsc = torch.as_tensor(np.asarray(ts, np.float32)).to(dtype).reshape(S, 1, 1, 1)
+    tec = torch.as_tensor(np.asarray(te, np.float32)).to(dtype).reshape(S, 1, 1, 1)
     dc = rd[:, H // 2, W // 2]
     dot_c = (dc * pn).sum(-1, keepdim=True)[pidx][:, None, None, :]
     dot_p = (rd * pn[:, None, None, :]).sum(-1, keepdim=True)[pidx]
@@ -87,7 +90,7 @@ def patch_forward(field, patch_idx, ts, te, rays_o_all, rays_d_all, plane_n, vin
     ps = ro[pidx] + rd[pidx] * t_s
     pe = ro[pidx] + rd[pidx] * t_e
     pts = torch.cat([ps, pe[diff]], 0)
-    q = pts.reshape(-1, 3) if points is None else torch.as_tensor(np.asarray(points, np.float32)).double()
+    q = pts.reshape(-1, 3) if points is None else torch.as_tensor(np.asarray(points, np.float32)).to(dtype)
     assert q.shape[0] == pts.reshape(-1, 3).shape[0], "points do not match the sample layout"
     sdf = field(q).reshape(*pts.shape[:-1], 1)
     s0 = sdf[:S]
@@ -95,7 +98,7 @@ def patch_forward(field, patch_idx, ts, te, rays_o_all, rays_d_all, plane_n, vin
     s1 = torch.where(diff[:, None, None, None], torch.zeros_like(s1), s1)
     s1 = s1.clone()
     s1[diff] = sdf[S:]
-    inv_s = inv_s_of(variance)
+    inv_s = inv_s_of(variance, dtype)
     alpha = neus_alpha(s0, s1, inv_s)                                 # (S, H, W, 1)
     # patch weights: w = alpha * prod_{j<i}(1 - alpha_j) within each patch
     a = alpha.reshape(S, H * W)
@@ -133,8 +136,8 @@ def patch_forward(field, patch_idx, ts, te, rays_o_all, rays_d_all, plane_n, vin
         (g_ad,) = torch.autograd.grad(s_ad.sum(), xs, create_graph=True)
         gradients = g_ad.reshape(S, H, W, 3)
     # accumulation (models/renderer.py:263-267)
-    wsum = torch.zeros((B, H * W, 1), dtype=torch.float64).index_add(0, pidx, weights.reshape(S, H * W, 1))
-    comp = torch.zeros((B, H * W, 3), dtype=torch.float64).index_add(
+    wsum = torch.zeros((B, H * W, 1), dtype=dtype).index_add(0, pidx, weights.reshape(S, H * W, 1))
+    comp = torch.zeros((B, H * W, 3), dtype=dtype).index_add(
         0, pidx, (weights * gradients).reshape(S, H * W, 3))
     return dict(alpha=alpha, weights=weights, gradients=gradients,
                 weight_sum=wsum.reshape(B, H, W, 1), comp_normal=comp.reshape(B, H, W, 3),

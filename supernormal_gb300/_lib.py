@@ -60,8 +60,22 @@ class MlpDesc(C.Structure):
     ]
 
 
+SN_SCENE_MAX_PRIMS = 4
+SN_PRIM_SPHERE, SN_PRIM_TORUS, SN_PRIM_BOX = 0, 1, 2
+
+
+class Prim(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("center", C.c_double * 3),
+                ("size", C.c_double * 3), ("amp", C.c_double), ("freq", C.c_double)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("n_prims", C.c_int32), ("reserved", C.c_int32), ("prims", Prim * SN_SCENE_MAX_PRIMS),
+                ("disp_amp", C.c_double), ("disp_freq", C.c_double), ("lipschitz", C.c_double)]
+
+
 _P, _I64, _I, _F, _SZ = C.c_void_p, C.c_int64, C.c_int, C.c_float, C.c_size_t
-_GD, _MD = C.POINTER(GridDesc), C.POINTER(MlpDesc)
+_GD, _MD, _SD = C.POINTER(GridDesc), C.POINTER(MlpDesc), C.POINTER(SceneDesc)
 
 # name -> (restype, argtypes); mirrors include/supernormal_gb300.h
 SIGNATURES: dict[str, tuple] = {
@@ -77,7 +91,7 @@ SIGNATURES: dict[str, tuple] = {
     "sn_march_count": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _F, _F, _I64, _P, _P, _P]),
     "sn_march_fill": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _F, _F, _I64, _P, _I64,
                            _P, _P, _P, _P, _P]),
-    "sn_march_padded": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _F, _F, _I64, _I64,
+    "sn_march_padded": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _F, _P, _F, _I64, _I64,
                              _P, _P, _P, _P, _P, _P]),
     "sn_compact_padded": (_I, [_I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sn_grid_query": (_I, [_I64, _P, _P, _P, _I, _I, _I, _I, _P, _P]),
@@ -121,7 +135,10 @@ SIGNATURES: dict[str, tuple] = {
     "sn_scale_count": (_I, [_P, C.c_int32, C.c_int32, _P, _P]),
     "sn_gen_patches": (_I, [_I64, _I, _I, _P, _P, _P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sn_mask_prep": (_I, [_I64, _P, _P, _P, _P]),
+    "sn_scene_render_gt": (_I, [_SD, _I, _I, _I, _P, _P, _I, C.c_double, _P, _P, _P]),
+    "sn_scene_sdf": (_I, [_SD, _I64, _P, _P, _P]),
     "sn_lr_schedule": (_I, [_P, _P, _P, _F, _I, _I, _F, _P]),
+    "sn_step_size_schedule": (_I, [_P, C.c_double, C.c_double, _I, _P, _P]),
     "sn_adam_step": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _F, _I, _F, _F, _F, _I, _P]),
 }
 

@@ -28,6 +28,16 @@ __global__ void lr_schedule_kernel(int32_t* __restrict__ iter, float* __restrict
   *iter = k + 1;
 }
 
+// Marching step of iteration *iter on the log schedule of exp_runner.py:81-83,149:
+// 10 ** (log10(start) - (log10(start) - log10(end)) / end_iter * iter) in double,
+// rounded once to float (the reference passes the numpy float64 to the marcher's
+// float argument).
+__global__ void step_size_schedule_kernel(const int32_t* __restrict__ iter, double start, double end,
+                                          int end_iter, float* __restrict__ step) {
+  const double slop = (log10(start) - log10(end)) / (double)end_iter;
+  *step = (float)pow(10.0, log10(start) - slop * (double)*iter);
+}
+
 struct AdamArgs {
   int64_t n;
   float* p;
@@ -113,6 +123,14 @@ int sn_lr_schedule(int32_t* iter, float* lr, int32_t* adam_step, float base_lr, 
   lr_schedule_kernel<<<1, 1, 0, as_stream(stream)>>>(iter, lr, adam_step, base_lr, warm_up_end,
                                                      end_iter, alpha);
   return check_launch("lr_schedule");
+}
+
+int sn_step_size_schedule(const int32_t* iter, double start_step, double end_step, int end_iter,
+                          float* step, void* stream) {
+  SN_REQUIRE(iter && step, "step_size_schedule: null buffer");
+  SN_REQUIRE(start_step > 0.0 && end_step > 0.0 && end_iter > 0, "step_size_schedule: bad schedule");
+  step_size_schedule_kernel<<<1, 1, 0, as_stream(stream)>>>(iter, start_step, end_step, end_iter, step);
+  return check_launch("step_size_schedule");
 }
 
 int sn_adam_step(int64_t n, float* param, float* grad, float* exp_avg, float* exp_avg_sq,

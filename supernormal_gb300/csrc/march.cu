@@ -374,6 +374,7 @@ struct MarchArgs {
   const float* jitter;
   GridView grid;
   float step;
+  const float* step_dev;  // nullable: the step size in device memory (overrides step)
   float cone;
   int64_t max_iters;
   const int32_t* packed;
@@ -417,9 +418,10 @@ __global__ void __launch_bounds__(128) march_warp_kernel(MarchArgs a, int64_t sl
     d[k] = a.rays_d[3 * ray + k];
     inv[k] = __fdiv_rn(1.0f, d[k]);
   }
+  const float step = a.step_dev ? *a.step_dev : a.step;
   float near = a.t_min[ray];
   const float far = a.t_max[ray];
-  if (a.jitter) near = __fadd_rn(near, __fmul_rn(a.jitter[ray], a.step));
+  if (a.jitter) near = __fadd_rn(near, __fmul_rn(a.jitter[ray], step));
   int64_t base = 0, room = 0;
   if (MODE == 1) {
     base = a.packed[2 * ray];
@@ -428,7 +430,7 @@ __global__ void __launch_bounds__(128) march_warp_kernel(MarchArgs a, int64_t sl
     base = ray * slot_stride;
     room = slot_stride;
   }
-  const float dt_min = a.step, dt_max = 1e10f;
+  const float dt_min = step, dt_max = 1e10f;
   int64_t j = 0, iters = 0;
   float t0 = near;
   float dt = step_dt(t0, a.cone, dt_min, dt_max);
@@ -928,13 +930,15 @@ int sn_march_count(int64_t n_rays, const float* rays_o, const float* rays_d, con
 int sn_march_padded(int64_t n_rays, const float* rays_o, const float* rays_d, const float* t_min,
                     const float* t_max, const float* jitter, const float* roi,
                     const uint8_t* grid_binary, int rx, int ry, int rz, int contraction_type,
-                    float step_size, float cone_angle, int64_t max_iters, int64_t slot_stride,
-                    int32_t* num_steps, int64_t* ray_indices, float* t_starts, float* t_ends,
-                    int32_t* status, void* stream) {
+                    float step_size, const float* step_size_dev, float cone_angle,
+                    int64_t max_iters, int64_t slot_stride, int32_t* num_steps,
+                    int64_t* ray_indices, float* t_starts, float* t_ends, int32_t* status,
+                    void* stream) {
   MarchArgs a;
   SN_TRY(march_common(a, n_rays, rays_o, rays_d, t_min, t_max, jitter, roi, grid_binary, rx, ry, rz,
                       contraction_type, step_size, cone_angle, max_iters, status));
   SN_REQUIRE(slot_stride > 0, "march_padded: slot_stride must be positive");
+  a.step_dev = step_size_dev;
   SN_REQUIRE(num_steps && ray_indices && t_starts && t_ends, "march_padded: null output");
   if (n_rays == 0) return SN_OK;
   a.num_steps = num_steps;

@@ -11,6 +11,7 @@ per pixel (models/dataset_loader.py:112-137, :223-277).
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 from dataclasses import dataclass, field
 from typing import Optional
@@ -28,11 +29,36 @@ __all__ = ["SDFScene", "sphere", "displaced_torus", "box", "union", "CameraRig",
 @dataclass
 class SDFScene:
     """An analytic signed distance (approximate where displaced) with a
-    Lipschitz bound used to keep sphere tracing conservative."""
+    Lipschitz bound used to keep sphere tracing conservative.  ``prims`` /
+    ``disp`` describe the same scene to the device ground-truth renderer
+    (``sn_scene_render_gt``): (kind, centre, size, amp, freq) per primitive
+    and the union displacement (amp, freq); empty when the scene is not a
+    plain union of at most four primitives."""
 
     fn: callable
     lipschitz: float = 1.0
     name: str = "scene"
+    prims: tuple = ()
+    disp: tuple = (0.0, 0.0)
+
+    def descriptor(self):
+        """The scene as an ``sn_scene_desc`` (None when it has no descriptor)."""
+        from ._lib import SN_SCENE_MAX_PRIMS, SceneDesc
+
+        if not self.prims or len(self.prims) > SN_SCENE_MAX_PRIMS:
+            return None
+        d = SceneDesc()
+        d.n_prims = len(self.prims)
+        for k, (kind, ctr, size, amp, freq) in enumerate(self.prims):
+            p = d.prims[k]
+            p.kind = kind
+            for i in range(3):
+                p.center[i] = float(ctr[i])
+                p.size[i] = float(size[i])
+            p.amp, p.freq = float(amp), float(freq)
+        d.disp_amp, d.disp_freq = float(self.disp[0]), float(self.disp[1])
+        d.lipschitz = float(self.lipschitz)
+        return d
 
     def __call__(self, p: Tensor) -> Tensor:
         return self.fn(p)
@@ -51,7 +77,7 @@ def sphere(radius: float = 0.5, center=(0.0, 0.0, 0.0)) -> SDFScene:
     def f(p):
         return torch.linalg.vector_norm(p - c.to(p), dim=-1) - radius
 
-    return SDFScene(f, 1.0, f"sphere(r={radius})")
+    return SDFScene(f, 1.0, f"sphere(r={radius})", prims=((0, tuple(center), (radius, 0.0, 0.0), 0.0, 0.0),))
 
 
 def displaced_torus(R: float = 0.5, r: float = 0.2, amp: float = 0.02, freq: float = 20.0,
@@ -71,7 +97,8 @@ def displaced_torus(R: float = 0.5, r: float = 0.2, amp: float = 0.02, freq: flo
         return d
 
     lip = 1.0 + abs(amp) * freq * (1.0 / max(R - r, 1e-3) + 1.0 / r)
-    return SDFScene(f, lip, f"torus(R={R},r={r},amp={amp},freq={freq})")
+    return SDFScene(f, lip, f"torus(R={R},r={r},amp={amp},freq={freq})",
+                    prims=((1, tuple(center), (R, r, 0.0), amp, freq),))
 
 
 def box(half=(0.3, 0.3, 0.3), center=(0.0, 0.0, 0.0)) -> SDFScene:
@@ -84,7 +111,7 @@ def box(half=(0.3, 0.3, 0.3), center=(0.0, 0.0, 0.0)) -> SDFScene:
         inside = q.amax(dim=-1).clamp_max(0.0)
         return outside + inside
 
-    return SDFScene(f, 1.0, f"box({tuple(half)})")
+    return SDFScene(f, 1.0, f"box({tuple(half)})", prims=((2, tuple(center), tuple(half), 0.0, 0.0),))
 
 
 def union(*scenes: SDFScene, displacement: float = 0.0, freq: float = 20.0) -> SDFScene:
@@ -96,7 +123,10 @@ def union(*scenes: SDFScene, displacement: float = 0.0, freq: float = 20.0) -> S
         return d
 
     lip = max(s.lipschitz for s in scenes) + abs(displacement) * freq * math.sqrt(3.0)
-    return SDFScene(f, lip, "union(" + ",".join(s.name for s in scenes) + ")")
+    plain = all(s.prims and s.disp[0] == 0.0 for s in scenes)
+    prims = tuple(p for s in scenes for p in s.prims) if plain else ()
+    return SDFScene(f, lip, "union(" + ",".join(s.name for s in scenes) + ")", prims=prims,
+                    disp=(displacement, freq) if displacement else (0.0, 0.0))
 
 
 def random_scene(seed: int) -> SDFScene:
@@ -200,10 +230,24 @@ def sphere_trace(scene: SDFScene, o: Tensor, d: Tensor, near: Tensor, far: Tenso
     return t, hit
 
 
+def render_view_gt(scene: SDFScene, rig: CameraRig, view: int, xs: Tensor, ys: Tensor):
+    """Ground-truth normals (N, 3) and hit mask of one view at pixel
+    coordinates (xs, ys) with torch float64 ops (any device)."""
+    d = pixel_rays(rig, view, xs, ys)
+    o = rig.poses[view, :3, 3].to(xs.device).expand_as(d)
+    near, far = _near_far(o, d)
+    t, hit = sphere_trace(scene, o.reshape(-1, 3), d.reshape(-1, 3), near.reshape(-1), far.reshape(-1))
+    pts = o.reshape(-1, 3) + d.reshape(-1, 3) * t[:, None]
+    return scene.normal(pts) * hit[:, None], hit
+
+
 @dataclass
 class SyntheticDataset:
     """Views of an analytic scene with GT normals / masks, resident on
     `device`; gen_random_patches mirrors the reference sampler.  On a GPU the
+    ground truth of a scene with a descriptor comes from one
+    ``sn_scene_render_gt`` launch (double sphere tracing); otherwise from
+    the torch float64 path (``render_view_gt``).  On a GPU the
     patches' rays and V^-1 are formed per pixel by `sn_gen_patches`, so no
     per-pixel (H, W, 3) ray or (H, W, 3, 3) V^-1 table is kept (48 B per
     pixel); `rays_all` / `V_inverse_all` build those tables on first use."""
@@ -219,27 +263,31 @@ class SyntheticDataset:
     def __post_init__(self):
         n, H, W = self.rig.poses.shape[0], self.rig.H, self.rig.W
         dev = self.device
-        ys, xs = torch.meshgrid(torch.arange(H, device=dev, dtype=torch.float64),
-                                torch.arange(W, device=dev, dtype=torch.float64), indexing="ij")
-        normals, masks = [], []
-        for v in range(n):
-            d = pixel_rays(self.rig, v, xs, ys)                         # (H, W, 3)
-            o = self.rig.poses[v, :3, 3].to(dev).expand_as(d)
-            near, far = _near_far(o, d)
-            t, hit = sphere_trace(self.scene, o.reshape(-1, 3), d.reshape(-1, 3), near.reshape(-1),
-                                  far.reshape(-1))
-            pts = o.reshape(-1, 3) + d.reshape(-1, 3) * t[:, None]
-            nrm = self.scene.normal(pts) * hit[:, None]
-            normals.append(nrm.reshape(H, W, 3).float())
-            masks.append(hit.reshape(H, W).float())
-        self.normals = torch.stack(normals)
-        self.masks = torch.stack(masks)
         self.pose_all = self.rig.poses.to(dev).float()
         self.intrinsics_all = self.rig.intrinsics.to(dev).float()
         self.kinv = inv3x3(self.rig.intrinsics[:, :3, :3].double()).to(dev).contiguous()
         self.pose34 = self.rig.poses[:, :3, :4].double().to(dev).contiguous()
         self.n_images, self.H, self.W = n, H, W
         self._tables = None
+        desc = self.scene.descriptor()
+        if dev.type == "cuda" and desc is not None:
+            # one launch for every view (sn_scene_render_gt: double sphere tracing)
+            from ._lib import call, stream_handle
+
+            self.normals = torch.empty((n, H, W, 3), device=dev)
+            self.masks = torch.empty((n, H, W), device=dev)
+            call("sn_scene_render_gt", C.byref(desc), n, H, W, self.kinv, self.pose34, 400, 1e-6,
+                 self.normals, self.masks, stream_handle())
+            return
+        ys, xs = torch.meshgrid(torch.arange(H, device=dev, dtype=torch.float64),
+                                torch.arange(W, device=dev, dtype=torch.float64), indexing="ij")
+        normals, masks = [], []
+        for v in range(n):
+            nrm, hit = render_view_gt(self.scene, self.rig, v, xs, ys)
+            normals.append(nrm.reshape(H, W, 3).float())
+            masks.append(hit.reshape(H, W).float())
+        self.normals = torch.stack(normals)
+        self.masks = torch.stack(masks)
 
     def _build_tables(self):
         if self._tables is None:

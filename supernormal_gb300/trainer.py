@@ -140,6 +140,7 @@ class FusedTrainer:
                                   dtype=torch.uint8, device=dev)
         # ---- device scalars ----
         self.iter_dev = torch.zeros((1,), dtype=torch.int32, device=dev)
+        self.dt_dev = torch.zeros((1,), device=dev)   # marching step of the step-size schedule
         self.lr_dev = torch.zeros((1,), device=dev)
         self.adam_step_dev = torch.zeros((1,), dtype=torch.int32, device=dev)
         self.status = torch.zeros((1,), dtype=torch.int32, device=dev)
@@ -247,6 +248,13 @@ class FusedTrainer:
         slop = (math.log10(c.start_step_size) - math.log10(c.end_step_size)) / c.end_iter
         return 10 ** (math.log10(c.start_step_size) - slop * it)
 
+    def step_key(self, it: int):
+        """What a captured iteration depends on besides its device state: the
+        fixed step size, or None when the step follows the log schedule (the
+        marcher then reads the step that sn_step_size_schedule writes on the
+        device from the device iteration counter)."""
+        return None if self.cfg.start_step_size is not None else self.cfg.step_size
+
     @torch.no_grad()
     def weight_norm_forward(self, st) -> None:
         v = self.views
@@ -291,14 +299,15 @@ class FusedTrainer:
             self.occupancy_update(it)
         if c.increase_bandwidth_every > 0 and it % c.increase_bandwidth_every == 0:
             self.net.increase_bandwidth()
-        self.run_step(rays_o, rays_d, plane_n, vinv, normal, mask, self.step_size(it),
+        self.run_step(rays_o, rays_d, plane_n, vinv, normal, mask, self.step_key(it),
                       self.net.active_levels())
         self.iter_step += 1
         return self.loss_out
 
     @torch.no_grad()
-    def run_step(self, rays_o, rays_d, plane_n, vinv, normal, mask, dt: float, active: int) -> None:
-        """The capturable part of an iteration (fixed dt / bandwidth)."""
+    def run_step(self, rays_o, rays_d, plane_n, vinv, normal, mask, dt, active: int) -> None:
+        """The capturable part of an iteration (fixed bandwidth; dt fixed, or
+        None for the device-side step-size schedule)."""
         self.forward_backward(rays_o, rays_d, plane_n, vinv, normal, mask, dt, active)
         self.optimizer_step()
 
@@ -314,9 +323,11 @@ class FusedTrainer:
         self._mark("adam_end")
 
     @torch.no_grad()
-    def forward_backward(self, rays_o, rays_d, plane_n, vinv, normal, mask, dt: float,
+    def forward_backward(self, rays_o, rays_d, plane_n, vinv, normal, mask, dt,
                          active: int) -> None:
-        """Loss and gradients (accumulated into the flat gradient buffer)."""
+        """Loss and gradients (accumulated into the flat gradient buffer).
+        dt: the marching step, or None to take it from the configured log
+        schedule at the device iteration counter."""
         c, st = self.cfg, stream_handle()
         B, P, H, W, C0 = self.B, self.P, c.patch_h, c.patch_w, self.C0
         assert rays_o.shape[0] == B and rays_o.is_contiguous() and rays_d.is_contiguous()
@@ -340,8 +351,13 @@ class FusedTrainer:
         call("sn_near_far_sphere", B, _center_ptr(rays_o, kc), _center_ptr(rays_d, kc), 3 * P,
              self.near, self.far, self.jitter, seed, self.iter_dev, self.ro_c, self.rd_c, st)
         # --- marching over the centre rays: one pass into per-ray slots, scan, pack ---
+        dt_dev = None
+        if dt is None:
+            call("sn_step_size_schedule", self.iter_dev, float(c.start_step_size), float(c.end_step_size),
+                 int(c.end_iter), self.dt_dev, st)
+            dt_dev, dt = self.dt_dev, c.start_step_size
         call("sn_march_padded", B, self.ro_c, self.rd_c, self.near, self.far, self.jitter, roi, binary,
-             rx, ry, rz, ctype, float(dt), 0.0, 0, self.max_steps, self.counts0, self.ridx_pad,
+             rx, ry, rz, ctype, float(dt), dt_dev, 0.0, 0, self.max_steps, self.counts0, self.ridx_pad,
              self.ts_pad, self.te_pad, self.status, st)
         call("sn_pack_counts", B, self.counts0, self.packed0, self.total0, self.scan_ws, st)
         call("sn_compact_padded", B, self.max_steps, self.packed0, self.ridx_pad, self.ts_pad,
@@ -513,6 +529,7 @@ class GraphStep:
         self.points: list = []
         self.samples: list = []    # per replayed step: (marched centre samples, kept samples)
         self.launches = 0
+        self.captures = 0          # graphs captured so far (iteration copies and occupancy update)
         self.invalidate()
 
     def invalidate(self) -> None:
@@ -541,6 +558,7 @@ class GraphStep:
         finally:
             tr.profile, tr._capturing = prof, False
         rec["launches"] = lib().sn_kernel_launches() - n0
+        self.captures += 1
         rec["marks"] = list(tr.marks)
         tr.marks.clear()
         return rec
@@ -579,7 +597,7 @@ class GraphStep:
         copies and, past the occupancy warm-up, the occupancy update)."""
         tr, c = self.tr, self.tr.cfg
         it = tr.iter_step
-        key = (tr.step_size(it), tr.net.active_levels())
+        key = (tr.step_key(it), tr.net.active_levels())
         if key != self._step_key:
             self.flush()
             self._steps = [None] * self.n_copies
@@ -611,7 +629,7 @@ class GraphStep:
         if batch is not None:
             for dst, src in zip(self.inputs, batch):
                 dst.copy_(src, non_blocking=True)
-        key = (tr.step_size(it), tr.net.active_levels())
+        key = (tr.step_key(it), tr.net.active_levels())
         if key != self._step_key:
             self.flush()
             self._steps = [None] * self.n_copies

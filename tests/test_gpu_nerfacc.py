@@ -197,8 +197,10 @@ def test_padded_single_pass_marcher_matches(nf):
     tep = torch.empty(n * stride, device="cuda")
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
     roi, binary, rx, ry, rz, ct = nf._grid_args(g, "cuda")
-    call("sn_march_padded", n, T(o), T(d), T(near), T(far), T(jitter), roi, binary, rx, ry, rz, ct, step,
-         0.0, 0, stride, counts, rp, tsp, tep, status, st)
+    # the step size from device memory (the scalar argument is then ignored)
+    step_dev = torch.tensor([step], dtype=torch.float32, device="cuda")
+    call("sn_march_padded", n, T(o), T(d), T(near), T(far), T(jitter), roi, binary, rx, ry, rz, ct, 123.0,
+         step_dev, 0.0, 0, stride, counts, rp, tsp, tep, status, st)
     packed2, total = nf._pack_counts(counts)
     m = int(total.item())
     ri2 = torch.empty(m, dtype=torch.int64, device="cuda")

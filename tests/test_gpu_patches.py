@@ -48,3 +48,29 @@ def test_dataset_keeps_no_per_pixel_tables(built_lib):
     ds = scenes.SyntheticDataset(scenes.sphere(0.5), scenes.ring_cameras(3, 40, 50), torch.device("cuda"))
     ds.gen_random_patches(64)
     assert ds._tables is None
+
+
+@pytest.mark.parametrize("which", ["sphere", "torus", "union"])
+def test_scene_ground_truth_kernel_matches_torch(built_lib, which):
+    """sn_scene_render_gt (one launch, double sphere tracing, central-difference
+    normals) against the torch float64 path (autograd normals) on every pixel."""
+    from supernormal_gb300 import scenes
+
+    sc = {"sphere": scenes.sphere(0.45, (0.05, 0.0, -0.02)),
+          "torus": scenes.displaced_torus(0.5, 0.2, 0.02, 20.0),
+          "union": scenes.random_scene(3)}[which]
+    assert sc.descriptor() is not None
+    rig = scenes.ring_cameras(3, 48, 64, radius=3.0, elevation_deg=25.0)
+    ds = scenes.SyntheticDataset(sc, rig, torch.device("cuda"))
+    H, W = rig.H, rig.W
+    ys, xs = torch.meshgrid(torch.arange(H, device="cuda", dtype=torch.float64),
+                            torch.arange(W, device="cuda", dtype=torch.float64), indexing="ij")
+    for v in range(3):
+        nrm, hit = scenes.render_view_gt(sc, rig, v, xs, ys)
+        m_ref = hit.reshape(H, W).float()
+        m_got = ds.masks[v]
+        differ = (m_ref != m_got)
+        assert differ.float().mean().item() < 2e-3
+        both = (m_ref > 0) & (m_got > 0)
+        err = (ds.normals[v][both] - nrm.reshape(H, W, 3).float()[both]).abs().max().item()
+        assert both.sum() > 100 and err < 1e-5, err

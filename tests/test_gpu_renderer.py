@@ -206,19 +206,18 @@ def _trainer(scene, B=128, **kw):
     return tr, net, var
 
 
-@pytest.mark.parametrize("method", ["dfd", "ad"])
-def test_trainer_loss_and_grads_match_oracle(scene, method):
-    tr, net, var = _trainer(scene, gradient_method=method)
-    g = torch.Generator(device="cuda").manual_seed(5)
-    ro, rd, pn, vinv, nrm, mask = scene.gen_random_patches(128, generator=g)
+def _check_trainer_step(tr, net, var, batch, method, min_samples):
+    """One forward/backward of the fused step against the oracle on the kept
+    samples: culling, the four losses and every parameter gradient."""
+    ro, rd, pn, vinv, nrm, mask = batch
     prm, fld = oracle_field(net)
     var_ref = var.variance.detach().cpu().double().clone().requires_grad_(True)
     tr.grads.zero_()
-    tr.forward_backward(ro, rd, pn, vinv, nrm, mask, 1.0 / 96, net.active_levels())
+    tr.forward_backward(ro, rd, pn, vinv, nrm, mask, tr.step_size(tr.iter_step), net.active_levels())
     torch.cuda.synchronize()
     tr.check_status()
     S = int(tr.S.item())
-    assert S > 300
+    assert S > min_samples
     # culling parity on the pre-cull samples
     n0 = int(tr.total0.item())
     ri0, ts0, te0 = cpu(tr.ridx0[:n0]), cpu(tr.ts0[:n0]), cpu(tr.te0[:n0])
@@ -239,6 +238,42 @@ def test_trainer_loss_and_grads_match_oracle(scene, method):
     for n, r in zip(names + ["variance"], rgrads):
         got = cpu(tr.gviews[n])
         assert grad_err(n, got, r.numpy().reshape(got.shape)) < 2e-3, n
+
+
+@pytest.mark.parametrize("method", ["dfd", "ad"])
+def test_trainer_loss_and_grads_match_oracle(scene, method):
+    tr, net, var = _trainer(scene, gradient_method=method)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    _check_trainer_step(tr, net, var, scene.gen_random_patches(128, generator=g), method, 300)
+
+
+def test_trainer_step_at_benchmark_shapes_matches_oracle(built_lib):
+    """The benchmark's configuration: displaced torus seen by 612x512 views on
+    an elevated ring, hash grid 16 levels x 2 features x 2^19 entries, MLP
+    35 -> 64 -> 16, 128^3 occupancy grid (warm-up sweep, then updates every 8
+    iterations), marching step 2/1024, FP32, here 256 patches.  After 24
+    training iterations from the benchmark's initialisation, one iteration
+    against the oracle on the kept samples."""
+    from supernormal_gb300 import scenes
+    from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
+    from supernormal_gb300.trainer import FusedTrainer, TrainConfig
+
+    enc = dict(otype="HashGrid", n_levels=16, n_features_per_level=2, log2_hashmap_size=19,
+               base_resolution=16, per_level_scale=1.447)
+    rig = scenes.ring_cameras(4, 512, 612, radius=3.0, elevation_deg=30.0, fov_deg=40.0)
+    ds = scenes.SyntheticDataset(scenes.displaced_torus(0.5, 0.2, 0.02, 20.0), rig, torch.device("cuda"))
+    torch.manual_seed(1234)
+    net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=enc, input_concat=True).cuda()
+    var = SingleVarianceNetwork(0.5).cuda()
+    net.bindwidth = 16
+    cfg = TrainConfig(batch_size=256, step_size=2.0 / 1024, occ_update_freq=8, occ_threshold=0.1,
+                      increase_bandwidth_every=0, end_iter=5000)
+    tr = FusedTrainer(net, var, cfg)
+    g = torch.Generator(device="cuda").manual_seed(21)
+    for _ in range(24):
+        tr.train_step(*ds.gen_random_patches(256, generator=g))
+    tr.check_status()
+    _check_trainer_step(tr, net, var, ds.gen_random_patches(256, generator=g), "dfd", 256 * 8)
 
 
 def test_adam_matches_torch(built_lib):

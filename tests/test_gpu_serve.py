@@ -43,6 +43,55 @@ def test_graph_step_matches_eager(built_lib):
     assert gs._steps[0] is not None and gs._occ is not None
 
 
+def test_graph_step_follows_step_size_schedule(built_lib):
+    """The reference's log step-size schedule (exp_runner.py:81-83,149;
+    1e-2 -> 1e-3) as graph replays: the marcher reads the step the schedule
+    kernel writes from the device iteration counter, so 20 iterations need
+    one captured iteration, and they train like the eager iterations, whose
+    marcher takes the same device-side step."""
+    from supernormal_gb300 import scenes
+    from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
+    from supernormal_gb300.trainer import FusedTrainer, GraphStep, TrainConfig
+
+    ds = scenes.SyntheticDataset(scenes.sphere(0.5), scenes.ring_cameras(6, 96, 96, elevation_deg=20),
+                                 torch.device("cuda"))
+    enc = dict(otype="HashGrid", n_levels=16, n_features_per_level=2, log2_hashmap_size=15,
+               base_resolution=16, per_level_scale=1.447)
+
+    def make():
+        torch.manual_seed(0)
+        net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=enc, input_concat=True).cuda()
+        var = SingleVarianceNetwork(0.3).cuda()
+        cfg = TrainConfig(batch_size=128, start_step_size=1e-2, end_step_size=1e-3, end_iter=20,
+                          occ_update_freq=0, increase_bandwidth_every=0, warm_up_end=2, seed=3)
+        net.bindwidth = 16
+        return FusedTrainer(net, var, cfg)
+
+    g = torch.Generator(device="cuda").manual_seed(1)
+    batches = [ds.gen_random_patches(128, generator=g) for _ in range(20)]
+    eager, graphed = make(), make()
+    gs = GraphStep(graphed)
+    le, lg, marched, steps = [], [], [], []
+    for i, b in enumerate(batches):
+        le.append(eager.train_step(*b).clone())
+        marched.append(int(eager.total0.item()))
+        steps.append(float(eager.dt_dev.item()))
+        lg.append(gs.step(b).clone())
+    torch.cuda.synchronize()
+    eager.check_status()
+    graphed.check_status()
+    assert gs.captures == 1
+    # the device schedule is the host schedule rounded once to float
+    import numpy as np
+
+    want = [np.float32(eager.step_size(i)) for i in range(20)]
+    assert steps == [float(w) for w in want]
+    assert marched[-1] > 3 * marched[0]       # finer steps march more samples
+    assert torch.equal(le[0], lg[0])
+    for a, b in zip(le, lg):
+        assert torch.allclose(a, b, rtol=2e-3, atol=1e-6), (a, b)
+
+
 def test_graph_step_profile_marks(built_lib):
     """Profiled graph replays (three copies with captured stage events) report
     every step's stage marks in order, its field-point count and the kernels
