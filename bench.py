@@ -3,18 +3,26 @@
 
 Workload (the reference-equivalent GPU configuration): a displaced torus
 (R=0.5, r=0.2, amplitude 0.02, frequency 20) seen by 20 views of 612x512 on an
-elevated ring; hash grid 16 levels x 2 features, 2^19 entries per level, base
-resolution 16, scale 1.447; SDF MLP 35 -> 64 -> 16; 128^3 occupancy grid
-(threshold 0.1, updated every 8 iterations with the post-warm-up cell
-sampling); marching step 2/1024; 2048 patches of 3x3 per iteration; FP32;
-all 16 levels active (the most expensive bandwidth of the schedule).  Data
-are synthetic (no dataset is shipped).  A step is one full training
-iteration: marching, culling, patch expansion, field forward, render + loss +
-adjoint, field backward, learning-rate schedule and Adam, plus the amortised
-occupancy update.
+elevated ring (15 train; views 0, 4, 8, 12, 16 held out for evaluation as
+config/diligent.conf:16 excludes them); hash grid 16 levels x 2 features,
+2^19 entries per level, base resolution 16, scale 1.447; SDF MLP
+35 -> 64 -> 16; 128^3 occupancy grid (threshold 0.1, updated every 8
+iterations); marching step 2/1024; 2048 patches of 3x3 per iteration; FP32.
+Data are synthetic (no dataset is shipped).
+
+The run: (1) the configuration's whole training schedule from the seeded
+initialisation (5000 iterations, one finer level every 300, occupancy
+warm-up then sampled updates, warm-up + cosine learning rate), timed end to
+end (``training_run``); (2) quality of the trained field on the held-out
+views (normal angular error, mask IoU, Chamfer / F-score, ``quality``);
+(3) W warm-up and K timed steps at the trained state with all 16 levels
+active: a step is one full training iteration (marching, culling, patch
+expansion, field forward, render + loss + adjoint, field backward,
+learning-rate schedule and Adam, plus the amortised occupancy update).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--precision fp32|mixed] [--eager] [--serve small|full|off] [--quality]
+                  [--train-iters N] [--precision fp32|mixed] [--eager]
+                  [--serve small|full|off] [--quality]
 
 The timed region replays each iteration as a CUDA graph whose captured copies
 carry the stage events (per-stage times and the roofline's kernel durations
@@ -23,9 +31,12 @@ end-to-end figure feeds every iteration from pinned host memory through the
 trainer's prefetcher and reads its loss back.  N > 1 runs as independent
 replicas (one process per GPU via torchrun; the path has no exchange step),
 value = all ranks' rays / max rank time.
---impl reference times the reference's CPU implementation of the path (the
-float64 restatement in oracle/, the reference having no CPU path of its own)
-on host cores over a bounded, proportional sample of the same workload.
+Baselines: ``kernels_vs_reference`` times the reference's own marcher and
+patch-weight kernels (built from its sources) against ours on the run's
+inputs; ``cpu_baseline`` and --impl reference time the reference path's
+math (the float32 restatement in oracle/, the reference having no CPU path
+of its own) on host cores over a bounded, proportional sample of the same
+workload, on a state both arms rebuild on the host.
 """
 from __future__ import annotations
 
@@ -54,7 +65,7 @@ ENC = dict(otype="HashGrid", n_levels=16, n_features_per_level=2, log2_hashmap_s
 WORKLOAD = "patch-NeuS training iteration, displaced torus 20x612x512, hashgrid L16 F2 T2^19, 128^3 grid, dt=2/1024"
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=200)
@@ -64,9 +75,15 @@ def parse():
     p.add_argument("--views", type=int, default=20)
     p.add_argument("--height", type=int, default=512)
     p.add_argument("--width", type=int, default=612)
-    p.add_argument("--pretrain", type=int, default=200, help="untimed iterations before warm-up")
+    p.add_argument("--train-iters", type=int, default=5000,
+                   help="training run from the initialisation before the timed steps (the configuration's "
+                        "5000-iteration schedule)")
+    p.add_argument("--bandwidth-every", type=int, default=300, help="one finer hash level every N iterations")
     p.add_argument("--cpu-sample-patches", type=int, default=8)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-quality", action="store_true", help="skip the held-out-view quality evaluation")
+    p.add_argument("--no-reference-kernels", action="store_true",
+                   help="skip timing the reference's own marcher / patch-weight kernels")
     p.add_argument("--no-clocks", action="store_true")
     p.add_argument("--precision", choices=["fp32", "mixed"], default="fp32",
                    help="mixed: FP16 hash-table copy and one-pass TF32 MLP products (config 3's path)")
@@ -80,7 +97,7 @@ def parse():
                    help="instead of the throughput run: FP32 vs mixed precision reconstruction quality "
                         "on the sphere scene (angular error, mask IoU, Chamfer / F@0.01)")
     p.add_argument("--quality-iters", type=int, default=1000)
-    return p.parse_args()
+    return p.parse_args(argv)
 
 
 # ---------------------------------------------------------------------------
@@ -176,6 +193,22 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
+TEST_VIEWS = (0, 4, 8, 12, 16)   # held out for evaluation, as config/diligent.conf:16 excludes them
+
+
+def workload_config(args, world) -> dict:
+    """The workload both arms run (identical dictionaries in both JSON lines)."""
+    return {"workload": WORKLOAD, "scene": "displaced torus R=0.5 r=0.2 amp=0.02 freq=20",
+            "patches_per_step": args.batch, "patch": "3x3", "rays_per_step": args.batch * 9,
+            "views": args.views, "train_views": args.views - len([v for v in TEST_VIEWS if v < args.views]),
+            "resolution": [args.height, args.width], "hash": "L16 F2 T2^19 base 16 scale 1.447",
+            "mlp": "35-64-16 softplus(beta=100), weight norm", "hash_levels": 16, "log2_table": 19,
+            "active_levels": 16, "occupancy": "128^3, threshold 0.1, updated every 8 iterations",
+            "step_size": 2.0 / 1024, "precision": args.precision,
+            "l2": "step working set > L2: table + Adam state 4 x 64 MiB streamed every step",
+            "parallelism": f"replicas{world}"}
+
+
 def build_workload(args, device, seed):
     from supernormal_gb300 import scenes
     from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
@@ -185,33 +218,78 @@ def build_workload(args, device, seed):
     scene = scenes.displaced_torus(0.5, 0.2, 0.02, 20.0)
     rig = scenes.ring_cameras(args.views, args.height, args.width, radius=3.0, elevation_deg=30.0,
                               fov_deg=40.0)
+    test = [v for v in TEST_VIEWS if v < args.views]
+    train = [v for v in range(args.views) if v not in test]
+    pick = lambda vs: scenes.CameraRig(rig.poses[vs], rig.intrinsics[vs], rig.H, rig.W)
     net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=ENC,
                      input_concat=True).to(device)
     var = SingleVarianceNetwork(0.5).to(device)
     cfg = TrainConfig(batch_size=args.batch, step_size=2.0 / 1024, occ_update_freq=8,
-                      occ_threshold=0.1, increase_bandwidth_every=0, end_iter=5000, seed=seed,
+                      occ_threshold=0.1, increase_bandwidth_every=args.bandwidth_every,
+                      end_iter=args.train_iters, seed=seed,
                       encoding_cache=not getattr(args, "no_encoding_cache", False),
                       precision=getattr(args, "precision", "fp32"))
     tr = FusedTrainer(net, var, cfg, device=device)
-    net.bindwidth = ENC["n_levels"]
-    return scene, rig, net, var, tr
+    return scene, pick(train), pick(test) if test else None, net, var, tr
+
+
+def training_run(args, tr, ds, g) -> dict:
+    """The benchmark configuration's whole training schedule from the seeded
+    initialisation: fresh patches every iteration, occupancy warm-up sweeps
+    for 256 iterations then sampled updates every 8, one finer level every
+    ``bandwidth_every`` iterations, warm-up + cosine learning rate, each
+    iteration a CUDA-graph replay (re-captured when the bandwidth changes).
+    Timed end to end with CUDA events (captures and host waits included)."""
+    from supernormal_gb300.trainer import GraphStep
+
+    n = args.train_iters
+    gs = GraphStep(tr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(n):
+        gs.step(ds.gen_random_patches(args.batch, generator=g))
+    e1.record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    tr.check_status()
+    ms = e0.elapsed_time(e1)
+    rays = n * args.batch * tr.P
+    return {"iterations": n, "seconds": ms / 1e3, "wall_seconds": wall, "rays_per_s": rays / (ms / 1e3),
+            "graph_captures": gs.captures, "final_active_levels": tr.net.active_levels(),
+            "loss": [float(x) for x in tr.loss_out.tolist()],
+            "note": "whole schedule from initialisation: patch sampling, occupancy updates, bandwidth "
+                    "schedule and graph captures inside the timed span"}
 
 
 def run_ours(args, world, rank, local):
-    from supernormal_gb300 import scenes
+    from supernormal_gb300 import quality, scenes
     from supernormal_gb300._lib import lib
     from supernormal_gb300.trainer import GraphStep, HostPrefetcher
 
     dev = torch.device("cuda", local)
-    scene, rig, net, var, tr = build_workload(args, dev, seed=1234 + rank)
+    t_setup = time.perf_counter()
+    scene, rig, test_rig, net, var, tr = build_workload(args, dev, seed=1234 + rank)
     ds = scenes.SyntheticDataset(scene, rig, dev)
     g = torch.Generator(device=dev).manual_seed(99 + rank)
     pool = [ds.gen_random_patches(args.batch, generator=g) for _ in range(16)]
-    # warm state: occupancy warm-up from the initial field, a short pre-training
-    tr.occupancy_update(0)
-    for i in range(args.pretrain):
-        tr.train_step(*pool[i % len(pool)])
-    tr.iter_step = max(tr.iter_step, tr.cfg.occ_warmup_steps)   # post-warm-up occupancy regime
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t_setup
+    # the training schedule from initialisation, then the state is measured
+    train = training_run(args, tr, ds, g) if args.train_iters > 0 else None
+    if args.train_iters <= 0:
+        tr.occupancy_update(0)
+    net.bindwidth = max(net.bindwidth, ENC["n_levels"])      # timed steps: all 16 levels
+    tr.iter_step = max(tr.iter_step, tr.cfg.occ_warmup_steps)
+    qual = None
+    if rank == 0 and test_rig is not None and not args.no_quality:
+        tq = time.perf_counter()
+        test_ds = scenes.SyntheticDataset(scene, test_rig, dev)
+        qual = quality.evaluate(net, var, tr.grid, test_ds, scene, tr.cfg.step_size)
+        qual["after_iterations"] = tr.iter_step
+        qual["views"] = f"held-out views {list(TEST_VIEWS)} of {args.views}"
+        qual["seconds"] = time.perf_counter() - tq
     # iterations as CUDA-graph replays carrying the stage events (captured
     # before the warm-up), or eager launches with --eager
     gs = None if args.eager else GraphStep(tr, profile=True)
@@ -228,6 +306,7 @@ def run_ours(args, world, rank, local):
         gs.flush()
         gs.stage_marks.clear()
         gs.points.clear()
+        gs.samples.clear()
 
     # ---------------- device-resident timed region ----------------
     K = args.steps
@@ -298,30 +377,36 @@ def run_ours(args, world, rank, local):
         return None
     peaks, peak_kind = load_peaks()
     rl = roofline(stages, q, tr, peaks, peak_kind, K)
+    spr = None
+    if samples is not None and len(samples):
+        spr = {"marched": float(samples[:, 0].mean()) / args.batch, "kept": float(samples[:, 1].mean()) / args.batch}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": ms_max / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": value / REFERENCE_RAYS_PER_S,
         "dtype": "f32" if tr.cfg.precision == "fp32" else "f32 with f16 table, tf32 mlp", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "patches_per_step": args.batch, "patch": "3x3",
-                   "rays_per_step": args.batch * tr.P, "views": args.views,
-                   "resolution": [args.height, args.width], "hash_levels": 16, "log2_table": 19,
-                   "active_levels": net.active_levels(), "step_size": 2.0 / 1024,
-                   "occupancy_update_every": 8, "encoding_cache": tr.enc_cache is not None,
-                   "precision": tr.cfg.precision,
-                   "samples_per_ray": float(tr.S.item()) / args.batch,
-                   "l2": "step working set > L2: table + Adam state 4 x 64 MiB streamed every step",
-                   "parallelism": f"replicas{world}"},
+        "config": workload_config(args, world),
+        "state": {"kind": "trained", "iterations": tr.iter_step if train else 0,
+                  "samples_per_ray": spr, "encoding_cache": tr.enc_cache is not None,
+                  "note": "timed after the training run from the seeded initialisation; "
+                          "occupancy update every 8 iterations in its sampled regime"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "roofline": rl,
         "stages_ms_per_step": {k: v / K for k, v in stages.items()},
         "stage_roofline": stage_rooflines(stages, q, samples, tr, rl["peak"], K),
+        "setup_s": setup_s,
     }
+    if train is not None:
+        out["training_run"] = train
+    if qual is not None:
+        out["quality"] = qual
     if clk:
         out["clocks"] = clk
+    if not args.no_reference_kernels:
+        out["kernels_vs_reference"] = reference_kernels_leg(tr, pool[0])
     if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args, tr, scene, rig, budget_s=20.0)
+        out["cpu_baseline"] = cpu_baseline(args, budget_s=20.0)
     if args.serve != "off":
         del tr, ds, pool, host, pf, gs
         torch.cuda.empty_cache()
@@ -440,6 +525,8 @@ def stage_rooflines(stages, q, samples, tr, peak, K):
     32 B per parameter; field kernels as in roofline()."""
     if samples is None or q is None or len(samples) == 0:
         return None
+    if len(samples) != len(q):
+        raise ValueError(f"stage_rooflines: sample counts of {len(samples)} steps against field points of {len(q)}")
     L, F = tr.net.active_levels(), 2
     enc = L * F * 4 if tr.enc_cache is not None else 0
     marched, kept = samples[:, 0].sum(), samples[:, 1].sum()
@@ -492,137 +579,232 @@ def roofline(stages, q, tr, peaks, peak_kind, K):
 
 
 # ---------------------------------------------------------------------------
-def cpu_step_factory(args, net_state, scene, rig, seed):
-    """One proportional sample of a training iteration on host cores (float64 oracle)."""
-    import numpy as np
+# Baseline legs.  They run the reference's arithmetic outside the package:
+# the host restatement in oracle/ on the CPU (cpu_baseline, --impl reference)
+# and the reference's own kernels compiled from its sources (oracle/_ref) on
+# the GPU (kernels_vs_reference).  Nothing on the timed path of our arm calls
+# them.
+HOST_STATE = ("seeded initialisation (torch seed 1234; the same parameters as the GPU arm's initial "
+              "network) with the occupancy grid of the analytic torus (sigmoid(-80 sdf) at cell centres "
+              "above min(mean, 0.1)): a state both arms rebuild exactly on host cores")
 
+
+def host_step_factory(args, seed, dtype=torch.float32):
+    """One proportional sample of a training iteration on host cores: the
+    reference's math restated in oracle/ (marcher in C, field, culling,
+    patch render, losses and their backward in torch on the CPU), on the
+    host state above.  B_s of ``args.batch`` patches; the amortised
+    occupancy update and the Adam elements are scaled by the same fraction.
+    Batches are drawn before timing (the reference gathers them from images
+    already in memory)."""
     from oracle import field as OF
     from oracle import march as OM
     from oracle import renderer as OR
-    from supernormal_gb300 import scenes
+    from oracle import scene as OS
 
     B_s = args.cpu_sample_patches
     frac = B_s / args.batch
-    prm, geom, variance, binary, n_params = net_state
-    table = prm["table"]
-    g = torch.Generator().manual_seed(seed)
-    n_occ = max(1, int(round((128 ** 3 // 2) / 8 * frac)))      # amortised occupancy points
+    prm, geom = OS.sdf_network_init(1234, ENC)
+    prm = {k: v.to(dtype).requires_grad_(True) for k, v in prm.items()}
+    variance = torch.tensor(0.5, dtype=dtype, requires_grad=True)
+    binary = OS.analytic_occupancy(OS.torus_sdf, 128, 0.1)
+    n_params = sum(v.numel() for v in prm.values()) + 1
+    poses, kinv = OS.ring_rig(args.views, args.height, args.width)
+    train_views = [v for v in range(args.views) if v not in TEST_VIEWS]
+    poses, kinv = poses[train_views], kinv[train_views]
+    rng = np.random.default_rng(seed)
+    pool = [OS.gen_random_patches(OS.torus_sdf, OS.torus_lipschitz(), poses, kinv, args.height, args.width,
+                                  B_s, rng) for _ in range(4)]
+    n_occ_cells = int(binary.sum())
+    n_occ = max(1, int(round((128 ** 3 // 4 + min(n_occ_cells, 128 ** 3 // 4)) / 8 * frac)))
     n_adam = max(4, int(round(n_params * frac)))
-    adam_p = torch.zeros(n_adam, dtype=torch.float64, requires_grad=True)
+    adam_p = torch.zeros(n_adam, dtype=dtype, requires_grad=True)
     opt = torch.optim.Adam([adam_p], lr=5e-4)
     roi = np.array([-1, -1, -1, 1, 1, 1], np.float32)
-    fld = lambda x: OF.sdf_network(x, **prm, geom=geom, active_levels=16, out_cols=1)
+    fld = lambda x: OF.sdf_network(x, **prm, geom=geom, active_levels=16, out_cols=1, dtype=dtype)
+    g = torch.Generator().manual_seed(seed)
+    state = {"i": 0}
 
     def step():
-        ro, rd, pn, vinv, nrm, mask = scenes.sample_patches(scene, rig, B_s, generator=g)
-        ro_c = ro[:, 1, 1].numpy()
-        rd_c = rd[:, 1, 1].numpy()
-        b = 2 * (ro_c * rd_c).sum(1)
-        c = (ro_c * ro_c).sum(1) - 1
-        a = (rd_c * rd_c).sum(1)
-        disc = np.sqrt(np.maximum(b * b - 4 * a * c, 0))
-        near = ((-b - disc) / (2 * a)).astype(np.float32)
-        far = ((-b + disc) / (2 * a)).astype(np.float32)
+        ro, rd, pn, vinv, nrm, mask = pool[state["i"] % len(pool)]
+        state["i"] += 1
+        ro_c, rd_c = ro[:, 1, 1], rd[:, 1, 1]
+        near, far = OS.near_far(ro_c.astype(np.float64), rd_c.astype(np.float64))
         jit = torch.rand(B_s, generator=g).numpy().astype(np.float32)
-        packed, ri, ts, te = OM.ray_marching(ro_c, rd_c, near, far, roi, binary, 2.0 / 1024, jitter=jit)
+        packed, ri, ts, te = OM.ray_marching(ro_c, rd_c, near.astype(np.float32), far.astype(np.float32), roi,
+                                             binary, 2.0 / 1024, jitter=jit)
+        marched, kept = ri.size, 0
         if ri.size:
-            vis, _ = OR.cull(fld, packed, ri, ts, te, ro_c, rd_c, variance.detach())
+            vis, _ = OR.cull(fld, packed, ri, ts, te, ro_c, rd_c, variance.detach(), dtype=dtype)
             ri, ts, te = ri[vis], ts[vis], te[vis]
+            kept = ri.size
         if ri.size:
-            out = OR.patch_forward(fld, ri, ts, te, ro.numpy(), rd.numpy(), pn.numpy(), vinv.numpy(),
-                                   variance)
-            L = OR.losses(out["comp_normal"], out["weight_sum"], out["gradients"], nrm.numpy(),
-                          mask.numpy())
+            out = OR.patch_forward(fld, ri, ts, te, ro, rd, pn, vinv, variance, dtype=dtype)
+            L = OR.losses(out["comp_normal"], out["weight_sum"], out["gradients"], nrm, mask)
             L["total"].backward()
         with torch.no_grad():
-            x = torch.rand((n_occ, 3), generator=g, dtype=torch.float64) * 2 - 1
+            x = torch.rand((n_occ, 3), generator=g, dtype=dtype) * 2 - 1
             torch.sigmoid(-fld(x) * 80.0)
-        adam_p.grad = torch.randn(n_adam, generator=g, dtype=torch.float64)
+        adam_p.grad = torch.randn(n_adam, generator=g, dtype=dtype)
         opt.step()
         for p in list(prm.values()) + [variance]:
             p.grad = None
-        return B_s * 9
+        return B_s * 9, marched, kept
 
     return step
 
 
-def cpu_state(tr):
-    from oracle import field as OF
-
-    prm = OF.params_from_module(tr.net)
-    geom = OF.geometry_from_module(tr.net)
-    variance = tr.dev_net.variance.detach().cpu().double().clone().requires_grad_(True)
-    binary = tr.grid.binary.cpu().numpy().astype("uint8")
-    return prm, geom, variance, binary, tr.n_params
+def _host_sample(args, n, dt, marched, kept):
+    return (f"{n} iterations of {args.cpu_sample_patches} patches (1/{args.batch // args.cpu_sample_patches} "
+            f"of a step; amortised occupancy points and Adam elements scaled alike), float32 restatement of "
+            f"the reference math in oracle/ on host cores, {dt:.1f} s; samples per ray marched "
+            f"{marched:.1f}, kept {kept:.1f}; state: {HOST_STATE}")
 
 
-def cpu_baseline(args, tr, scene, rig, budget_s=20.0):
+def cpu_baseline(args, budget_s=20.0):
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
-    step = cpu_step_factory(args, cpu_state(tr), scene, rig, seed=7)
+    step = host_step_factory(args, seed=7)
     step()  # warm-up
-    rays, t0 = 0, time.perf_counter()
-    n = 0
+    rays = marched = kept = n = 0
+    t0 = time.perf_counter()
     while time.perf_counter() - t0 < budget_s and n < 50:
-        rays += step()
-        n += 1
+        r, m, k = step()
+        rays, marched, kept, n = rays + r, marched + m, kept + k, n + 1
     dt = time.perf_counter() - t0
+    B = n * args.cpu_sample_patches
     return {"value": rays / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} iterations of {args.cpu_sample_patches} patches (1/{args.batch // args.cpu_sample_patches} "
-                      f"of a step: patches, amortised occupancy points and Adam elements scaled alike), "
-                      f"float64 oracle, {dt:.1f} s"}
+            "sample": _host_sample(args, n, dt, marched / B, kept / B)}
+
+
+def reference_kernels_leg(tr, batch, reps: int = 20) -> dict:
+    """The reference's own marcher and patch-weight kernels (nerfacc 0.3.5
+    compiled from its sources for sm_103a) against ours on this step's
+    inputs, CUDA-event medians over ``reps`` repetitions: the marcher as the
+    reference runs it (count pass, cumsum, the .item() sync, fill pass:
+    NA/nerfacc/cuda/csrc/ray_marching.cu:194-289) against sn_march_padded +
+    sn_pack_counts + sn_compact_padded; the patch weights forward and backward
+    (render_weight.cu:502-626) against sn_weight_from_alpha_fwd/bwd on the
+    NeuS alphas of the step's kept samples."""
+    try:
+        from oracle import refkernels
+    except Exception as e:   # pragma: no cover
+        return {"unavailable": f"reference kernel loader: {e}"}
+    ref = refkernels.load()
+    if isinstance(ref, Exception):
+        return {"unavailable": f"reference kernels not built: {ref}"}
+    from supernormal_gb300._lib import call, stream_handle
+
+    st = stream_handle()
+    rays_o, rays_d, plane_n, vinv, normal, mask = batch
+    tr.forward_backward(rays_o, rays_d, plane_n, vinv, normal, mask, tr.step_key(tr.iter_step),
+                        tr.net.active_levels())
+    torch.cuda.synchronize()
+    B, P, dt = tr.B, tr.P, tr.cfg.step_size
+    ro, rd, near, far, jit = tr.ro_c.clone(), tr.rd_c.clone(), tr.near.clone(), tr.far.clone(), tr.jitter.clone()
+    t_min = (near + jit * dt).contiguous()            # the reference adds the jitter in Python
+    grid = tr.grid
+    roi = grid._roi_aabb.contiguous().float()
+    binary = grid._binary.contiguous()
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps + 2):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts[2:]))
+
+    ref_out = {}
+
+    def ref_march():
+        ref_out["r"] = ref.ray_marching(ro, rd, t_min, far, roi, binary, dt)
+
+    def our_march():
+        call("sn_march_padded", B, ro, rd, near, far, jit, roi, binary.view(torch.uint8), *tr.res,
+             grid._contraction_type.value, float(dt), None, 0.0, 0, tr.max_steps, tr.counts0, tr.ridx_pad,
+             tr.ts_pad, tr.te_pad, tr.status, st)
+        call("sn_pack_counts", B, tr.counts0, tr.packed0, tr.total0, tr.scan_ws, st)
+        call("sn_compact_padded", B, tr.max_steps, tr.packed0, tr.ridx_pad, tr.ts_pad, tr.te_pad, tr.ridx0,
+             tr.ts0, tr.te0, st)
+
+    t_ref_m, t_our_m = timed(ref_march), timed(our_march)
+    n0 = int(tr.total0.item())
+    same = bool(torch.equal(ref_out["r"][1], tr.ridx0[:n0]))
+    # NeuS alphas of the kept samples per patch pixel from the step's field values
+    S = int(tr.S.item())
+    packed = tr.packed1.contiguous()
+    alphas = _patch_alphas(tr, S).contiguous()
+    w_ref = ref.patch_weight_fwd(packed, alphas)
+    w_our = torch.empty_like(alphas)
+    g_w = torch.randn(alphas.shape, device=alphas.device, generator=torch.Generator(device=alphas.device).manual_seed(3))
+    ga_our = torch.empty_like(alphas)
+    t_ref_f = timed(lambda: ref.patch_weight_fwd(packed, alphas))
+    t_our_f = timed(lambda: call("sn_weight_from_alpha_fwd", B, P, packed, alphas, w_our, st))
+    t_ref_b = timed(lambda: ref.patch_weight_bwd(packed, alphas, w_ref, g_w))
+    t_our_b = timed(lambda: call("sn_weight_from_alpha_bwd", B, P, packed, alphas, w_our, g_w, ga_our, st))
+    ga_ref = ref.patch_weight_bwd(packed, alphas, w_ref, g_w)
+    tr.grads.zero_()
+    torch.cuda.synchronize()
+    return {"march": {"reference_ms": t_ref_m, "ours_ms": t_our_m, "speedup": t_ref_m / t_our_m,
+                      "rays": B, "samples": n0, "ray_indices_identical": same,
+                      "reference": "count pass + cumsum + .item() + fill pass",
+                      "ours": "single-pass warp-per-ray marcher + scan + compaction, no host sync"},
+            "patch_weights_fwd": {"reference_ms": t_ref_f, "ours_ms": t_our_f, "speedup": t_ref_f / t_our_f,
+                                  "samples": S, "identical": bool(torch.equal(w_ref, w_our))},
+            "patch_weights_bwd": {"reference_ms": t_ref_b, "ours_ms": t_our_b, "speedup": t_ref_b / t_our_b,
+                                  "identical": bool(torch.equal(ga_ref, ga_our))},
+            "note": "inputs: this run's centre rays, jitter and occupancy grid, and the NeuS alphas of its kept "
+                    "samples; the training iteration itself runs the weights fused into the patch render"}
+
+
+def _patch_alphas(tr, S):
+    """(S, P) NeuS alphas (models/renderer.py:164-179) of the last step's kept
+    samples from its field values: the end value is the next start of the
+    ray, or the separate end evaluation where t_end != next t_start."""
+    P = tr.P
+    sdf = tr.sdf1[:, 0]
+    s0 = sdf[: S * P].view(S, P)
+    s1 = torch.cat([s0[1:], s0[-1:]], 0).clone()
+    ep = tr.endp1[:S]
+    has_end = ep[:, 1] != 0
+    slots = ep[has_end, 0].long()
+    s1[has_end] = sdf.view(-1, P)[S + slots]
+    inv_s = torch.exp(tr.dev_net.variance.detach() * 10.0).clip(1e-6, 1e6)
+    prev, nxt = torch.sigmoid(s0 * inv_s), torch.sigmoid(s1 * inv_s)
+    return (((prev - nxt) + 1e-5) / (prev + 1e-5)).clip(0.0, 1.0)
 
 
 def run_reference(args, world, rank, local):
-    """CPU arm: the reference path's math (oracle port) on host cores."""
+    """The reference path's math on host cores (float32 restatement in
+    oracle/, the reference having no CPU path of its own), rank 0 only.
+    Imports nothing from the package."""
     if rank != 0:
         return None
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
-    dev = torch.device("cuda", local) if torch.cuda.is_available() else torch.device("cpu")
-    from supernormal_gb300 import scenes
-    from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
-    from oracle import field as OF
-
-    torch.manual_seed(1234)
-    scene = scenes.displaced_torus(0.5, 0.2, 0.02, 20.0)
-    rig = scenes.ring_cameras(args.views, args.height, args.width, radius=3.0, elevation_deg=30.0,
-                              fov_deg=40.0)
-    net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=ENC, input_concat=True)
-    var = SingleVarianceNetwork(0.5)
-    prm = OF.params_from_module(net)
-    geom = OF.geometry_from_module(net)
-    variance = var.variance.detach().double().clone().requires_grad_(True)
-    # occupancy of the initial field (all cells) on host cores
-    import numpy as np
-
-    r = 128
-    c = (np.stack(np.meshgrid(*[np.arange(r)] * 3, indexing="ij"), -1).reshape(-1, 3) + 0.5) / r * 2 - 1
-    # the sphere-initialised SDF is |x| - 0.5 (+ small table terms): binarise its occupancy
-    occ = 1.0 / (1.0 + np.exp(np.clip((np.linalg.norm(c, axis=1) - 0.5) * 80.0, -50, 50)))
-    binary = (occ > min(occ.mean(), 0.1)).reshape(r, r, r).astype(np.uint8)
-    n_params = net.encoding.params.numel() + sum(p.numel() for n_, p in net.named_parameters()
-                                                 if not n_.startswith("encoding"))
-    step = cpu_step_factory(args, (prm, geom, variance, binary, n_params), scene, rig, seed=11)
+    step = host_step_factory(args, seed=11)
     for _ in range(max(args.warmup, 1)):
         step()
-    rays, t0 = 0, time.perf_counter()
+    rays = marched = kept = 0
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        rays += step()
+        r, m, k = step()
+        rays, marched, kept = rays + r, marched + m, kept + k
     dt = time.perf_counter() - t0
     value = rays / dt
-    sample = (f"{args.steps} iterations of {args.cpu_sample_patches} patches each (1/"
-              f"{args.batch // args.cpu_sample_patches} of a step, occupancy points and Adam elements "
-              f"scaled alike), float64 restatement of the reference math, {threads} threads")
+    B = args.steps * args.cpu_sample_patches
+    sample = _host_sample(args, args.steps, dt, marched / B, kept / B)
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": value / REFERENCE_RAYS_PER_S,
-            "dtype": "f64",
-            "data": "synthetic",
-            "config": {"workload": WORKLOAD, "patches_per_step": args.batch,
-                       "sampled_patches_per_step": args.cpu_sample_patches, "device": "host cores"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": sample},
+            "dtype": "f32", "data": "synthetic", "config": workload_config(args, world),
+            "state": {"kind": "host", "samples_per_ray": {"marched": marched / B, "kept": kept / B},
+                      "note": HOST_STATE},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

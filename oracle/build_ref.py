@@ -6,7 +6,7 @@ to sm_103a cubins in ``oracle/_ref/``, and records the exported kernel symbol
 names (read with ``nm`` from host objects of the same sources) in
 ``oracle/_ref/manifest.json``.  Nothing is copied from the reference tree:
 the compiler reads the sources where they lie.  The cubins are loaded with the
-CUDA driver API by tests/refkernels.py to compare our kernels with the
+CUDA driver API by oracle/refkernels.py to compare our kernels with the
 reference ones on the GPU.  Needs the reference tree, so it runs only where
 that tree is mounted; elsewhere the prebuilt files are used as they are.
 """

@@ -1,10 +1,12 @@
-"""Checker: launch the reference's own CUDA kernels (oracle/_ref cubins) on the GPU.
+"""ORACLE (test infrastructure only): launch the reference's own CUDA kernels
+(oracle/_ref cubins) on the GPU, as the checker in tests/ and as the timed
+reference-kernel baseline of bench.py.
 
 The cubins are nerfacc 0.3.5's ray_marching.cu / render_weight.cu / contraction.cu compiled
 from source for sm_103a by oracle/build_ref.py.  They are loaded with the
 CUDA driver API into the current (torch) context and launched with the
 reference's own launch shapes (ray_marching.cu:227-228,
-render_weight.cu:519-527).  Test infrastructure only.
+render_weight.cu:519-527).
 """
 from __future__ import annotations
 
@@ -15,7 +17,7 @@ from pathlib import Path
 
 import torch
 
-REF = Path(__file__).resolve().parents[1] / "oracle" / "_ref"
+REF = Path(__file__).resolve().parent / "_ref"
 
 
 class Int3(C.Structure):

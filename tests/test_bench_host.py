@@ -44,6 +44,18 @@ def test_stage_rooflines_byte_model():
     assert bench.stage_rooflines(stages, None, None, _Tr(), 1000.0, 2) is None
 
 
+def test_stage_rooflines_rejects_mismatched_steps():
+    """Sample counts and field points must cover the same steps (a warm-up
+    step left in one of them would scale the byte model wrongly)."""
+    import pytest
+
+    stages = {"march": 1.0, "render": 1.0, "adam": 1.0, "field_fwd": 2.0, "field_bwd": 4.0}
+    q = np.full(20, 1000.0)
+    samples = np.full((25, 2), 100.0)
+    with pytest.raises(ValueError):
+        bench.stage_rooflines(stages, q, samples, _Tr(), 1000.0, 20)
+
+
 def test_reference_arm_prints_its_line():
     """bench.py --impl reference (the CPU restatement on host cores) prints one
     JSON line with the contract's keys."""
@@ -53,12 +65,16 @@ def test_reference_arm_prints_its_line():
     import sys
 
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "0", "--cpu-sample-patches", "2"], capture_output=True, text=True,
-                       timeout=600, cwd=root)
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0', "
+            "'--cpu-sample-patches', '2']; runpy.run_path('bench.py', run_name='__main__'); "
+            "print('PKG_LOADED', any(m.startswith('supernormal_gb300') for m in sys.modules))")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=root)
     assert r.returncode == 0, r.stderr[-2000:]
     line = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+    assert "PKG_LOADED False" in r.stdout          # the reference arm imports nothing from the package
     assert line["impl"] == "reference" and line["metric"] == "train_rays_per_s" and line["value"] > 0
+    assert line["dtype"] == "f32" and line["state"]["samples_per_ray"]["marched"] > 0
+    assert line["config"] == bench.workload_config(bench.parse([]), 1)
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
     assert line["higher_is_better"] is True and line["vs_baseline"] > 0

@@ -27,7 +27,7 @@ def nf(built_lib):
 
 @pytest.fixture(scope="module")
 def ref():
-    from tests import refkernels
+    from oracle import refkernels
 
     r = refkernels.load()
     if isinstance(r, Exception):

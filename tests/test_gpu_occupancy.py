@@ -56,7 +56,7 @@ def test_query_points_bit_exact(nf, tag):
 
 
 def test_query_points_vs_reference_kernel(nf):
-    from tests import refkernels
+    from oracle import refkernels
 
     ref = refkernels.load()
     if isinstance(ref, Exception):
@@ -166,10 +166,12 @@ def test_occupancy_grid_api_replays_reference(nf, tag):
     np.testing.assert_array_equal(seen["x"].cpu().numpy(), f("x"))
     want, _ = OO.ema_update(f("occs_before"), None if cells is None else f("cells"), f("occ"), 0.95)
     np.testing.assert_array_equal(grid.occs.cpu().numpy(), want)
-    _, thr = OO.binarize(want, float(f("occ_thre")))
+    b_want, thr = OO.binarize(want, float(f("occ_thre")))
     near = _near_threshold(want, thr)
     got_b = grid.binary.cpu().numpy().reshape(-1)
-    np.testing.assert_array_equal(got_b[~near], f("binary_after").reshape(-1)[~near])
+    np.testing.assert_array_equal(got_b[~near], b_want.reshape(-1)[~near])
+    if cells is None:   # no repeated cells: the reference's own grid
+        np.testing.assert_array_equal(got_b[~near], f("binary_after").reshape(-1)[~near])
 
 
 def test_sample_cells(nf):
