@@ -506,6 +506,33 @@ int sn_scene_render_gt(const sn_scene_desc* scene, int n_views, int H, int W,
 int sn_scene_sdf(const sn_scene_desc* scene, int64_t n, const float* x,
                  float* out, void* stream);
 
+/* ---- mesh extraction (models/renderer.py:9-34, 353-358) ------------------ */
+/* Lattice points of slab [i0, i0 + n_i) of an nx x ny x nz lattice over
+ * [bound_min, bound_max] (double, 3 each): x_out[((i - i0) ny + j) nz + k] =
+ * bound_min + (i, j, k) (bound_max - bound_min) / (n - 1).  Replaces the
+ * torch.linspace / meshgrid blocks of extract_fields (models/renderer.py:9-24). */
+int sn_lattice_points(int64_t i0, int64_t n_i, int nx, int ny, int nz,
+                      const double* bound_min, const double* bound_max,
+                      float* x_out, void* stream);
+/* out[i] = -in[i] (the query_func of NeuSRenderer.extract_geometry is -sdf). */
+int sn_negate(int64_t n, const float* in, float* out, void* stream);
+size_t sn_marching_cubes_workspace_bytes(int nx, int ny, int nz);
+/* Marching cubes of values (nx, ny, nz; k fastest) at threshold (inside:
+ * value > threshold); replaces mcubes.marching_cubes in extract_geometry
+ * (models/renderer.py:27-34).  One vertex per lattice edge whose ends lie on
+ * either side, at the linear-interpolation crossing, in world coordinates
+ * bound_min + index (bound_max - bound_min) / (n - 1); triangles index the
+ * vertices, right-hand normals pointing from the inside out, each cube face
+ * pairing its crossings so that inside corners are cut off (no cracks).
+ * counts[0] = vertices, counts[1] = triangles (device); at most vert_cap /
+ * tri_cap are written, so a first call with zero capacities sizes the
+ * outputs.  Needs 3 nx ny nz < 2^31. */
+int sn_marching_cubes(const float* values, int nx, int ny, int nz,
+                      float threshold, const double* bound_min,
+                      const double* bound_max, int64_t vert_cap,
+                      int64_t tri_cap, float* vertices, int32_t* triangles,
+                      int32_t* counts, void* workspace, void* stream);
+
 /* ---- optimiser (exp_runner.py:97, 205-210, 270-279) ------------------------ */
 /* Reads iteration k from *iter, writes lr(k) of the warm-up + cosine schedule
  * and adam_step = k + 1, then stores k + 1 in *iter. */
@@ -524,14 +551,6 @@ int sn_adam_step(int64_t n, float* param, float* grad, float* exp_avg,
                  float* exp_avg_sq, void* param_half, const float* lr_dev,
                  const int32_t* step_dev, float lr, int step, float beta1,
                  float beta2, float eps, int zero_grad, void* stream);
-
-/* ---- tensor-core MLP pieces (tcgen05, sm_103a) ------------------------------ */
-/* y = x W^T + b with W (64, k), k <= 64: the first Linear of SDFNetwork
- * (models/fields.py:90-99, nn.Linear in fp32), fp32-accurate via 3xTF32 on
- * the tensor cores with TMEM accumulators.  b may be null.  A bounded wait
- * that runs out ORs SN_STATUS_TIMEOUT into *status. */
-int sn_linear_tc(int64_t n, int k, const float* x, const float* w, const float* b, float* y,
-                 int32_t* status, void* stream);
 
 #ifdef __cplusplus
 }

@@ -164,3 +164,27 @@ def losses(comp_normal, weight_sum, gradients, gt_normal, gt_mask, loss_type="l2
     mask_loss = F.binary_cross_entropy(weight_sum.clip(1e-5, 1.0 - 1e-5), mask)
     total = normal_weight * normal_loss + mask_weight * mask_loss + eikonal_weight * eikonal
     return dict(normal=normal_loss, eikonal=eikonal, mask=mask_loss, total=total)
+
+
+def pixel_forward(field, ridx, ts, te, rays_o, rays_d, variance, n_rays):
+    """NeuSRenderer.render_normal_pixel_based after marching and culling
+    (models/renderer.py:338-351), float64: alpha of alpha_fn on the kept
+    samples, per-ray weights (NA/nerfacc/vol_rendering.py:624-678), the SDF
+    gradient (autograd) at the sample midpoints, accumulated normals and
+    depths.  Returns (comp_normal (n_rays, 3), comp_depth (n_rays, 1))."""
+    ridx = np.asarray(ridx, np.int64)
+    with torch.no_grad():
+        alpha = center_alpha(field, ridx, ts, te, rays_o, rays_d, variance).numpy()
+    packed = nerfacc_ref.pack_info(ridx, n_rays)
+    w = nerfacc_ref.weights_fwd(alpha, packed)
+    o = torch.as_tensor(np.asarray(rays_o, np.float32)[ridx]).double()
+    d = torch.as_tensor(np.asarray(rays_d, np.float32)[ridx]).double()
+    mid = (torch.as_tensor(np.asarray(ts, np.float32)).double().reshape(-1, 1)
+           + torch.as_tensor(np.asarray(te, np.float32)).double().reshape(-1, 1)) / 2.0
+    x = (o + d * mid).detach().requires_grad_(True)
+    (g,) = torch.autograd.grad(field(x).sum(), x)
+    wt = torch.as_tensor(w).reshape(-1, 1)
+    idx = torch.as_tensor(ridx)
+    comp = torch.zeros((n_rays, 3), dtype=torch.float64).index_add(0, idx, wt * g)
+    depth = torch.zeros((n_rays, 1), dtype=torch.float64).index_add(0, idx, wt * mid)
+    return comp, depth

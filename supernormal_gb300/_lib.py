@@ -85,7 +85,6 @@ SIGNATURES: dict[str, tuple] = {
     "sn_scan_workspace_bytes": (_SZ, [_I64]),
     "sn_pack_counts": (_I, [_I64, _P, _P, _P, _P, _P]),
     "sn_pack_counts_static": (_I, [_I64, _P, _P, _P, _P]),
-    "sn_linear_tc": (_I, [_I64, _I, _P, _P, _P, _P, _P, _P]),
     "sn_count_indices": (_I, [_I64, _P, _I64, _P, _P]),
     "sn_unpack_info": (_I, [_I64, _P, _I64, _P, _P]),
     "sn_march_count": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _F, _F, _I64, _P, _P, _P]),
@@ -137,6 +136,10 @@ SIGNATURES: dict[str, tuple] = {
     "sn_mask_prep": (_I, [_I64, _P, _P, _P, _P]),
     "sn_scene_render_gt": (_I, [_SD, _I, _I, _I, _P, _P, _I, C.c_double, _P, _P, _P]),
     "sn_scene_sdf": (_I, [_SD, _I64, _P, _P, _P]),
+    "sn_lattice_points": (_I, [_I64, _I64, _I, _I, _I, _P, _P, _P, _P]),
+    "sn_negate": (_I, [_I64, _P, _P, _P]),
+    "sn_marching_cubes_workspace_bytes": (_SZ, [_I, _I, _I]),
+    "sn_marching_cubes": (_I, [_P, _I, _I, _I, _F, _P, _P, _I64, _I64, _P, _P, _P, _P, _P]),
     "sn_lr_schedule": (_I, [_P, _P, _P, _F, _I, _I, _F, _P]),
     "sn_step_size_schedule": (_I, [_P, C.c_double, C.c_double, _I, _P, _P]),
     "sn_adam_step": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _F, _I, _F, _F, _F, _I, _P]),

@@ -63,11 +63,15 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> Path:
     sources = sorted(CSRC.glob("*.cu"))
     with cf.ThreadPoolExecutor(max_workers=min(len(sources), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), sources))
-    if _stale(LIB, objs):
+    listing = BUILD / "objects.txt"          # relink when a source was added or removed
+    names = "\n".join(o.name for o in objs)
+    changed = not listing.exists() or listing.read_text() != names
+    if changed or _stale(LIB, objs):
         cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        listing.write_text(names)
     if verbose:
         print(f"built {LIB}")
     return LIB

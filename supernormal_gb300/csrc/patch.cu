@@ -175,6 +175,13 @@ __device__ __forceinline__ float transmittance(float v, float& carry, int lane) 
   return T;
 }
 
+// d loss / d w_j of one sample: the rendered-normal gradient along the
+// sample's gradient plus the weight-sum gradient (one expression for every
+// pass, so the passes see the same rounded values).
+__device__ __forceinline__ float weight_grad(const float gc[3], float gws, const float g[3]) {
+  return __fadd_rn(__fmaf_rn(gc[2], g[2], __fmaf_rn(gc[1], g[1], __fmul_rn(gc[0], g[0]))), gws);
+}
+
 // 3x3 patches (288 threads): at least three blocks per SM (72 registers);
 // unbounded, the kernel takes 96 registers and only two blocks fit.
 template <int MODE, int MAXT>
@@ -284,8 +291,8 @@ __global__ void __launch_bounds__(MAXT, MAXT == 288 ? 3 : 1) patch_block_kernel(
     gws = a.g_wsum[p * P + k];
   }
 
-  // ---------------- adjoint: total = sum_j g_w_j w_j ----------------
-  float total = 0.0f;
+  // ---------------- adjoint: total = sum_j g_w_j w_j (double-float) ----------------
+  ff total{0.0f, 0.0f};
   Tc = 1.0f;
   for (int j0 = 0; j0 < steps; j0 += 32) {
     const int j = j0 + lane;
@@ -294,16 +301,17 @@ __global__ void __launch_bounds__(MAXT, MAXT == 288 ? 3 : 1) patch_block_kernel(
     chunk_sample(a, R, base + j, S, inv_s, ok, lane, sm_s0, sm_pos, s);
     const float T = transmittance(ok ? __fsub_rn(1.0f, s.alpha) : 1.0f, Tc, lane);
     const float w = ok ? __fmul_rn(s.alpha, T) : 0.0f;
-    const float gw = gc[0] * s.g[0] + gc[1] * s.g[1] + gc[2] * s.g[2] + gws;
-    total = __fmaf_rn(gw, w, total);
+    const float gw = ok ? weight_grad(gc, gws, s.g) : 0.0f;
+    total = ff_add_f(total, __fmul_rn(gw, w));
   }
-  total = warp_sum(total);
+  total = warp_sum_ff(total);
 
   // ---------------- adjoint per sample ----------------
   const int W = a.W, H = a.H;
   const int kl = R.c > 0 ? k - 1 : k, kr = R.c < W - 1 ? k + 1 : k;
   const int ku = R.r > 0 ? k - W : k, kd = R.r < H - 1 ? k + W : k;
-  float d_inv = 0.0f, prefix = 0.0f, carry_in = 0.0f;
+  float d_inv = 0.0f, carry_in = 0.0f;
+  ff prefix{0.0f, 0.0f};
   Tc = 1.0f;
   for (int j0 = 0; j0 < steps; j0 += 32) {
     const int j = j0 + lane;
@@ -313,17 +321,23 @@ __global__ void __launch_bounds__(MAXT, MAXT == 288 ? 3 : 1) patch_block_kernel(
     chunk_sample(a, R, i, S, inv_s, ok, lane, sm_s0, sm_pos, s);
     const float T = transmittance(ok ? __fsub_rn(1.0f, s.alpha) : 1.0f, Tc, lane);
     const float w = ok ? __fmul_rn(s.alpha, T) : 0.0f;
-    const float gw = ok ? gc[0] * s.g[0] + gc[1] * s.g[1] + gc[2] * s.g[2] + gws : 0.0f;
+    const float gw = ok ? weight_grad(gc, gws, s.g) : 0.0f;
     // accum_j = sum_{i >= j} g_i w_i (NA/nerfacc/cuda/csrc/render_weight.cu:325-337)
-    float incl = __fmul_rn(gw, w);
+    // = total - (sum of earlier chunks + this chunk's exclusive scan), in
+    // double-float so the suffix behind the surface keeps its digits
+    const float gwj = __fmul_rn(gw, w);
+    ff incl{gwj, 0.0f};
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const float y = __shfl_up_sync(kFull, incl, o);
-      if (lane >= o) incl = __fadd_rn(y, incl);
+      const ff y = shfl_up_ff(incl, o);
+      if (lane >= o) incl = ff_add(y, incl);
     }
-    const float accum = __fsub_rn(total, __fadd_rn(prefix, __fsub_rn(incl, __fmul_rn(gw, w))));
-    prefix = __fadd_rn(prefix, __shfl_sync(kFull, incl, 31));
-    const float dalpha = __fdiv_rn(__fmaf_rn(gw, T, -accum), fmaxf(__fsub_rn(1.0f, s.alpha), 1e-10f));
+    ff excl = shfl_up_ff(incl, 1);
+    if (lane == 0) excl = ff{0.0f, 0.0f};
+    const ff accum = ff_add(total, ff_neg(ff_add(prefix, excl)));
+    prefix = ff_add(prefix, shfl_ff(incl, 31));
+    const float num = ff_val(ff_add(two_prod(gw, T), ff_neg(accum)));
+    const float dalpha = __fdiv_rn(num, fmaxf(__fsub_rn(1.0f, s.alpha), 1e-10f));
     // alpha = clip(q): sigmoid terms
     const float dq = (ok && s.q >= 0.0f && s.q <= 1.0f) ? dalpha : 0.0f;
     const float ce = s.cdf0 + 1e-5f;

@@ -15,7 +15,8 @@ import torch
 from torch import Tensor
 
 from ._lib import call, stream_handle
-from .nerfacc import ContractionType, OccupancyGrid, _pack_counts, ray_marching
+from .nerfacc import (ContractionType, OccupancyGrid, _pack_counts, accumulate_along_rays, ray_marching,
+                      render_weight_from_alpha)
 
 __all__ = ["NeuSRenderer", "near_far_from_sphere"]
 
@@ -158,6 +159,45 @@ class NeuSRenderer:
         self.last_samples = (patch_indices, t_s, t_e)
         return self.render_samples(ro, rd, marching_plane_normal, V_inverse_patch_all, patch_indices,
                                    t_s, t_e, gradient_method)
+
+    @torch.no_grad()
+    def render_normal_pixel_based(self, rays_o: Tensor, rays_d: Tensor, near: Tensor, far: Tensor,
+                                  generator=None):
+        """Per-pixel normal and depth rendering for validation
+        (models/renderer.py:278-351): rays (N, 3) marched with stratified
+        jitter and culled at early_stop_eps = 1e-3 with the NeuS alpha of the
+        same alpha_fn, weights per ray, normals from SDFNetwork.gradient at
+        the sample midpoints, then accumulated.  Returns (comp_normal (N, 3),
+        comp_depth (N, 1))."""
+        ro = rays_o.contiguous().float()
+        rd = rays_d.contiguous().float()
+        n_rays = ro.shape[0]
+        alpha_fn = self._center_alpha_fn(ro, rd)
+        ray_indices, t_starts, t_ends = ray_marching(
+            ro, rd, t_min=near.reshape(-1), t_max=far.reshape(-1), grid=self.occupancy_grid,
+            render_step_size=self.sampling_step_size, stratified=True, cone_angle=0.0, alpha_thre=0.0,
+            early_stop_eps=1e-3, alpha_fn=alpha_fn, generator=generator)
+        self.last_samples = (ray_indices, t_starts, t_ends)
+        if ray_indices.numel() == 0:
+            return torch.zeros((n_rays, 3), device=ro.device), torch.zeros((n_rays, 1), device=ro.device)
+        alpha = alpha_fn(t_starts, t_ends, ray_indices)
+        midpoints = (t_starts + t_ends) / 2.0
+        positions = ro[ray_indices] + rd[ray_indices] * midpoints
+        gradients = self.sdf_network.gradient(positions).reshape(-1, 3).detach()
+        weights = render_weight_from_alpha(alpha, ray_indices=ray_indices, n_rays=n_rays)
+        comp_normal = accumulate_along_rays(weights, ray_indices, values=gradients, n_rays=n_rays)
+        comp_depth = accumulate_along_rays(weights, ray_indices, values=midpoints, n_rays=n_rays)
+        return comp_normal, comp_depth
+
+    def extract_geometry(self, bound_min, bound_max, resolution, threshold=0.0):
+        """Mesh of the SDF's zero level set (models/renderer.py:353-358): the
+        lattice of -sdf from the fused field and the device marching cubes;
+        (vertices float64 (V, 3), triangles int64 (T, 3)) numpy arrays."""
+        from .mesh import marching_cubes, sdf_lattice
+
+        u = sdf_lattice(self.sdf_network, bound_min, bound_max, resolution)
+        v, t = marching_cubes(u, threshold, bound_min, bound_max)
+        return v.double().cpu().numpy(), t.long().cpu().numpy()
 
     def render_samples(self, rays_o_patch_all, rays_d_patch_all, marching_plane_normal,
                        V_inverse_patch_all, patch_indices, t_s, t_e, gradient_method="dfd"):

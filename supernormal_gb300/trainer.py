@@ -104,6 +104,7 @@ class FusedTrainer:
                 p.data = v
                 p.grad = gv
                 self.views[name], self.gviews[name] = v, gv
+        self.offsets = offs
         if cfg.precision not in ("fp32", "mixed"):
             raise ValueError(f"precision {cfg.precision!r}: 'fp32' or 'mixed'")
         if cfg.precision == "mixed" and cfg.gradient_method != "dfd":
@@ -419,6 +420,86 @@ class FusedTrainer:
              g["g0"], st)
         call("sn_weightnorm_bwd", self.dout, self.H, v["v1"], v["g1"], self.n1, self.dw1, g["v1"],
              g["g1"], st)
+
+    # ---- checkpoints in the reference's layout (exp_runner.py:298-315) ----
+    # The reference's optimizer is torch.optim.Adam over
+    # list(sdf_network.parameters()) + list(deviation_network.parameters())
+    # (exp_runner.py:89-97): the hash table, then per layer the parameters
+    # weight_norm leaves (bias, weight_g, weight_v), then the variance.
+    _REFERENCE_ORDER = ("table", "b0", "g0", "v0", "b1", "g1", "v1", "variance")
+
+    def _reference_params(self):
+        views = dict(self.views)
+        return [views[k] for k in self._REFERENCE_ORDER]
+
+    def _flat(self, buf: Tensor, name: str) -> Tensor:
+        a, n, shape = self.offsets[name]
+        return buf[a:a + n].view(shape)
+
+    @torch.no_grad()
+    def optimizer_state_dict(self) -> dict:
+        """The torch.optim.Adam state_dict the reference would save: per
+        parameter (in the reference's order) step, exp_avg, exp_avg_sq taken
+        from the flat Adam buffers, and the current learning rate."""
+        params = [p.detach().clone() for p in self._reference_params()]
+        opt = torch.optim.Adam(params, lr=float(self.cfg.learning_rate), betas=(0.9, 0.999), eps=1e-8)
+        steps = int(self.iter_dev.item())
+        if steps > 0:
+            for name, p in zip(self._REFERENCE_ORDER, params):
+                opt.state[p] = {"step": torch.tensor(float(steps)),
+                                "exp_avg": self._flat(self.exp_avg, name).clone(),
+                                "exp_avg_sq": self._flat(self.exp_avg_sq, name).clone()}
+        sd = opt.state_dict()
+        sd["param_groups"][0]["lr"] = float(self.lr_dev.item()) if steps > 0 else float(self.cfg.learning_rate)
+        return sd
+
+    @torch.no_grad()
+    def load_optimizer_state_dict(self, sd: dict) -> None:
+        """Loads a torch.optim.Adam state_dict of the reference's optimizer
+        (validated by torch itself) into the flat Adam buffers; the step
+        count becomes the device iteration counter."""
+        params = [p.detach().clone() for p in self._reference_params()]
+        opt = torch.optim.Adam(params, lr=float(self.cfg.learning_rate))
+        opt.load_state_dict(sd)
+        steps = set()
+        for name, p in zip(self._REFERENCE_ORDER, params):
+            st = opt.state.get(p)
+            if not st:
+                self._flat(self.exp_avg, name).zero_()
+                self._flat(self.exp_avg_sq, name).zero_()
+                continue
+            self._flat(self.exp_avg, name).copy_(st["exp_avg"])
+            self._flat(self.exp_avg_sq, name).copy_(st["exp_avg_sq"])
+            steps.add(int(float(st["step"])))
+        if len(steps) > 1:
+            raise ValueError(f"parameters have different Adam step counts {sorted(steps)}")
+        k = steps.pop() if steps else 0
+        self.iter_dev.fill_(k)
+
+    def state_dict(self) -> dict:
+        """Checkpoint with the reference's keys (exp_runner.py:305-310)."""
+        return {"sdf_network_fine": self.net.state_dict(),
+                "variance_network_fine": self.dev_net.state_dict(),
+                "optimizer": self.optimizer_state_dict(),
+                "iter_step": self.iter_step}
+
+    @torch.no_grad()
+    def load_state_dict(self, ckpt: dict) -> None:
+        """Resumes from a checkpoint of the reference's layout
+        (exp_runner.py:297-303); the parameters are copied into the flat
+        buffers the kernels use (the module tensors stay views of them)."""
+        self.net.load_state_dict(ckpt["sdf_network_fine"])
+        self.dev_net.load_state_dict(ckpt["variance_network_fine"])
+        self.load_optimizer_state_dict(ckpt["optimizer"])
+        self.iter_step = int(ckpt["iter_step"])
+        if self.params_half is not None:
+            self.params_half.copy_(self.params)
+
+    def save_checkpoint(self, path) -> None:
+        torch.save(self.state_dict(), path)
+
+    def load_checkpoint(self, path) -> None:
+        self.load_state_dict(torch.load(path, map_location=self.device))
 
     def check_status(self) -> None:
         v = int(self.status.item())

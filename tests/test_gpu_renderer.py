@@ -149,18 +149,19 @@ class _FixedSdf:
         return self.values[: x.shape[0]], self.ext
 
 
-@pytest.mark.parametrize("method", ["dfd", "ad"])
-def test_patch_adjoint_matches_oracle_on_fixed_sdf(scene, method):
+@pytest.mark.parametrize("method,step", [("dfd", 1.0 / 96), ("ad", 1.0 / 96), ("dfd", 1.0 / 512)])
+def test_patch_adjoint_matches_oracle_on_fixed_sdf(scene, method, step):
     """The fused patch kernel alone: d loss / d sdf (every start and end point),
     d / d variance and, for 'ad', d / d gradients, for a linear loss on all three
     outputs, against float64 autograd of the oracle's patch math on the same
-    float32 sdf values."""
+    float32 sdf values.  The fine step gives rays of several 32-sample chunks
+    (the kernel's transmittance and suffix-sum carries between chunks)."""
     from supernormal_gb300.renderer import NeuSRenderer, near_far_from_sphere
 
     net, var = make()
     r = NeuSRenderer(net, var, gradient_method=method)
     r.occupancy_grid = full_grid()
-    r.sampling_step_size = 1.0 / 96
+    r.sampling_step_size = step
     g = torch.Generator(device="cuda").manual_seed(11)
     ro, rd, pn, vinv, _, _ = scene.gen_random_patches(64, generator=g)
     near, far = near_far_from_sphere(ro[:, 1, 1], rd[:, 1, 1])
@@ -169,6 +170,8 @@ def test_patch_adjoint_matches_oracle_on_fixed_sdf(scene, method):
     pts = r.last_points
     S, P = pidx.shape[0], 9
     assert S > 100
+    if step < 0.005:
+        assert torch.bincount(pidx).max().item() > 96      # several chunks per ray
     vals = net.sdf(pts).detach().clone().requires_grad_(True)
     ext = None
     if method == "ad":
@@ -206,7 +209,7 @@ def _trainer(scene, B=128, **kw):
     return tr, net, var
 
 
-def _check_trainer_step(tr, net, var, batch, method, min_samples):
+def _check_trainer_step(tr, net, var, batch, method, min_samples, table_tol=2e-3):
     """One forward/backward of the fused step against the oracle on the kept
     samples: culling, the four losses and every parameter gradient."""
     ro, rd, pn, vinv, nrm, mask = batch
@@ -235,9 +238,25 @@ def _check_trainer_step(tr, net, var, batch, method, min_samples):
         assert abs(lo[i] - Lr[k].item()) <= 1e-4 * max(abs(Lr[k].item()), 1e-6), (k, lo[i], Lr[k].item())
     names = ["table", "v0", "g0", "b0", "v1", "g1", "b1"]
     rgrads = torch.autograd.grad(Lr["total"], [prm[n] for n in names] + [var_ref])
+    errs = {}
     for n, r in zip(names + ["variance"], rgrads):
         got = cpu(tr.gviews[n])
-        assert grad_err(n, got, r.numpy().reshape(got.shape)) < 2e-3, n
+        errs[n] = grad_err(n, got, r.numpy().reshape(got.shape))
+        if n == "table":
+            errs["table_levels"] = _table_level_errors(net, got, r.numpy())
+    for n in names + ["variance"]:
+        assert errs[n] < table_tol if n == "table" else errs[n] < 2e-3, (n, errs)
+    return errs
+
+
+def _table_level_errors(net, got, ref):
+    """Per-level ||got - ref|| / ||ref|| of the hash-table gradient (F = 2)."""
+    off = net.encoding.level_offsets() * 2
+    out = []
+    for l in range(len(off) - 1):
+        a, b = got[off[l]:off[l + 1]].astype(np.float64), ref[off[l]:off[l + 1]]
+        out.append(float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)))
+    return out
 
 
 @pytest.mark.parametrize("method", ["dfd", "ad"])
@@ -334,3 +353,30 @@ def test_render_with_no_samples_returns_zeros(scene):
     out = r.render(ro, rd, pn, near, far, vinv, mode="eval")
     assert out["gradients"] is None
     assert torch.count_nonzero(out["comp_normal"]) == 0 and torch.count_nonzero(out["weight_sum"]) == 0
+
+
+def test_render_normal_pixel_based_matches_oracle(scene):
+    """NeuSRenderer.render_normal_pixel_based (models/renderer.py:278-351) on a
+    view's pixel rays: normals and depths against the float64 oracle on the
+    samples the marcher kept (early stop 1e-3)."""
+    from supernormal_gb300 import scenes
+    from supernormal_gb300.renderer import NeuSRenderer, near_far_from_sphere
+
+    net, var = make(d_out=1)
+    r = NeuSRenderer(net, var)
+    r.occupancy_grid = full_grid()
+    r.sampling_step_size = 1.0 / 96
+    d, _ = scenes.view_rays(scene.rig, 1, torch.device("cuda"))
+    rd = d[::3, ::3].reshape(-1, 3).contiguous()
+    ro = scene.pose_all[1, :3, 3].expand(rd.shape).contiguous()
+    near, far = near_far_from_sphere(ro, rd)
+    g = torch.Generator(device="cuda").manual_seed(8)
+    comp, depth = r.render_normal_pixel_based(ro, rd, near, far, generator=g)
+    ridx, ts, te = (cpu(t) for t in r.last_samples)
+    assert ridx.size > 500 and comp.shape == (rd.shape[0], 3) and depth.shape == (rd.shape[0], 1)
+    _, fld = oracle_field(net)
+    ref_c, ref_d = OR.pixel_forward(fld, ridx, ts, te, cpu(ro), cpu(rd), var.variance.detach().cpu(), rd.shape[0])
+    assert np.abs(cpu(comp) - ref_c.numpy()).max() < 2e-4
+    assert np.abs(cpu(depth) - ref_d.numpy()).max() < 2e-4
+    hit = cpu(depth)[:, 0] > 0
+    assert hit.sum() > 20 and (np.linalg.norm(cpu(comp)[hit], axis=-1) > 0.5).mean() > 0.9

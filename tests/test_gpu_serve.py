@@ -65,7 +65,9 @@ def test_graph_step_follows_step_size_schedule(built_lib):
         cfg = TrainConfig(batch_size=128, start_step_size=1e-2, end_step_size=1e-3, end_iter=20,
                           occ_update_freq=0, increase_bandwidth_every=0, warm_up_end=2, seed=3)
         net.bindwidth = 16
-        return FusedTrainer(net, var, cfg)
+        tr = FusedTrainer(net, var, cfg)
+        tr.grid._binary = torch.ones_like(tr.grid._binary)   # every cell occupied: no updates needed
+        return tr
 
     g = torch.Generator(device="cuda").manual_seed(1)
     batches = [ds.gen_random_patches(128, generator=g) for _ in range(20)]
