@@ -62,6 +62,13 @@ size_t sn_scan_workspace_bytes(int64_t n);
  * and NA/nerfacc/pack.py:73-75, without a host synchronisation. */
 int sn_pack_counts(int64_t n, const int32_t* counts, int32_t* packed_info,
                    int32_t* total, void* workspace, void* stream);
+/* sn_pack_counts over the first min(*count, cap) entries of a capacity-sized
+ * array (count: device int32): the same packed_info and total there, nothing
+ * read or written past the count, so a fixed-capacity (graph-captured) step
+ * scans only its live entries. */
+int sn_pack_counts_n(int64_t cap, const int32_t* count, const int32_t* counts,
+                     int32_t* packed_info, int32_t* total, void* workspace,
+                     void* stream);
 /* sn_pack_counts that allocates nothing and takes no workspace: the tile sums
  * of the multi-tile scan live in a static device array.  No reference
  * counterpart (the reference's cumsum allocates through torch); it serves
@@ -336,7 +343,8 @@ int sn_weightnorm_bwd(int rows, int cols, const float* v, const float* g,
 /* ---- renderer glue (models/renderer.py:63-276) ----------------------------- */
 /* diff[i] = t_ends[i] != t_starts[i+1] over the flattened samples (the last
  * sample compares with its own start): models/renderer.py:88-93, :151-154.
- * count (nullable, device) bounds cap at run time; diff[count..cap) = 0. */
+ * count (nullable, device) bounds cap at run time; entries past the count
+ * are not written (sn_pack_counts_n scans only below the count). */
 int sn_end_diff(int64_t cap, const int32_t* count, const float* t_starts,
                 const float* t_ends, int32_t* diff, void* stream);
 /* Query points of patch-centre samples for the culling alpha_fn

@@ -85,6 +85,7 @@ SIGNATURES: dict[str, tuple] = {
     "sn_scan_workspace_bytes": (_SZ, [_I64]),
     "sn_pack_counts": (_I, [_I64, _P, _P, _P, _P, _P]),
     "sn_pack_counts_static": (_I, [_I64, _P, _P, _P, _P]),
+    "sn_pack_counts_n": (_I, [_I64, _P, _P, _P, _P, _P, _P]),
     "sn_count_indices": (_I, [_I64, _P, _I64, _P, _P]),
     "sn_unpack_info": (_I, [_I64, _P, _I64, _P, _P]),
     "sn_march_count": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _F, _F, _I64, _P, _P, _P]),

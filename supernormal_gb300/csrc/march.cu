@@ -46,7 +46,13 @@ int num_sms() {
 // Scans each tile, adds the tile offset and writes packed_info = {offset, count}.
 __global__ void __launch_bounds__(kScanThreads)
 scan_tile_apply(const int32_t* __restrict__ in, int64_t n, const int32_t* __restrict__ tile_offsets,
-                int32_t* __restrict__ packed, int32_t* __restrict__ total) {
+                int32_t* __restrict__ packed, int32_t* __restrict__ total,
+                const int32_t* __restrict__ live = nullptr) {
+  if (live) n = min(n, (int64_t)*live);   // entries at or past *live are neither read nor written
+  if ((int64_t)blockIdx.x * kScanTile >= n) {
+    if (!tile_offsets && threadIdx.x == 0 && total) *total = 0;
+    return;
+  }
   const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
   int v[kScanItems], c[kScanItems];
 #pragma unroll
@@ -64,7 +70,7 @@ scan_tile_apply(const int32_t* __restrict__ in, int64_t n, const int32_t* __rest
 }
 
 int pack_counts(int64_t n, const int32_t* counts, int32_t* packed, int32_t* total, void* ws,
-                cudaStream_t st) {
+                cudaStream_t st, const int32_t* live = nullptr) {
   if (n == 0) {
     if (total) {
       if (cudaMemsetAsync(total, 0, sizeof(int32_t), st) != cudaSuccess) {
@@ -76,14 +82,14 @@ int pack_counts(int64_t n, const int32_t* counts, int32_t* packed, int32_t* tota
   }
   const int64_t n_tiles = (n + kScanTile - 1) / kScanTile;
   if (n_tiles == 1) {
-    scan_tile_apply<<<1, kScanThreads, 0, st>>>(counts, n, nullptr, packed, total);
+    scan_tile_apply<<<1, kScanThreads, 0, st>>>(counts, n, nullptr, packed, total, live);
     return check_launch("pack_counts");
   }
   SN_REQUIRE(ws != nullptr, "pack_counts: workspace required for n=%lld", (long long)n);
   int32_t* tiles = reinterpret_cast<int32_t*>(ws);
-  scan_tile_reduce<<<(unsigned)n_tiles, kScanThreads, 0, st>>>(counts, n, tiles);
-  scan_tile_offsets<<<1, kScanThreads, 0, st>>>(tiles, n_tiles, total);
-  scan_tile_apply<<<(unsigned)n_tiles, kScanThreads, 0, st>>>(counts, n, tiles, packed, nullptr);
+  scan_tile_reduce<<<(unsigned)n_tiles, kScanThreads, 0, st>>>(counts, n, tiles, live);
+  scan_tile_offsets<<<1, kScanThreads, 0, st>>>(tiles, n_tiles, total, live, n);
+  scan_tile_apply<<<(unsigned)n_tiles, kScanThreads, 0, st>>>(counts, n, tiles, packed, nullptr, live);
   return check_launch("pack_counts", 3);
 }
 
@@ -762,6 +768,15 @@ int sn_pack_counts(int64_t n, const int32_t* counts, int32_t* packed_info, int32
 // written by scan_tile_reduce before scan_tile_offsets reads it).  The scratch
 // is one per device, so calls that overlap on the device (other streams or
 // host threads) race on it.
+int sn_pack_counts_n(int64_t cap, const int32_t* count, const int32_t* counts, int32_t* packed_info,
+                     int32_t* total, void* workspace, void* stream) {
+  SN_REQUIRE(cap >= 0, "pack_counts_n: cap < 0");
+  SN_REQUIRE(cap <= ((int64_t)1 << 31) - 1, "pack_counts_n: cap too large");
+  SN_REQUIRE(count != nullptr, "pack_counts_n: a device count is required");
+  SN_REQUIRE(cap == 0 || (counts && packed_info), "pack_counts_n: null buffer");
+  return sn::pack_counts(cap, counts, packed_info, total, workspace, as_stream(stream), count);
+}
+
 int sn_pack_counts_static(int64_t n, const int32_t* counts, int32_t* packed_info, int32_t* total,
                           void* stream) {
   SN_REQUIRE(n >= 0, "pack_counts_static: n < 0");

@@ -20,18 +20,14 @@
 
 namespace sn {
 
-// diff[i] = t_ends[i] != t_starts[i+1] (last sample compares with itself);
-// entries in [count, cap) are set to 0.
+// diff[i] = t_ends[i] != t_starts[i+1] (last sample compares with itself)
+// for i < min(*count, cap); entries past the count are not written.
 __global__ void end_diff_kernel(int64_t cap, const int32_t* __restrict__ count,
                                 const float* __restrict__ ts, const float* __restrict__ te,
                                 int32_t* __restrict__ diff) {
   const int64_t n = count ? min((int64_t)*count, cap) : cap;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cap;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    if (i >= n) {
-      diff[i] = 0;  // entries past the live count take part in capacity-sized scans
-      continue;
-    }
     const float nxt = (i + 1 < n) ? ts[i + 1] : ts[i];
     diff[i] = (__fsub_rn(te[i], nxt) != 0.0f) ? 1 : 0;
   }

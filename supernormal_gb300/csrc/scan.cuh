@@ -58,8 +58,15 @@ __device__ int block_exclusive_scan(int (&v)[kScanItems]) {
 }
 
 __global__ void __launch_bounds__(kScanThreads)
-scan_tile_reduce(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ tile_sums) {
+scan_tile_reduce(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ tile_sums,
+                 const int32_t* __restrict__ live = nullptr) {
+  // live (nullable, device): only entries below *live count (the rest read as 0)
+  if (live) n = min(n, (int64_t)*live);
   const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  if ((int64_t)blockIdx.x * kScanTile >= n) {
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = 0;
+    return;
+  }
   int s = 0;
 #pragma unroll
   for (int i = 0; i < kScanItems; ++i)
@@ -77,7 +84,13 @@ scan_tile_reduce(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict_
 
 // Single block: exclusive scan of the tile sums in place; writes the total.
 __global__ void __launch_bounds__(kScanThreads)
-scan_tile_offsets(int32_t* __restrict__ tile_sums, int64_t n_tiles, int32_t* __restrict__ total) {
+scan_tile_offsets(int32_t* __restrict__ tile_sums, int64_t n_tiles, int32_t* __restrict__ total,
+                  const int32_t* __restrict__ live = nullptr, int64_t n = 0) {
+  // live: only the tiles holding entries below min(*live, n) (the rest are 0)
+  if (live) {
+    const int64_t m = min(n, (int64_t)*live);
+    n_tiles = min(n_tiles, (m + kScanTile - 1) / kScanTile);
+  }
   int carry = 0;
   for (int64_t t0 = 0; t0 < n_tiles; t0 += kScanTile) {
     int v[kScanItems];

@@ -366,7 +366,7 @@ class FusedTrainer:
         self._mark("march_end")
         # --- culling: field at centre samples, NeuS alpha, visibility, compaction ---
         call("sn_end_diff", C0, self.total0, self.ts0, self.te0, self.diff, st)
-        call("sn_pack_counts", C0, self.diff, self.endp, self.n_ends, self.scan_ws, st)
+        call("sn_pack_counts_n", C0, self.total0, self.diff, self.endp, self.n_ends, self.scan_ws, st)
         call("sn_center_points", C0, self.total0, self.ridx0, self.ts0, self.te0, self.ro_c,
              self.rd_c, self.endp, self.n_ends, self.xyz0, self.q0, st)
         call("sn_field_fwd", 2 * C0, self.q0, self.xyz0, self._table(), gd, active, mlp, 1, self.sdf0, st)
@@ -379,7 +379,7 @@ class FusedTrainer:
         self._mark("cull_end")
         # --- training points: expansion through the marching plane ---
         call("sn_end_diff", C0, self.S, self.ts1, self.te1, self.diff, st)
-        call("sn_pack_counts", C0, self.diff, self.endp1, self.n_ends1, self.scan_ws, st)
+        call("sn_pack_counts_n", C0, self.S, self.diff, self.endp1, self.n_ends1, self.scan_ws, st)
         call("sn_patch_points", C0, self.S, H, W, self.ridx1, self.ts1, self.te1, rays_o, rays_d,
              plane_n, self.endp1, self.n_ends1, self.xyz1, self.tps, self.tpe, self.q1, st)
         cap1 = 2 * C0 * P

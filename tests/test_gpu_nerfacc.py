@@ -279,3 +279,32 @@ def _grid(nf, binary):
     g = nf.OccupancyGrid(roi_aabb=[-1.0, -1.0, -1.0, 1.0, 1.0, 1.0], resolution=res).cuda()
     g._binary = torch.as_tensor(binary.astype(bool), device="cuda")
     return g
+
+
+@pytest.mark.parametrize("cap,live", [(0, 0), (5000, 0), (5000, 4096), (5000, 5000), (3 * 4096 + 7, 4097),
+                                      (1 << 21, 190_000)])
+def test_pack_counts_bounded_by_device_count(nf, cap, live):
+    """sn_pack_counts_n: the packed prefix and total of the live entries,
+    bit for bit as sn_pack_counts over those entries alone, and nothing
+    written past the count (garbage past it is ignored)."""
+    from supernormal_gb300._lib import call, stream_handle
+
+    g = torch.Generator(device="cuda").manual_seed(cap + live)
+    counts = torch.randint(0, 7, (cap,), dtype=torch.int32, device="cuda", generator=g)
+    if cap > live:
+        counts[live:] = 1 << 20                        # never read
+    ws = torch.empty(int(call("sn_scan_workspace_bytes", max(cap, 1))), dtype=torch.uint8, device="cuda")
+    packed = torch.full((max(cap, 1), 2), -5, dtype=torch.int32, device="cuda")
+    total = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    n_dev = torch.tensor([live], dtype=torch.int32, device="cuda")
+    call("sn_pack_counts_n", cap, n_dev, counts, packed, total, ws, stream_handle())
+    want_p = torch.full((max(live, 1), 2), -5, dtype=torch.int32, device="cuda")
+    want_t = torch.zeros((1,), dtype=torch.int32, device="cuda")
+    if live:
+        call("sn_pack_counts", live, counts[:live].contiguous(), want_p, want_t, ws, stream_handle())
+    torch.cuda.synchronize()
+    assert int(total.item()) == int(want_t.item())
+    if live:
+        assert torch.equal(packed[:live], want_p[:live])
+    if cap > live:
+        assert (packed[live:cap] == -5).all()
