@@ -36,15 +36,29 @@ def diff_mask_of(ts, te):
     return (te - nxt) != 0
 
 
-def center_alpha(field, ridx, ts, te, rays_o_c, rays_d_c, variance, dtype=torch.float64):
-    """alpha_fn_patch_center (models/renderer.py:80-122)."""
+def _f32_points(o, d, t):
+    """o + d * t as the reference forms it on the device: float32 product, then
+    float32 sum (two roundings)."""
+    return (np.asarray(o, np.float32) + (np.asarray(d, np.float32) * np.asarray(t, np.float32)).astype(np.float32)
+            ).astype(np.float32)
+
+
+def center_alpha(field, ridx, ts, te, rays_o_c, rays_d_c, variance, dtype=torch.float64, f32_points=False):
+    """alpha_fn_patch_center (models/renderer.py:80-122).  f32_points: the
+    query points in the reference's float32 arithmetic (so hash cells match a
+    float32 pipeline exactly); else in ``dtype``."""
     ridx = np.asarray(ridx)
     o = torch.as_tensor(np.asarray(rays_o_c, np.float32)[ridx]).to(dtype)
     d = torch.as_tensor(np.asarray(rays_d_c, np.float32)[ridx]).to(dtype)
     tsd = torch.as_tensor(np.asarray(ts, np.float32)).to(dtype).reshape(-1, 1)
     ted = torch.as_tensor(np.asarray(te, np.float32)).to(dtype).reshape(-1, 1)
     diff = torch.as_tensor(diff_mask_of(ts, te))
-    ps, pe = o + d * tsd, o + d * ted
+    if f32_points:
+        o32, d32 = np.asarray(rays_o_c, np.float32)[ridx], np.asarray(rays_d_c, np.float32)[ridx]
+        ps = torch.as_tensor(_f32_points(o32, d32, np.asarray(ts, np.float32).reshape(-1, 1))).to(dtype)
+        pe = torch.as_tensor(_f32_points(o32, d32, np.asarray(te, np.float32).reshape(-1, 1))).to(dtype)
+    else:
+        ps, pe = o + d * tsd, o + d * ted
     sdf = field(torch.cat([ps, pe[diff]], 0))
     n = ps.shape[0]
     s0 = sdf[:n]
@@ -174,17 +188,18 @@ def pixel_forward(field, ridx, ts, te, rays_o, rays_d, variance, n_rays):
     depths.  Returns (comp_normal (n_rays, 3), comp_depth (n_rays, 1))."""
     ridx = np.asarray(ridx, np.int64)
     with torch.no_grad():
-        alpha = center_alpha(field, ridx, ts, te, rays_o, rays_d, variance).numpy()
+        alpha = center_alpha(field, ridx, ts, te, rays_o, rays_d, variance, f32_points=True).numpy()
     packed = nerfacc_ref.pack_info(ridx, n_rays)
     w = nerfacc_ref.weights_fwd(alpha, packed)
-    o = torch.as_tensor(np.asarray(rays_o, np.float32)[ridx]).double()
-    d = torch.as_tensor(np.asarray(rays_d, np.float32)[ridx]).double()
-    mid = (torch.as_tensor(np.asarray(ts, np.float32)).double().reshape(-1, 1)
-           + torch.as_tensor(np.asarray(te, np.float32)).double().reshape(-1, 1)) / 2.0
-    x = (o + d * mid).detach().requires_grad_(True)
+    # midpoints and positions in the reference's float32 arithmetic (:342-345)
+    mid32 = ((np.asarray(ts, np.float32).reshape(-1, 1) + np.asarray(te, np.float32).reshape(-1, 1))
+             .astype(np.float32) / np.float32(2.0)).astype(np.float32)
+    mid = torch.as_tensor(mid32).double()
+    x32 = _f32_points(np.asarray(rays_o, np.float32)[ridx], np.asarray(rays_d, np.float32)[ridx], mid32)
+    x = torch.as_tensor(x32).double().requires_grad_(True)
     (g,) = torch.autograd.grad(field(x).sum(), x)
     wt = torch.as_tensor(w).reshape(-1, 1)
     idx = torch.as_tensor(ridx)
     comp = torch.zeros((n_rays, 3), dtype=torch.float64).index_add(0, idx, wt * g)
     depth = torch.zeros((n_rays, 1), dtype=torch.float64).index_add(0, idx, wt * mid)
-    return comp, depth
+    return comp, depth, {"alpha": alpha, "weights": w, "gradients": g.detach()}

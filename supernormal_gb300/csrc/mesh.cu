@@ -21,8 +21,9 @@
 // share the face, so no cracks), the face segments are oriented from the
 // crossing where the face boundary (counter-clockwise around the outward
 // normal) enters the inside to the next crossing where it leaves, the
-// segments chain into closed loops, and each loop is fanned into triangles,
-// whose right-hand normals then point from the inside to the outside.
+// segments chain into closed loops, and each loop is fanned into triangles
+// from a vertex none of whose diagonals lies on a cube face; the right-hand
+// normals then point from the inside to the outside.
 #include "common.cuh"
 #include "scan.cuh"
 
@@ -41,6 +42,13 @@ struct McTable {
 
 constexpr int mc_edge_of(int c0, int axis) {
   return axis == 0 ? ((c0 >> 1) & 3) : axis == 1 ? (4 + ((c0 & 1) | (((c0 >> 2) & 1) << 1))) : (8 + (c0 & 3));
+}
+
+// Faces of the cube edge e as a 6-bit mask (bit 2 * axis + side).
+constexpr int mc_edge_faces(int e) {
+  const int axis = e >> 2, o = e & 3;
+  const int x0 = axis == 0 ? 1 : 0, x1 = axis == 2 ? 1 : 2;  // the other two axes, low first
+  return (1 << (2 * x0 + (o & 1))) | (1 << (2 * x1 + ((o >> 1) & 1)));
 }
 
 constexpr McTable make_mc_table() {
@@ -94,10 +102,25 @@ constexpr McTable make_mc_table() {
         seen[e] = true;
         loop[n++] = e;
       }
+      // fan apex: a vertex none of whose diagonals lies on a cube face, so no
+      // diagonal can coincide with one of the neighbouring cube's (such a pair
+      // would make the edge shared by four triangles); every loop has one
+      int ap = 0;
+      for (int c = 0; c < n; ++c) {
+        bool good = true;
+        for (int j = 0; j < n; ++j)
+          if (j != c && j != (c + 1) % n && j != (c + n - 1) % n &&
+              (mc_edge_faces(loop[c]) & mc_edge_faces(loop[j])) != 0)
+            good = false;
+        if (good) {
+          ap = c;
+          break;
+        }
+      }
       for (int i = 1; i + 1 < n; ++i) {
-        t.edge[cs][3 * nt + 0] = (int8_t)loop[0];
-        t.edge[cs][3 * nt + 1] = (int8_t)loop[i];
-        t.edge[cs][3 * nt + 2] = (int8_t)loop[i + 1];
+        t.edge[cs][3 * nt + 0] = (int8_t)loop[ap];
+        t.edge[cs][3 * nt + 1] = (int8_t)loop[(ap + i) % n];
+        t.edge[cs][3 * nt + 2] = (int8_t)loop[(ap + i + 1) % n];
         ++nt;
       }
     }

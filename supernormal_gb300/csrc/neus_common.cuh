@@ -27,7 +27,8 @@ __device__ __forceinline__ float neus_alpha(float s0, float s1, float inv_s, flo
   return fminf(fmaxf(q, 0.0f), 1.0f);
 }
 
-// Double-float (hi + lo) sums for the adjoint's suffix sums over long rays.
+// Double-float (hi + lo) arithmetic for the transmittance product and the
+// adjoint's suffix sums over long rays.
 // sum_{i >= j} g_i w_i is formed as total - prefix, which in float32 loses
 // everything below eps * |total| exactly where the suffix is small (behind the
 // surface); carrying the rounding errors (Knuth's TwoSum) keeps it to
@@ -55,6 +56,13 @@ __device__ __forceinline__ float ff_val(ff x) { return __fadd_rn(x.hi, x.lo); }
 __device__ __forceinline__ ff two_prod(float a, float b) {
   const float p = __fmul_rn(a, b);
   return ff{p, __fmaf_rn(a, b, -p)};
+}
+// (x.hi + x.lo)(y.hi + y.lo) to double-float precision (the lo * lo term dropped).
+__device__ __forceinline__ ff ff_mul(ff x, ff y) {
+  const ff p = two_prod(x.hi, y.hi);
+  const float e = __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, p.lo));
+  const float h = __fadd_rn(p.hi, e);
+  return ff{h, __fsub_rn(e, __fsub_rn(h, p.hi))};
 }
 __device__ __forceinline__ ff shfl_ff(ff v, int src) {
   return ff{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};

@@ -67,6 +67,10 @@ def test_random_field_is_watertight(seed):
     assert len(v) == len(ref) and len(t) > 100
     np.testing.assert_allclose(v[np.lexsort(v.T)], ref[np.lexsort(ref.T)], atol=2e-5)
     _topology(v, t)
+    # the host restatement numbers vertices the same way: identical triangles
+    hv, ht = OMS.marching_cubes(u, 0.0, (0, 0, 0), (23, 19, 17))
+    np.testing.assert_array_equal(t, ht)
+    np.testing.assert_allclose(v, hv, atol=2e-5)
 
 
 def test_empty_and_capacity():

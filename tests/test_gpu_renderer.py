@@ -375,8 +375,17 @@ def test_render_normal_pixel_based_matches_oracle(scene):
     ridx, ts, te = (cpu(t) for t in r.last_samples)
     assert ridx.size > 500 and comp.shape == (rd.shape[0], 3) and depth.shape == (rd.shape[0], 1)
     _, fld = oracle_field(net)
-    ref_c, ref_d = OR.pixel_forward(fld, ridx, ts, te, cpu(ro), cpu(rd), var.variance.detach().cpu(), rd.shape[0])
-    assert np.abs(cpu(comp) - ref_c.numpy()).max() < 2e-4
-    assert np.abs(cpu(depth) - ref_d.numpy()).max() < 2e-4
+    ref_c, ref_d, parts = OR.pixel_forward(fld, ridx, ts, te, cpu(ro), cpu(rd), var.variance.detach().cpu(),
+                                           rd.shape[0])
+    # the pieces: alpha of the same alpha_fn, weights, gradients at the midpoints
+    ri_t = r.last_samples[0]
+    alpha = r._center_alpha_fn(ro, rd)(r.last_samples[1], r.last_samples[2], ri_t)
+    mid = (r.last_samples[1] + r.last_samples[2]) / 2.0
+    grads = net.gradient(ro[ri_t] + rd[ri_t] * mid).reshape(-1, 3).detach()
+    errs = {"alpha": np.abs(cpu(alpha).ravel() - parts["alpha"]).max(),
+            "gradients": np.abs(cpu(grads) - parts["gradients"].numpy()).max() / np.abs(parts["gradients"].numpy()).max(),
+            "normal": np.abs(cpu(comp) - ref_c.numpy()).max(), "depth": np.abs(cpu(depth) - ref_d.numpy()).max()}
+    assert errs["alpha"] < 1e-5 and errs["gradients"] < 1e-5, errs
+    assert errs["normal"] < 2e-4 * max(1.0, np.abs(ref_c.numpy()).max()) and errs["depth"] < 2e-4, errs
     hit = cpu(depth)[:, 0] > 0
     assert hit.sum() > 20 and (np.linalg.norm(cpu(comp)[hit], axis=-1) > 0.5).mean() > 0.9
