@@ -201,13 +201,30 @@ struct GridView {
   int res[3];
   const uint8_t* bits;
   int ctype;
+  float ext[3], rext[3], rres[3];  // extent; exact reciprocals of extent and resolution, or 0
 };
+
+// 1/v when v is a normal power of two (then x * (1/v) rounds exactly as x / v,
+// both being the correctly rounded value of the same real number), else 0.
+__device__ __forceinline__ float pow2_recip(float v) {
+  const uint32_t b = __float_as_uint(v);
+  const uint32_t e = (b >> 23) & 0xFFu;
+  const bool p2 = (b & 0x807FFFFFu) == 0u && e >= 1u && e <= 253u;
+  return p2 ? __uint_as_float((254u - e) << 23) : 0.0f;
+}
+// x / v, as a multiplication when r = pow2_recip(v) is nonzero (same bits).
+__device__ __forceinline__ float div_by(float x, float v, float r) {
+  return r != 0.0f ? __fmul_rn(x, r) : __fdiv_rn(x, v);
+}
 
 __device__ __forceinline__ void load_roi(GridView& g) {
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     g.lo[d] = g.roi[d];
     g.hi[d] = g.roi[3 + d];
+    g.ext[d] = __fsub_rn(g.hi[d], g.lo[d]);
+    g.rext[d] = pow2_recip(g.ext[d]);
+    g.rres[d] = pow2_recip((float)g.res[d]);
   }
 }
 
@@ -215,7 +232,7 @@ __device__ __forceinline__ void load_roi(GridView& g) {
 // (NA/nerfacc/cuda/csrc/include/helpers_contraction.h:16-114).
 __device__ __forceinline__ void contract(const GridView& g, const float p[3], float u[3]) {
 #pragma unroll
-  for (int d = 0; d < 3; ++d) u[d] = __fdiv_rn(__fsub_rn(p[d], g.lo[d]), __fsub_rn(g.hi[d], g.lo[d]));
+  for (int d = 0; d < 3; ++d) u[d] = div_by(__fsub_rn(p[d], g.lo[d]), g.ext[d], g.rext[d]);
   if (g.ctype == SN_CONTRACTION_UN_BOUNDED_TANH) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) u[d] = __fmaf_rn(tanhf(__fsub_rn(u[d], 0.5f)), 0.5f, 0.5f);
@@ -264,11 +281,11 @@ __device__ __forceinline__ float advance_voxel(const GridView& g, float t, float
   float tx[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const float ext = __fsub_rn(g.hi[d], g.lo[d]);
+    const float ext = g.ext[d];
     const float res = (float)g.res[d];
-    const float xu = __fmul_rn(__fdiv_rn(__fsub_rn(p[d], g.lo[d]), ext), res);
+    const float xu = __fmul_rn(div_by(__fsub_rn(p[d], g.lo[d]), ext, g.rext[d]), res);
     const float f = floorf(__fadd_rn(__fadd_rn(xu, 0.5f), copysignf(0.5f, dir[d])));
-    tx[d] = __fmul_rn(__fdiv_rn(__fmul_rn(__fsub_rn(f, xu), inv[d]), res), ext);
+    tx[d] = __fmul_rn(div_by(__fmul_rn(__fsub_rn(f, xu), inv[d]), res, g.rres[d]), ext);
   }
   float dist = fminf(fminf(tx[0], tx[1]), tx[2]);
   dist = fmaxf(dist, 0.0f);
@@ -320,6 +337,9 @@ struct MarchArgs {
 // fixed slots ray*slot_stride (padded; num_steps written too).
 // CONE false: cone_angle == 0, where calc_dt(t) = clamp(t * 0, dt_min, dt_max)
 // is dt_min for every t, so each speculative step is one addition.
+// Lanes that speculate on consecutive DDA skips through empty space.
+constexpr int kSkipLanes = 16;
+
 template <int MODE, bool CONE>  // MODE: 0 count, 1 fill packed, 2 fill padded
 __global__ void __launch_bounds__(128) march_warp_kernel(MarchArgs a, int64_t slot_stride) {
   const auto step_dt = [&](float t, float cone, float lo, float hi) {
@@ -434,6 +454,64 @@ __global__ void __launch_bounds__(128) march_warp_kernel(MarchArgs a, int64_t sl
       if (!(ntm < far)) break;
       // the sequential loop re-tests occupancy at ntm from state (t0, t1):
       // the next speculation round starts there (its lane 0 is that test)
+      if (m == 0 && g.ctype == SN_CONTRACTION_AABB) {
+        // Empty space (the round's first position was empty): speculate on
+        // the skips instead.  Lane l takes l further DDA skips from ntm, each
+        // from the position the previous one reached, as the sequential loop
+        // would if every one of them were empty; all lanes then test their
+        // positions in one round trip.  The first lane that is occupied, or
+        // past far, is where the sequential loop stops skipping, so every
+        // state formed here is the sequential one.
+        bool finished = false;
+        float base_tm = ntm;
+        while (true) {
+          float tm_l = base_tm;
+          for (int s = 1; s < kSkipLanes; ++s) {
+            if (lane >= s && tm_l < far) {
+              float q[3];
+#pragma unroll
+              for (int k = 0; k < 3; ++k) q[k] = __fmaf_rn(tm_l, d[k], o[k]);
+              tm_l = advance_voxel(g, tm_l, dt_min, q, d, inv, far);
+            }
+          }
+          const bool in = lane < kSkipLanes && tm_l < far;
+          bool oc = false;
+          if (in) {
+            float q[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) q[k] = __fmaf_rn(tm_l, d[k], o[k]);
+            oc = occupied_at(g, q);
+          }
+          const unsigned stop = __ballot_sync(0xffffffffu, lane < kSkipLanes && (oc || !in));
+          if (stop) {
+            const int k = __ffs(stop) - 1;
+            const float tk = __shfl_sync(0xffffffffu, tm_l, k);
+            iters += k;
+            if (!(tk < far)) {
+              finished = true;
+            } else {
+              const float ndt = step_dt(tk, a.cone, dt_min, dt_max);
+              t0 = __fsub_rn(tk, __fmul_rn(ndt, 0.5f));
+              t1 = __fadd_rn(tk, __fmul_rn(ndt, 0.5f));
+              tm0 = tk;   // occupied: the next round's lane 0 emits there
+            }
+            break;
+          }
+          // all kSkipLanes positions empty and before far: skip on from the last
+          const float tl = __shfl_sync(0xffffffffu, tm_l, kSkipLanes - 1);
+          float q[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) q[k] = __fmaf_rn(tl, d[k], o[k]);
+          base_tm = advance_voxel(g, tl, dt_min, q, d, inv, far);
+          iters += kSkipLanes;
+          if (!(base_tm < far)) {
+            finished = true;
+            break;
+          }
+          if (iters > a.max_iters) break;
+        }
+        if (finished) break;
+      }
     }
     if (iters > a.max_iters) {
       limit = true;
