@@ -91,8 +91,8 @@ def parse(argv=None):
                    help="time eager launches instead of CUDA-graph replays of each iteration")
     p.add_argument("--no-encoding-cache", action="store_true",
                    help="field backward recomputes the encoding instead of reading the forward's")
-    p.add_argument("--serve", choices=["small", "full", "off"], default="small",
-                   help="serving-loop trace after the training measurement (p50/p99 latency)")
+    p.add_argument("--serve", choices=["small", "full", "off"], default="full",
+                   help="serving-loop trace after the training measurement (p50/p99 latency); full: 32 objects")
     p.add_argument("--quality", action="store_true",
                    help="instead of the throughput run: FP32 vs mixed precision reconstruction quality "
                         "on the sphere scene (angular error, mask IoU, Chamfer / F@0.01)")
@@ -457,9 +457,10 @@ def run_quality(iters: int, dev) -> dict:
 
 
 def run_serve(size: str, dev) -> dict:
-    """The serving loop on a seeded request trace, served (CUDA graphs, short
-    requests between reconstruction slices) and plain (one request at a time,
-    eager), under an HBM budget that forces offloads."""
+    """The serving loop on a seeded request trace under an HBM budget that
+    forces offloads: served (mixed precision, CUDA-graph reconstruction
+    slices on one stream, render / query requests on a second, ordered per
+    object) against plain (FP32, one request at a time, eager)."""
     from supernormal_gb300.serve import ServedObject, Server, object_specs, poisson_trace
 
     if size == "full":   # 32 objects, 8-100 views at 256^2-1024^2, tables 2^17-2^21
@@ -480,11 +481,16 @@ def run_serve(size: str, dev) -> dict:
                       "recon_block_iterations": 100, "query_grid": 256, "arrival_rate_per_s": cfg["rate"],
                       "trace_s": cfg["duration"], "requests": len(trace),
                       "hbm_budget_gb": budget / 1e9, "objects_total_gb": total / 1e9,
-                      "setup_s": setup_s}}
+                      "setup_s": setup_s,
+                      "served": "mixed precision (FP16 table copy, one-pass TF32 MLP), graph replays, "
+                                "requests on a second stream beside reconstruction slices",
+                      "plain": "FP32, eager, one request at a time"}}
     # capacity: a saturating burst of the same request mix (rays/s over its makespan)
     burst = poisson_trace(len(objs), 2.0, 40.0, seed=13, recon_iters=100)
     out["config"]["burst_requests"] = len(burst)
     for policy in ("served", "plain"):
+        for o in objs:
+            o.set_precision("mixed" if policy == "served" else "fp32")
         srv = Server(objs, budget, query_res=256, slice_iters=10)
         srv.fit_budget()
         r = srv.run(trace, policy)

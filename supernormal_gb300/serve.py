@@ -17,18 +17,23 @@ memory, every storage shrunk to zero bytes) to make room, and brought back on
 their next request.  Two service policies run the same trace:
 
 * ``plain``  -- one request at a time in arrival order, eager launches;
-* ``served`` -- training iterations replayed as CUDA graphs, and render /
-  query requests served between iterations of a running reconstruction block
-  (the block is resumed afterwards), so short requests do not wait behind
-  long blocks.
+* ``served`` -- training iterations replayed as CUDA graphs in slices on a
+  reconstruction stream, and render / query requests on a second stream, so
+  a short request is admitted while a reconstruction block is on the GPU and
+  runs alongside it instead of waiting behind it.
 
-Latency = completion (after a device synchronisation) minus arrival.
+Ordering across the two streams is per object: every piece of work of an
+object (its onload copies included) waits for the event its previous work
+recorded and records a new one, and an object is offloaded only after the
+host has waited for that event.  Latency = completion of the request's own
+work (its object's event) minus arrival.
 """
 from __future__ import annotations
 
 import math
 import time
 from collections import deque
+from contextlib import contextmanager
 from dataclasses import dataclass
 from typing import Optional
 
@@ -65,8 +70,10 @@ def object_specs(n_objects: int, seed: int = 0, views=(8, 100), res=(256, 1024),
 class ServedObject:
     """One reconstruction: dataset views, field, optimiser state, occupancy grid."""
 
-    def __init__(self, spec: ObjectSpec, device, batch: int = 512, step_size: float = 2.0 / 1024):
+    def __init__(self, spec: ObjectSpec, device, batch: int = 512, step_size: float = 2.0 / 1024,
+                 precision: str = "fp32"):
         self.spec = spec
+        self.ready = None   # event after the object's last enqueued work (None: nothing pending)
         dev = torch.device(device)
         scene = scenes.random_scene(spec.seed)
         rig = scenes.ring_cameras(spec.n_views, spec.res, spec.res, radius=3.0, elevation_deg=20.0)
@@ -81,7 +88,7 @@ class ServedObject:
         # would more than double an object's device footprint
         cfg = TrainConfig(batch_size=batch, step_size=step_size, occ_update_freq=8, occ_warmup_steps=16,
                           increase_bandwidth_every=100, end_iter=5000, seed=spec.seed,
-                          encoding_cache=False)
+                          encoding_cache=False, precision=precision)
         self.tr = FusedTrainer(net, var, cfg, device=dev)
         self.graph = GraphStep(self.tr)
         self.renderer = NeuSRenderer(net, var)
@@ -126,7 +133,9 @@ class ServedObject:
     def offload(self) -> None:
         if not self.resident:
             return
-        torch.cuda.synchronize()
+        if self.ready is not None:
+            self.ready.synchronize()      # the object's own work, whichever stream ran it
+        torch.cuda.current_stream().synchronize()
         for i, st in enumerate(self._state):
             if i not in self._host:     # pinned once per object, reused by every offload
                 self._host[i] = torch.empty(st.nbytes(), dtype=torch.uint8, pin_memory=True)
@@ -150,8 +159,24 @@ class ServedObject:
         self.graph.invalidate()
         self.resident = True
 
+    def set_precision(self, precision: str) -> None:
+        """Precision of the object's next training iterations (applied when it
+        next trains, resident: the FP16 table copy is formed then)."""
+        self._want_precision = precision
+
+    def _apply_precision(self) -> None:
+        want = getattr(self, "_want_precision", None)
+        if want is None or want == self.tr.cfg.precision:
+            return
+        self.tr.set_precision(want)
+        self.graph.invalidate()
+        self._state, self._work = self._classify()
+        self._sizes = [st.nbytes() for st in self._state], [st.nbytes() for st in self._work]
+        self._nbytes = sum(self._sizes[0]) + sum(self._sizes[1])
+
     # ---- requests --------------------------------------------------------
     def train_iterations(self, n: int, graphs: bool) -> None:
+        self._apply_precision()
         for _ in range(n):
             batch = self.ds.gen_random_patches(self.tr.B, generator=self.gen)
             if graphs:
@@ -244,13 +269,41 @@ class Server:
         self.query_res = query_res
         self.slice_iters = slice_iters
         self.swaps = 0
+        self.device = sync is None
         self.sync = torch.cuda.synchronize if sync is None else sync
-        if sync is None:
+        if self.device:
             self.mark = self._record_event
             self.wait = lambda ev: ev.synchronize()
+            self.recon_stream = torch.cuda.Stream()
+            self.req_stream = torch.cuda.Stream()
         else:                     # host-only tests: no device work to wait for
             self.mark = lambda: None
             self.wait = lambda ev: None
+            self.recon_stream = self.req_stream = None
+
+    @contextmanager
+    def on(self, obj, stream):
+        """Runs the enclosed work of ``obj`` on ``stream`` (None: the current
+        stream) after the object's previous work, on any stream, and records
+        the object's new event."""
+        if not self.device:
+            yield
+            return
+        stream = stream if stream is not None else torch.cuda.current_stream()
+        with torch.cuda.stream(stream):
+            if getattr(obj, "ready", None) is not None:
+                stream.wait_event(obj.ready)
+            yield
+            ev = torch.cuda.Event()
+            ev.record(stream)
+            obj.ready = ev
+
+    def done(self, obj) -> None:
+        """Host waits for the object's last work (not for the other stream)."""
+        if not self.device:
+            self.sync()
+        elif getattr(obj, "ready", None) is not None:
+            obj.ready.synchronize()
 
     @staticmethod
     def _record_event():
@@ -307,8 +360,8 @@ class Server:
                 else:
                     short_q.append(r)
 
-        def finish(r):
-            self.sync()
+        def finish(r, obj):
+            self.done(obj)
             r.done_at = now()
 
         while pending or recon_q or short_q or fifo:
@@ -322,30 +375,33 @@ class Server:
                 continue
             s = now()
             obj = self.objects[r.obj]
-            self.admit(obj, s)
-            if r.kind == "recon":
-                k = r.iters if policy == "plain" else min(r.iters, self.slice_iters)
-                obj.train_iterations(k, graphs)
-                r.iters -= k
-                train_rays += k * obj.tr.B * obj.tr.P
-                if r.iters == 0:
-                    finish(r)
-                    if policy != "plain":
-                        recon_q.popleft()
-                elif policy != "plain":
-                    # a slice ends without a device sync (the host looks at new
-                    # arrivals while the GPU works), but at most two slices are
-                    # queued: a short request never waits behind a longer backlog
-                    slice_done.append(self.mark())
-                    if len(slice_done) > 2:
-                        self.wait(slice_done.pop(0))
-            elif r.kind == "render":
-                img = obj.render(pose_seed=r.rid)
-                render_rays += img.shape[0] * img.shape[1]
-                finish(r)
+            if policy == "plain":
+                stream = None                    # the current stream, one request at a time
             else:
-                obj.query(self.query_res)
-                finish(r)
+                stream = self.recon_stream if r.kind == "recon" else self.req_stream
+            with self.on(obj, stream):
+                self.admit(obj, s)
+                if r.kind == "recon":
+                    k = r.iters if policy == "plain" else min(r.iters, self.slice_iters)
+                    obj.train_iterations(k, graphs)
+                    r.iters -= k
+                    train_rays += k * obj.tr.B * obj.tr.P
+                    if r.iters > 0 and policy != "plain":
+                        # a slice ends without a host wait (the host looks at new
+                        # arrivals while the GPU works), but at most two slices are
+                        # queued on the reconstruction stream
+                        slice_done.append(self.mark())
+                        if len(slice_done) > 2:
+                            self.wait(slice_done.pop(0))
+                elif r.kind == "render":
+                    img = obj.render(pose_seed=r.rid)
+                    render_rays += img.shape[0] * img.shape[1]
+                else:
+                    obj.query(self.query_res)
+            if r.kind != "recon" or r.iters == 0:
+                finish(r, obj)
+                if r.kind == "recon" and policy != "plain":
+                    recon_q.popleft()
             busy += now() - s
         span = now()
         lat = {k: sorted(r.done_at - r.arrival for r in reqs if r.kind == k) for k in ("recon", "render", "query")}

@@ -421,6 +421,19 @@ class FusedTrainer:
         call("sn_weightnorm_bwd", self.dout, self.H, v["v1"], v["g1"], self.n1, self.dw1, g["v1"],
              g["g1"], st)
 
+    def set_precision(self, precision: str) -> None:
+        """Switch between the FP32 field ('fp32') and the FP16 table copy with
+        one-pass TF32 MLP products ('mixed'); the copy is formed from the FP32
+        master weights (captured iterations must be re-captured)."""
+        if precision not in ("fp32", "mixed"):
+            raise ValueError(f"precision {precision!r}: 'fp32' or 'mixed'")
+        if precision == self.cfg.precision:
+            return
+        if precision == "mixed" and self.cfg.gradient_method != "dfd":
+            raise NotImplementedError("mixed precision is built for the dfd gradient path")
+        self.cfg.precision = precision
+        self.params_half = self.params.to(torch.float16) if precision == "mixed" else None
+
     # ---- checkpoints in the reference's layout (exp_runner.py:298-315) ----
     # The reference's optimizer is torch.optim.Adam over
     # list(sdf_network.parameters()) + list(deviation_network.parameters())

@@ -217,9 +217,10 @@ def test_serving_loop_small_trace(built_lib):
 
 def test_requests_same_alone_and_in_the_mix(built_lib):
     """A render (its stratified jitter seeded by the request) and an SDF query
-    give bit-identical results alone and interleaved with another object's
-    training slices, as the served policy runs them; training with those
-    requests interleaved matches training alone (atomics order aside)."""
+    give bit-identical results alone and running on the request stream while
+    another object's training slices run on the reconstruction stream, as the
+    served policy runs them; training with those requests alongside matches
+    training alone (atomics order aside)."""
     from supernormal_gb300.serve import ServedObject, object_specs
 
     specs = object_specs(2, seed=3, views=(6, 6), res=(96, 96), log2_table=(15, 15))
@@ -233,12 +234,19 @@ def test_requests_same_alone_and_in_the_mix(built_lib):
     for _ in range(3):
         b_alone.train_iterations(4, True)
         la.append(b_alone.tr.loss_out.clone())
-    for i in range(3):                        # slices of b with a's requests between them
-        b.train_iterations(4, True)
-        lb.append(b.tr.loss_out.clone())
+    # as the served policy runs them: b's slices on the reconstruction stream,
+    # a's requests on the request stream, concurrently on the device
+    from supernormal_gb300.serve import Server
+
+    srv = Server([a, b], budget_bytes=1 << 50)
+    for i in range(3):
+        with srv.on(b, srv.recon_stream):
+            b.train_iterations(4, True)
+            lb.append(b.tr.loss_out.clone())
         if i == 0:
-            img_mix = a.render(pose_seed=7)
-            q_mix = a.query(48)
+            with srv.on(a, srv.req_stream):
+                img_mix = a.render(pose_seed=7)
+                q_mix = a.query(48)
     torch.cuda.synchronize()
     assert torch.equal(img_alone, img_mix)
     assert torch.equal(q_alone, q_mix)
