@@ -18,13 +18,16 @@ def _mc(u, thr=0.0, lo=(-1.0, -1.0, -1.0), hi=(1.0, 1.0, 1.0)):
     return v.double().cpu().numpy(), t.long().cpu().numpy()
 
 
-def _topology(v, t):
+def _topology(v, t, closed=True):
     e = np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]])
     directed = {tuple(x) for x in e.tolist()}
     assert len(directed) == len(e), "a directed edge appears twice: inconsistent orientation"
     und = np.sort(e, axis=1)
     _, cnt = np.unique(und, axis=0, return_counts=True)
-    assert (cnt == 2).all(), "open or non-manifold edges"
+    if closed:
+        assert (cnt == 2).all(), "open or non-manifold edges"
+    else:                                  # cut by the lattice's box: boundary edges once
+        assert (cnt <= 2).all(), "non-manifold edges"
     return len(v) - len(cnt) + len(t)     # Euler characteristic
 
 
@@ -123,4 +126,6 @@ def test_sdf_network_extract_geometry_matches_oracle_lattice(built_lib):
     assert v.dtype == np.float64 and t.dtype == np.int64 and len(t) > 100
     crossing = OMS.edge_crossings(u, 0.0, lo.numpy(), hi.numpy())
     assert len(v) == len(crossing)
-    _topology(v, t)
+    _topology(v, t, closed=False)         # this field's zero set reaches the box
+    hv, ht = OMS.marching_cubes(u, 0.0, lo.numpy(), hi.numpy())
+    np.testing.assert_array_equal(t, ht)
