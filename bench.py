@@ -84,6 +84,8 @@ def parse(argv=None):
     p.add_argument("--no-quality", action="store_true", help="skip the held-out-view quality evaluation")
     p.add_argument("--no-reference-kernels", action="store_true",
                    help="skip timing the reference's own marcher / patch-weight kernels")
+    p.add_argument("--no-ad", action="store_true",
+                   help="skip timing the iteration with the 'ad' gradient method")
     p.add_argument("--no-clocks", action="store_true")
     p.add_argument("--precision", choices=["fp32", "mixed"], default="fp32",
                    help="mixed: FP16 hash-table copy and one-pass TF32 MLP products (config 3's path)")
@@ -405,6 +407,8 @@ def run_ours(args, world, rank, local):
         out["clocks"] = clk
     if not args.no_reference_kernels:
         out["kernels_vs_reference"] = reference_kernels_leg(tr, pool[0])
+    if not args.no_ad and tr.cfg.precision == "fp32":
+        out["ad_step"] = ad_step_leg(args, tr, pool)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, budget_s=20.0)
     if args.serve != "off":
@@ -412,6 +416,41 @@ def run_ours(args, world, rank, local):
         torch.cuda.empty_cache()
         out["serve"] = run_serve(args.serve, dev)
     return out
+
+
+def ad_step_leg(args, tr, pool, steps: int = 10) -> dict:
+    """The same iteration with the gradients of the normals from
+    SDFNetwork.gradient (the reference's 'ad' method, models/renderer.py:225-226)
+    instead of dfd, on the trained state: the field's first- and second-order
+    adjoint kernels run as well.  CUDA-graph replays, CUDA events."""
+    from supernormal_gb300.trainer import FusedTrainer, GraphStep, TrainConfig
+
+    c = tr.cfg
+    cfg = TrainConfig(batch_size=c.batch_size, step_size=c.step_size, occ_update_freq=c.occ_update_freq,
+                      occ_threshold=c.occ_threshold, increase_bandwidth_every=0, end_iter=c.end_iter, seed=c.seed,
+                      gradient_method="ad", encoding_cache=tr.enc_cache is not None)
+    tr_ad = FusedTrainer(tr.net, tr.dev_net, cfg, occupancy_grid=tr.grid, device=tr.device)
+    tr_ad.iter_step = tr.iter_step
+    gs = GraphStep(tr_ad, profile=True)
+    gs.prepare()
+    for i in range(3):
+        gs.step(pool[i % len(pool)])
+    gs.flush()
+    gs.stage_marks.clear()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(steps):
+        gs.step(pool[i % len(pool)])
+    e1.record()
+    torch.cuda.synchronize()
+    tr_ad.check_status()
+    gs.flush()
+    ms = e0.elapsed_time(e1) / steps
+    st = stage_times([m for step in gs.stage_marks for m in step])
+    return {"ms_per_step": ms, "rays_per_s": args.batch * tr.P / (ms / 1e3), "steps": steps,
+            "stages_ms_per_step": {k: v / steps for k, v in st.items()},
+            "gradient_method": "ad (SDFNetwork.gradient with the second-order adjoint)"}
 
 
 def run_quality(iters: int, dev) -> dict:
