@@ -305,6 +305,24 @@ int sn_field_fwd(int64_t n, const int32_t* count, const float* x,
                  const float* table, const sn_grid_desc* grid,
                  int active_levels, const sn_mlp_desc* mlp, int out_cols,
                  float* out, void* stream);
+/* Several objects' field forwards in one launch: segment i evaluates its n
+ * points x (n, 3) with its own table, level geometry, active levels and MLP
+ * into out (n, out_cols), as sn_field_fwd would (same kernels, same values;
+ * no device count, no encoding cache).  The persistent CTAs stage each
+ * segment's weights in turn.  No reference counterpart: it batches the
+ * SDF-grid queries (models/renderer.py:9-24) of several served objects. */
+#define SN_FIELD_MAX_SEGMENTS 4
+typedef struct {
+  int64_t n;
+  const float* x;
+  const void* table;          /* FP32, or FP16 pairs with SN_FIELD_TABLE_FP16 in mlp->flags */
+  const sn_grid_desc* grid;
+  int32_t active_levels;
+  const sn_mlp_desc* mlp;
+  float* out;
+} sn_field_segment;
+int sn_field_fwd_batch(int n_segments, const sn_field_segment* segments,
+                       int out_cols, void* stream);
 /* Fused field backward with recomputation: accumulates (+=) the gradients of
  * sum(grad_out * out) into grad_table / grad_w0 / grad_b0 / grad_w1 /
  * grad_b1 and writes grad_x (each nullable).  Replaces the autograd backward

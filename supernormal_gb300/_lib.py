@@ -74,6 +74,14 @@ class SceneDesc(C.Structure):
                 ("disp_amp", C.c_double), ("disp_freq", C.c_double), ("lipschitz", C.c_double)]
 
 
+SN_FIELD_MAX_SEGMENTS = 4
+
+
+class FieldSegment(C.Structure):
+    _fields_ = [("n", C.c_int64), ("x", C.c_void_p), ("table", C.c_void_p), ("grid", C.POINTER(GridDesc)),
+                ("active_levels", C.c_int32), ("mlp", C.POINTER(MlpDesc)), ("out", C.c_void_p)]
+
+
 _P, _I64, _I, _F, _SZ = C.c_void_p, C.c_int64, C.c_int, C.c_float, C.c_size_t
 _GD, _MD, _SD = C.POINTER(GridDesc), C.POINTER(MlpDesc), C.POINTER(SceneDesc)
 
@@ -114,6 +122,7 @@ SIGNATURES: dict[str, tuple] = {
     "sn_hashgrid_fwd": (_I, [_I64, _P, _P, _GD, _I, _P, _P]),
     "sn_hashgrid_bwd": (_I, [_I64, _P, _P, _GD, _I, _P, _P]),
     "sn_field_fwd": (_I, [_I64, _P, _P, _P, _GD, _I, _MD, _I, _P, _P]),
+    "sn_field_fwd_batch": (_I, [_I, C.POINTER(FieldSegment), _I, _P]),
     "sn_field_bwd": (_I, [_I64, _P, _P, _P, _I, _P, _GD, _I, _MD, _P, _P, _P, _P, _P, _P, _P]),
     "sn_field_grad_fwd": (_I, [_I64, _P, _P, _P, _GD, _I, _MD, _P, _P, _P]),
     "sn_field_grad_bwd": (_I, [_I64, _P, _P, _P, _P, _P, _GD, _I, _MD, _P, _P, _P, _P, _P, _P]),

@@ -598,6 +598,25 @@ int sn_field_fwd(int64_t n, const int32_t* count, const float* x, const float* t
   return field_fwd_tc(a, as_stream(stream));
 }
 
+int sn_field_fwd_batch(int n_segments, const sn_field_segment* segments, int out_cols, void* stream) {
+  SN_REQUIRE(segments != nullptr, "field_fwd_batch: null segments");
+  SN_REQUIRE(n_segments >= 1 && n_segments <= SN_FIELD_MAX_SEGMENTS, "field_fwd_batch: %d segments (1..%d)",
+             n_segments, SN_FIELD_MAX_SEGMENTS);
+  FieldArgs args[SN_FIELD_MAX_SEGMENTS];
+  int live = 0;
+  for (int i = 0; i < n_segments; ++i) {
+    const sn_field_segment& sg = segments[i];
+    SN_REQUIRE(sg.out != nullptr, "field_fwd_batch: segment %d has no output", i);
+    SN_TRY(fill_field_args(args[live], sg.n, nullptr, sg.x, reinterpret_cast<const float*>(sg.table), sg.grid,
+                           sg.active_levels, sg.mlp, out_cols));
+    SN_REQUIRE(sg.mlp->enc_cache == nullptr, "field_fwd_batch: segment %d asks for an encoding cache", i);
+    args[live].out = sg.out;
+    if (sg.n > 0) ++live;
+  }
+  if (live == 0) return SN_OK;
+  return field_fwd_tc_segments(args, live, as_stream(stream));
+}
+
 int sn_field_bwd(int64_t n, const int32_t* count, const float* x, const float* grad_out,
                  int out_cols, const float* table, const sn_grid_desc* grid, int active_levels,
                  const sn_mlp_desc* mlp, float* grad_table, float* grad_w0, float* grad_b0,

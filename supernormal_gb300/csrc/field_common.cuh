@@ -194,6 +194,7 @@ __device__ __forceinline__ int64_t effective_n(const FieldArgs& a) {
 
 // Tensor-core launchers (field_tc.cu).
 int field_fwd_tc(const FieldArgs& a, cudaStream_t st);
+int field_fwd_tc_segments(const FieldArgs* segs, int n_seg, cudaStream_t st);
 int field_bwd_tc(const FieldArgs& a, cudaStream_t st);
 
 // Host helpers (field.cu).

@@ -24,6 +24,8 @@
 #include "field_common.cuh"
 #include "tc.cuh"
 
+#include <string.h>
+
 namespace sn {
 namespace {
 
@@ -349,9 +351,21 @@ __device__ __forceinline__ void tmem_ld_n(uint32_t ta, float* v) {
   else tc::tmem_ld4(ta, v);
 }
 
+// Segments of one forward launch: point sets that each have their own table,
+// level geometry and MLP (several objects' queries in one persistent launch).
+constexpr int kMaxSegments = 4;
+struct FieldSegments {
+  int n;
+  FieldArgs seg[kMaxSegments];
+};
+
 // ONE: a single output column (the sdf; every training call), else up to kDoutMax.
+// Each CTA works through the segments in order: it stages segment s's
+// weights, processes its share of s's tiles (persistent, strided by the
+// grid), then moves on; one launch of one segment is the ordinary forward.
 template <bool ONE, int M>
-__global__ void __launch_bounds__(128 * M, M == 4 ? 2 : 1) field_fwd_tc_kernel(FieldArgs a) {
+__global__ void __launch_bounds__(128 * M, M == 4 ? 2 : 1)
+field_fwd_tc_kernel(const __grid_constant__ FieldSegments segs) {
   constexpr int kOc = ONE ? 1 : kDoutMax;
   constexpr int kNt = 128 * M;      // threads
   constexpr int kLpm = 16 / M;      // levels per member
@@ -368,122 +382,131 @@ __global__ void __launch_bounds__(128 * M, M == 4 ? 2 : 1) field_fwd_tc_kernel(F
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int q = warp & 3, g = warp >> 2;
   const int pt = 32 * q + lane;  // point within the tile == TMEM lane
-  const int oc = a.out_cols;
-  const float inv_beta = 1.0f / a.beta;
 
-  stage_w0<M>(a, sm + Sm::b1_hi, sm + Sm::b1_lo, nullptr, nullptr);
-  for (int e = t; e < kDoutMax * kH; e += kNt) s_w1[e] = e / kH < oc ? a.w1[e] : 0.0f;
-  if (t < kH) s_b0[t] = a.b0[t];
-  if (t < kDoutMax) s_b1[t] = t < oc ? a.b1[t] : 0.0f;
   if (warp == 0) {
     tc::tmem_alloc(slot, kCols);
     tc::tmem_relinquish();
   }
   if (t == 0) tc::mbar_init(bar, 2);  // one commit each from threads 0 and 32
-  tc::fence_proxy_async_smem();
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  const uint32_t tbase = *slot;
   const uint32_t lb = (uint32_t)(32 * q);
   const uint32_t s_b1_hi = tc::smem_u32(sm + Sm::b1_hi), s_b1_lo = tc::smem_u32(sm + Sm::b1_lo);
   uint32_t phase = 0;
   bool ok = true;
+  uint32_t tbase = 0;
 
-  const int64_t n = effective_n(a);
-  const int64_t n_tiles = (n + kTile - 1) / kTile;
-  // this point's coordinates one tile ahead: the stream read overlaps a tile
-  float xn[3] = {0.0f, 0.0f, 0.0f};
-  load_point(a, (int64_t)blockIdx.x * kTile + pt, n, xn);
-  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    const int64_t p = tile * kTile + pt;
-    const bool live = p < n;
-    const float x[3] = {xn[0], xn[1], xn[2]};
-    load_point(a, (tile + gridDim.x) * kTile + pt, n, xn);
-    {
-      float e[kFpm];
-      encode_group<(M == 8), M>(a, g, live, x, e);
-      if (a.enc_out && live) {
+  for (int si = 0; si < segs.n && ok; ++si) {
+    const FieldArgs& a = segs.seg[si];
+    const int oc = a.out_cols;
+    const float inv_beta = 1.0f / a.beta;
+    if (si > 0) __syncthreads();     // the previous segment's last tile is done with the weights
+    stage_w0<M>(a, sm + Sm::b1_hi, sm + Sm::b1_lo, nullptr, nullptr);
+    for (int e = t; e < kDoutMax * kH; e += kNt) s_w1[e] = e / kH < oc ? a.w1[e] : 0.0f;
+    if (t < kH) s_b0[t] = a.b0[t];
+    if (t < kDoutMax) s_b1[t] = t < oc ? a.b1[t] : 0.0f;
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    tbase = *slot;
+
+    const int64_t n = effective_n(a);
+    const int64_t n_tiles = (n + kTile - 1) / kTile;
+    // this point's coordinates one tile ahead: the stream read overlaps a tile
+    float xn[3] = {0.0f, 0.0f, 0.0f};
+    load_point(a, (int64_t)blockIdx.x * kTile + pt, n, xn);
+    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+      const int64_t p = tile * kTile + pt;
+      const bool live = p < n;
+      const float x[3] = {xn[0], xn[1], xn[2]};
+      load_point(a, (tile + gridDim.x) * kTile + pt, n, xn);
+      {
+        float e[kFpm];
+        encode_group<(M == 8), M>(a, g, live, x, e);
+        if (a.enc_out && live) {
 #pragma unroll
-        for (int i = 0; i < kLpm; ++i) {
-          const int l = level_of<M>(g, i);
-          if (l < a.active) __stcs(a.enc_out + (int64_t)l * a.cap + p, make_float2(e[2 * i], e[2 * i + 1]));
+          for (int i = 0; i < kLpm; ++i) {
+            const int l = level_of<M>(g, i);
+            if (l < a.active) __stcs(a.enc_out + (int64_t)l * a.cap + p, make_float2(e[2 * i], e[2 * i + 1]));
+          }
+        }
+        st_split<kFpm>(tc::taddr(tbase, lb, kFwdColInHi + kFpm * g), tc::taddr(tbase, lb, kFwdColInLo + kFpm * g), e);
+        if (g == 0) {
+          const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+          st_split8(tc::taddr(tbase, lb, kFwdColInHi + kXCol), tc::taddr(tbase, lb, kFwdColInLo + kXCol), xv);
         }
       }
-      st_split<kFpm>(tc::taddr(tbase, lb, kFwdColInHi + kFpm * g), tc::taddr(tbase, lb, kFwdColInLo + kFpm * g), e);
-      if (g == 0) {
-        const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-        st_split8(tc::taddr(tbase, lb, kFwdColInHi + kXCol), tc::taddr(tbase, lb, kFwdColInLo + kXCol), xv);
+      tc::tmem_wait_st();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (t == 0 || t == 32) {  // H = IN W0^T, M=128, N=64, K=40
+        tc::fence_after_sync();
+        const uint32_t idesc = tc::idesc_tf32(kTile, kH);
+        const uint32_t sbo = (kK1 / 4) * 128u;
+        const uint64_t w_hi = tc::smem_desc(s_b1_hi, 128u, sbo), w_lo = tc::smem_desc(s_b1_lo, 128u, sbo);
+        if (t == 0) {
+          mma_chain(tc::taddr(tbase, 0, kFwdColH0), tc::taddr(tbase, 0, kFwdColInHi), w_hi, kK1 / 8, idesc, true);
+        } else if (!a.one_pass) {
+          mma_chain(tc::taddr(tbase, 0, kFwdColH1), tc::taddr(tbase, 0, kFwdColInLo), w_hi, kK1 / 8, idesc, true);
+          mma_chain(tc::taddr(tbase, 0, kFwdColH1), tc::taddr(tbase, 0, kFwdColInHi), w_lo, kK1 / 8, idesc, false);
+        }
+        tc::mma_commit(bar);
       }
-    }
-    tc::tmem_wait_st();
-    tc::fence_before_sync();
-    __syncthreads();
-    if (t == 0 || t == 32) {  // H = IN W0^T, M=128, N=64, K=40
+      const bool got = tc::mbar_wait_bounded(bar, phase);
+      phase ^= 1u;
+      if (!__syncthreads_and(got)) {
+        ok = false;
+        break;
+      }
       tc::fence_after_sync();
-      const uint32_t idesc = tc::idesc_tf32(kTile, kH);
-      const uint32_t sbo = (kK1 / 4) * 128u;
-      const uint64_t w_hi = tc::smem_desc(s_b1_hi, 128u, sbo), w_lo = tc::smem_desc(s_b1_lo, 128u, sbo);
-      if (t == 0) {
-        mma_chain(tc::taddr(tbase, 0, kFwdColH0), tc::taddr(tbase, 0, kFwdColInHi), w_hi, kK1 / 8, idesc, true);
-      } else if (!a.one_pass) {
-        mma_chain(tc::taddr(tbase, 0, kFwdColH1), tc::taddr(tbase, 0, kFwdColInLo), w_hi, kK1 / 8, idesc, true);
-        mma_chain(tc::taddr(tbase, 0, kFwdColH1), tc::taddr(tbase, 0, kFwdColInHi), w_lo, kK1 / 8, idesc, false);
+      // hidden units kHpm g .. kHpm g + kHpm - 1 of this point -> partial outputs
+      float h[kHpm];
+      tmem_ld_n<kHpm>(tc::taddr(tbase, lb, kFwdColH0 + kHpm * g), h);
+      if (!a.one_pass) {
+        float h1[kHpm];
+        tmem_ld_n<kHpm>(tc::taddr(tbase, lb, kFwdColH1 + kHpm * g), h1);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < kHpm; ++i) h[i] += h1[i];
       }
-      tc::mma_commit(bar);
-    }
-    const bool got = tc::mbar_wait_bounded(bar, phase);
-    phase ^= 1u;
-    if (!__syncthreads_and(got)) {
-      ok = false;
-      break;
-    }
-    tc::fence_after_sync();
-    // hidden units kHpm g .. kHpm g + kHpm - 1 of this point -> partial outputs
-    float h[kHpm];
-    tmem_ld_n<kHpm>(tc::taddr(tbase, lb, kFwdColH0 + kHpm * g), h);
-    if (!a.one_pass) {
-      float h1[kHpm];
-      tmem_ld_n<kHpm>(tc::taddr(tbase, lb, kFwdColH1 + kHpm * g), h1);
       tc::tmem_wait_ld();
+      float part[kOc];
 #pragma unroll
-      for (int i = 0; i < kHpm; ++i) h[i] += h1[i];
-    }
-    tc::tmem_wait_ld();
-    float part[kOc];
+      for (int o = 0; o < kOc; ++o) part[o] = 0.0f;
 #pragma unroll
-    for (int o = 0; o < kOc; ++o) part[o] = 0.0f;
+      for (int i = 0; i < kHpm; ++i) {
+        const int j = kHpm * g + i;
+        float act, sg_unused;
+        softplus_fwd_grad_fast(h[i] + s_b0[j], a.beta, inv_beta, a.thresh, act, sg_unused);
 #pragma unroll
-    for (int i = 0; i < kHpm; ++i) {
-      const int j = kHpm * g + i;
-      float act, sg_unused;
-      softplus_fwd_grad_fast(h[i] + s_b0[j], a.beta, inv_beta, a.thresh, act, sg_unused);
+        for (int o = 0; o < kOc; ++o)
+          if (o < oc) part[o] = fmaf(s_w1[o * kH + j], act, part[o]);
+      }
 #pragma unroll
       for (int o = 0; o < kOc; ++o)
-        if (o < oc) part[o] = fmaf(s_w1[o * kH + j], act, part[o]);
-    }
+        if (o < oc) s_part[(g * kTile + pt) * kDoutMax + o] = part[o];
+      tc::fence_before_sync();
+      __syncthreads();
+      if (g == 0 && live) {
+        for (int o = 0; o < oc; ++o) {
+          float sum = s_b1[o];
 #pragma unroll
-    for (int o = 0; o < kOc; ++o)
-      if (o < oc) s_part[(g * kTile + pt) * kDoutMax + o] = part[o];
-    tc::fence_before_sync();
-    __syncthreads();
-    if (g == 0 && live) {
-      for (int o = 0; o < oc; ++o) {
-        float s = s_b1[o];
-#pragma unroll
-        for (int m = 0; m < M; ++m) s += s_part[(m * kTile + pt) * kDoutMax + o];
-        a.out[p * oc + o] = s;
+          for (int m = 0; m < M; ++m) sum += s_part[(m * kTile + pt) * kDoutMax + o];
+          a.out[p * oc + o] = sum;
+        }
       }
+      __syncthreads();
     }
-    __syncthreads();
   }
   if (!ok) {
-    if (t == 0 && a.status) atomicOr(a.status, SN_STATUS_TIMEOUT);
+    if (t == 0) {
+      for (int si = 0; si < segs.n; ++si)
+        if (segs.seg[si].status) atomicOr(segs.seg[si].status, SN_STATUS_TIMEOUT);
+    }
     (void)tc::mbar_wait_bounded(bar, phase ^ 1u);
     __syncthreads();
   }
   tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tbase, kCols);
+  if (warp == 0) tc::tmem_dealloc(*slot, kCols);
 }
 
 // ---------------------------------------------------------------------------
@@ -870,21 +893,34 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
 }  // namespace
 
 // Launchers used by sn_field_fwd / sn_field_bwd (field.cu).
-int field_fwd_tc(const FieldArgs& a, cudaStream_t st) {
+int field_fwd_tc_segments(const FieldArgs* segs, int n_seg, cudaStream_t st) {
   constexpr int M = kFwdMembers;
   constexpr size_t smem = FwdSmem<M>::bytes;
-  const void* fn = a.out_cols == 1 ? reinterpret_cast<const void*>(field_fwd_tc_kernel<true, M>)
-                                   : reinterpret_cast<const void*>(field_fwd_tc_kernel<false, M>);
+  SN_REQUIRE(n_seg >= 1 && n_seg <= kMaxSegments, "field_fwd: %d segments (1..%d)", n_seg, kMaxSegments);
+  const bool one = segs[0].out_cols == 1;
+  FieldSegments fs;
+  memset(&fs, 0, sizeof(fs));
+  fs.n = n_seg;
+  int64_t max_tiles = 0;
+  for (int i = 0; i < n_seg; ++i) {
+    SN_REQUIRE((segs[i].out_cols == 1) == one, "field_fwd: segments mix one and several output columns");
+    fs.seg[i] = segs[i];
+    const int64_t tiles = (segs[i].cap + kTile - 1) / kTile;
+    if (tiles > max_tiles) max_tiles = tiles;
+  }
+  const void* fn = one ? reinterpret_cast<const void*>(field_fwd_tc_kernel<true, M>)
+                       : reinterpret_cast<const void*>(field_fwd_tc_kernel<false, M>);
   SN_TRY(ensure_smem_limit(fn, smem, "field_fwd"));
-  const int64_t n_tiles = (a.cap + kTile - 1) / kTile;
   const int64_t cap = (M == 4 ? 2LL : 1LL) * num_sms();
-  const unsigned grid = (unsigned)(n_tiles < cap ? n_tiles : cap);
-  if (a.out_cols == 1)
-    field_fwd_tc_kernel<true, M><<<grid, 128 * M, smem, st>>>(a);
+  const unsigned grid = (unsigned)(max_tiles < cap ? (max_tiles > 0 ? max_tiles : 1) : cap);
+  if (one)
+    field_fwd_tc_kernel<true, M><<<grid, 128 * M, smem, st>>>(fs);
   else
-    field_fwd_tc_kernel<false, M><<<grid, 128 * M, smem, st>>>(a);
+    field_fwd_tc_kernel<false, M><<<grid, 128 * M, smem, st>>>(fs);
   return check_launch("field_fwd");
 }
+
+int field_fwd_tc(const FieldArgs& a, cudaStream_t st) { return field_fwd_tc_segments(&a, 1, st); }
 
 int field_bwd_tc(const FieldArgs& a, cudaStream_t st) {
   constexpr int M = kBwdMembers;

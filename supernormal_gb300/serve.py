@@ -218,18 +218,47 @@ class ServedObject:
         return out.reshape(ph, pw, 3, 3, 3).transpose(1, 2).reshape(H, W, 3)
 
     @torch.no_grad()
-    def query(self, res: int = 256, chunk: int = 1 << 22) -> torch.Tensor:
-        """SDF on a res^3 grid over [-1, 1]^3 (models/renderer.py:9-34)."""
-        dev = self.tr.device
-        lin = torch.linspace(-1.0, 1.0, res, device=dev)
-        out = torch.empty(res ** 3, device=dev)
-        n_plane = res * res
-        for z0 in range(0, res, max(1, chunk // n_plane)):
-            z1 = min(res, z0 + max(1, chunk // n_plane))
-            zz, yy, xx = torch.meshgrid(lin[z0:z1], lin, lin, indexing="ij")
-            pts = torch.stack([xx, yy, zz], dim=-1).reshape(-1, 3).contiguous()
-            out[z0 * n_plane:z1 * n_plane] = self.tr.net.sdf_raw(pts).reshape(-1)
-        return out.reshape(res, res, res)
+    def query(self, res: int = 256) -> torch.Tensor:
+        """SDF on a res^3 lattice over [-1, 1]^3 (models/renderer.py:9-24
+        extract_fields; X first, Z fastest)."""
+        return query_batch([self], res)[0]
+
+
+@torch.no_grad()
+def query_batch(objects: list, res: int = 256, slab_points: int = 1 << 22) -> list:
+    """SDF lattices (res^3 over [-1, 1]^3) of several objects from shared
+    lattice points, each slab one field launch over all objects' tables and
+    MLPs (``sn_field_fwd_batch``, at most SN_FIELD_MAX_SEGMENTS objects)."""
+    import ctypes as Ct
+
+    import numpy as np
+
+    from ._lib import SN_FIELD_MAX_SEGMENTS, FieldSegment, call, stream_handle
+
+    if not 1 <= len(objects) <= SN_FIELD_MAX_SEGMENTS:
+        raise ValueError(f"query_batch: 1..{SN_FIELD_MAX_SEGMENTS} objects")
+    dev = objects[0].tr.device
+    st = stream_handle()
+    outs = [torch.empty((res, res, res), device=dev) for _ in objects]
+    keep = []   # effective weights and descriptors live until the launches are enqueued
+    for o in objects:
+        net = o.tr.net
+        w0, b0, w1, b1 = (t.detach().contiguous() for t in net.mlp_tensors())
+        keep.append((w0, b0, w1, b1, net._mlp_desc(w0, b0, w1, b1)))
+    per = max(1, slab_points // (res * res))
+    x = torch.empty((min(per, res) * res * res, 3), device=dev)
+    lo, hi = np.full(3, -1.0), np.full(3, 1.0)
+    for i0 in range(0, res, per):
+        ni = min(per, res - i0)
+        n = ni * res * res
+        call("sn_lattice_points", i0, ni, res, res, res, lo.ctypes.data, hi.ctypes.data, x, st)
+        segs = (FieldSegment * len(objects))()
+        for k, o in enumerate(objects):
+            net = o.tr.net
+            segs[k] = FieldSegment(n, x.data_ptr(), net.encoding.params.data_ptr(), Ct.pointer(net.encoding.desc),
+                                   net.active_levels(), Ct.pointer(keep[k][4]), outs[k][i0:i0 + ni].data_ptr())
+        call("sn_field_fwd_batch", len(objects), segs, 1, st)
+    return outs
 
 
 @dataclass
@@ -269,6 +298,8 @@ class Server:
         self.query_res = query_res
         self.slice_iters = slice_iters
         self.swaps = 0
+        self.max_batch = 4              # objects per batched SDF-grid query launch
+        self.batched_queries = 0        # queries that joined another query's launches
         self.device = sync is None
         self.sync = torch.cuda.synchronize if sync is None else sync
         if self.device:
@@ -298,12 +329,35 @@ class Server:
             ev.record(stream)
             obj.ready = ev
 
+    @contextmanager
+    def on_many(self, objs, stream):
+        """``on`` for work that reads several objects at once."""
+        if not self.device:
+            yield
+            return
+        with torch.cuda.stream(stream):
+            for o in objs:
+                if getattr(o, "ready", None) is not None:
+                    stream.wait_event(o.ready)
+            yield
+            ev = torch.cuda.Event()
+            ev.record(stream)
+            for o in objs:
+                o.ready = ev
+
     def done(self, obj) -> None:
         """Host waits for the object's last work (not for the other stream)."""
         if not self.device:
             self.sync()
         elif getattr(obj, "ready", None) is not None:
             obj.ready.synchronize()
+
+    def query_batch(self, objs, res):
+        if len(objs) == 1 or not self.device:
+            for o in objs:
+                o.query(res)
+        else:
+            query_batch(objs, res)
 
     @staticmethod
     def _record_event():
@@ -375,6 +429,25 @@ class Server:
                 continue
             s = now()
             obj = self.objects[r.obj]
+            if policy != "plain" and r.kind == "query":
+                # SDF-grid queries waiting for other resident objects join this
+                # one's launches (one field launch per slab over all of them)
+                group = [r]
+                for q in list(short_q):
+                    if (len(group) < self.max_batch and q.kind == "query" and self.objects[q.obj].resident
+                            and all(self.objects[q.obj] is not self.objects[g.obj] for g in group)):
+                        group.append(q)
+                        short_q.remove(q)
+                objs = [self.objects[g.obj] for g in group]
+                with self.on_many(objs, self.req_stream):
+                    for o in objs:
+                        self.admit(o, s)
+                    self.query_batch(objs, self.query_res)
+                for g, o in zip(group, objs):
+                    finish(g, o)
+                self.batched_queries += len(group) - 1
+                busy += now() - s
+                continue
             if policy == "plain":
                 stream = None                    # the current stream, one request at a time
             else:
@@ -415,6 +488,7 @@ class Server:
 
         return {
             "policy": policy, "requests": len(reqs), "makespan_s": span, "busy_s": busy,
+            "batched_queries": self.batched_queries,
             "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
             "by_kind": {k: {"n": len(v), "p50_ms": pct(v, 50), "p99_ms": pct(v, 99)} for k, v in lat.items()},
             "rays_per_s": (train_rays + render_rays) / span if span > 0 else 0.0,

@@ -253,3 +253,34 @@ def test_requests_same_alone_and_in_the_mix(built_lib):
     assert torch.equal(a.render(pose_seed=7), img_alone)
     for x, y in zip(la, lb):
         assert torch.allclose(x, y, rtol=2e-3, atol=1e-6), (x, y)
+
+
+def test_query_batch_matches_per_object(built_lib):
+    """One field launch over several objects' tables and MLPs per slab
+    (sn_field_fwd_batch) gives each object's SDF lattice bit for bit as its
+    own launch does, including objects with different active levels and a
+    lattice split over several slabs."""
+    import numpy as np
+
+    from supernormal_gb300._lib import call, stream_handle
+    from supernormal_gb300.serve import ServedObject, object_specs, query_batch
+
+    specs = object_specs(3, seed=5, views=(6, 6, 6), res=(64, 64, 64), log2_table=(14, 15, 15))
+    objs = [ServedObject(s, "cuda", batch=128, step_size=1.0 / 64) for s in specs]
+    objs[0].train_iterations(5, False)
+    objs[2].train_iterations(9, False)
+    objs[1].tr.net.bindwidth = 7
+    res = 40
+    x = torch.empty((res ** 3, 3), device="cuda")
+    lo, hi = np.full(3, -1.0), np.full(3, 1.0)
+    call("sn_lattice_points", 0, res, res, res, res, lo.ctypes.data, hi.ctypes.data, x, stream_handle())
+    want = [o.tr.net.sdf_raw(x).reshape(res, res, res) for o in objs]
+    got = query_batch(objs, res, slab_points=11 * res * res)     # 4 slabs, the last one ragged
+    torch.cuda.synchronize()
+    for o in objs:
+        o.tr.net.check_status()
+    for w, g in zip(want, got):
+        assert torch.equal(w, g)
+    assert not torch.equal(got[0], got[1])
+    one = query_batch(objs[2:], res)
+    assert torch.equal(one[0], want[2])
