@@ -21,7 +21,8 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REF_ROOT = Path(os.environ.get("SUPERNORMAL_REFERENCE", "/root/reference"))
+# the SuperNormal tree: $SUPERNORMAL_REFERENCE, else a "reference" directory beside the repository
+REF_ROOT = Path(os.environ.get("SUPERNORMAL_REFERENCE", HERE.parent.parent / "reference"))
 CSRC = REF_ROOT / "third_parties" / "nerfacc-0.3.5" / "nerfacc-0.3.5" / "nerfacc" / "cuda" / "csrc"
 SOURCES = ["ray_marching.cu", "render_weight.cu", "contraction.cu"]
 KERNELS = {

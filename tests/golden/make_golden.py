@@ -13,7 +13,7 @@ The losses are exp_runner.py:169-203 written out (exp_runner.py itself needs
 pyhocon / open3d / trimesh, which are absent).
 
 Writes tests/golden/reference_render.npz and tests/golden/reference_field.npz.
-Usage:  python tests/golden/make_golden.py  [SuperNormal tree, default /root/reference]
+Usage:  python tests/golden/make_golden.py  [SuperNormal tree; default $SUPERNORMAL_REFERENCE, else "reference" beside the repository]
 """
 from __future__ import annotations
 
@@ -252,4 +252,4 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SUPERNORMAL_REFERENCE", "/root/reference"))
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SUPERNORMAL_REFERENCE", str(Path(__file__).resolve().parents[3] / "reference")))

@@ -19,7 +19,7 @@ reference's own draws.  One CPU thread: the CPU index_put then stores a
 repeated cell's last candidate.
 
 Writes tests/golden/reference_occupancy.npz.
-Usage:  python tests/golden/make_occupancy.py  [SuperNormal tree, default /root/reference]
+Usage:  python tests/golden/make_occupancy.py  [SuperNormal tree; default $SUPERNORMAL_REFERENCE, else "reference" beside the repository]
 """
 from __future__ import annotations
 
@@ -152,4 +152,4 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SUPERNORMAL_REFERENCE", "/root/reference"))
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SUPERNORMAL_REFERENCE", str(Path(__file__).resolve().parents[3] / "reference")))
