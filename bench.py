@@ -292,30 +292,35 @@ def run_ours(args, world, rank, local):
         qual["after_iterations"] = tr.iter_step
         qual["views"] = f"held-out views {list(TEST_VIEWS)} of {args.views}"
         qual["seconds"] = time.perf_counter() - tq
-    # iterations as CUDA-graph replays carrying the stage events (captured
-    # before the warm-up), or eager launches with --eager
-    gs = None if args.eager else GraphStep(tr, profile=True)
-    if gs is not None:
+    # iterations as CUDA-graph replays (captured before the warm-up), or eager
+    # launches with --eager; a second set of captures carries the stage events
+    gs = gp = None
+    if not args.eager:
+        gs, gp = GraphStep(tr), GraphStep(tr, profile=True)
         gs.prepare()
-    for i in range(args.warmup):
-        if gs is not None:
-            gs.step(pool[i % len(pool)])
+        gp.prepare()
+
+    def step(graph, i):
+        if graph is not None:
+            graph.step(pool[i % len(pool)])
         else:
             tr.train_step(*pool[i % len(pool)])
+
+    for i in range(args.warmup):
+        step(gs, i)
+    if gp is not None:
+        for i in range(gp.n_copies):           # first replays of the profiled copies, untimed
+            step(gp, i)
     torch.cuda.synchronize()
     tr.check_status()
-    if gs is not None:
-        gs.flush()
-        gs.stage_marks.clear()
-        gs.points.clear()
-        gs.samples.clear()
+    if gp is not None:
+        gp.flush()
+        gp.stage_marks.clear()
+        gp.points.clear()
+        gp.samples.clear()
 
     # ---------------- device-resident timed region ----------------
     K = args.steps
-    if gs is None:
-        tr.profile = True
-        tr.marks.clear()
-        tr.q_hist.clear()
     clocks = ClockSampler(local, not args.no_clocks and rank == 0)
     launches0 = gs.launches if gs is not None else lib().sn_kernel_launches()
     barrier(world)
@@ -324,10 +329,7 @@ def run_ours(args, world, rank, local):
     torch.cuda.nvtx.range_push("timed")      # profiler filter: the timed steps only
     start.record()
     for i in range(K):
-        if gs is not None:
-            gs.step(pool[i % len(pool)])
-        else:
-            tr.train_step(*pool[i % len(pool)])
+        step(gs, i)
     end.record()
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
@@ -335,15 +337,29 @@ def run_ours(args, world, rank, local):
     clk = clocks.stop()
     ms = start.elapsed_time(end)
     tr.check_status()
-    if gs is not None:
-        gs.flush()
-        launches = gs.launches - launches0
-        stages = stage_times([m for step in gs.stage_marks for m in step])
-        q = np.asarray(gs.points, dtype=np.float64)
-        samples = np.asarray(gs.samples, dtype=np.float64)
+    launches = (gs.launches if gs is not None else lib().sn_kernel_launches()) - launches0
+
+    # ---------------- the same K steps with stage events (roofline, stage times) ----------------
+    if gp is None:
+        tr.profile = True
+        tr.marks.clear()
+        tr.q_hist.clear()
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record()
+    for i in range(K):
+        step(gp, i)
+    p1.record()
+    torch.cuda.synchronize()
+    tr.check_status()
+    profiled_ms = p0.elapsed_time(p1)
+    if gp is not None:
+        gp.flush()
+        stages = stage_times([m for s_ in gp.stage_marks for m in s_])
+        q = np.asarray(gp.points, dtype=np.float64)
+        samples = np.asarray(gp.samples, dtype=np.float64)
     else:
         samples = None
-        launches = lib().sn_kernel_launches() - launches0
         stages = stage_times(tr.marks)
         q = torch.cat(tr.q_hist).double().cpu().numpy() if tr.q_hist else None
         tr.profile = False
@@ -356,11 +372,7 @@ def run_ours(args, world, rank, local):
     loss_host = torch.empty((5,), dtype=torch.float32).pin_memory()
     h2d = sum(t.numel() * t.element_size() for t in host[0])
     d2h = loss_host.numel() * loss_host.element_size()
-    pf = HostPrefetcher(tr, host[0], graph=None if args.eager else GraphStep(tr))
-    if pf.graph is not None:
-        pf.graph.prepare()
-        for i in range(3):              # replays of the fresh captures, untimed
-            pf.graph.step(pool[i % len(pool)])
+    pf = HostPrefetcher(tr, host[0], graph=gs)
     barrier(world)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -396,6 +408,7 @@ def run_ours(args, world, rank, local):
         "gpu_launches": int(launches),
         "roofline": rl,
         "stages_ms_per_step": {k: v / K for k, v in stages.items()},
+        "profiled_ms_per_step": profiled_ms / K,
         "stage_roofline": stage_rooflines(stages, q, samples, tr, rl["peak"], K),
         "setup_s": setup_s,
     }
@@ -412,7 +425,7 @@ def run_ours(args, world, rank, local):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, budget_s=20.0)
     if args.serve != "off":
-        del tr, ds, pool, host, pf, gs
+        del tr, ds, pool, host, pf, gs, gp
         torch.cuda.empty_cache()
         out["serve"] = run_serve(args.serve, dev)
     return out

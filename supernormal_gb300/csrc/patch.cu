@@ -305,9 +305,8 @@ __global__ void __launch_bounds__(MAXT, MAXT == 288 ? 3 : 1) patch_block_kernel(
     Sample s;
     chunk_sample(a, R, base + j, S, inv_s, ok, lane, sm_s0, sm_pos, s);
     const ff Tf = transmittance(s.alpha, ok, Tc, lane);
-    const float w = ok ? __fmul_rn(s.alpha, ff_val(Tf)) : 0.0f;
     const float gw = ok ? weight_grad(gc, gws, s.g) : 0.0f;
-    total = ff_add_f(total, __fmul_rn(gw, w));
+    if (ok) total = ff_add(total, ff_mul(ff{gw, 0.0f}, ff_mul(Tf, ff{s.alpha, 0.0f})));
   }
   total = warp_sum_ff(total);
 
@@ -330,9 +329,14 @@ __global__ void __launch_bounds__(MAXT, MAXT == 288 ? 3 : 1) patch_block_kernel(
     const float gw = ok ? weight_grad(gc, gws, s.g) : 0.0f;
     // accum_j = sum_{i >= j} g_i w_i (NA/nerfacc/cuda/csrc/render_weight.cu:325-337)
     // = total - (sum of earlier chunks + this chunk's exclusive scan), in
-    // double-float so the suffix behind the surface keeps its digits
-    const float gwj = __fmul_rn(gw, w);
-    ff incl{gwj, 0.0f};
+    // double-float so the suffix behind the surface keeps its digits.  The
+    // terms g_i alpha_i T_i are double-float products too: with T carried as
+    // prod (1 - alpha) from exact differences, T_j - sum_{i >= j} alpha_i T_i
+    // telescopes to the transmittance past the ray's end, so the numerator
+    // g_j T_j - accum_j keeps its digits when that remainder is small (an
+    // opaque ray), where float32 terms would leave rounding noise of order
+    // eps * g_j T_j.
+    ff incl = ok ? ff_mul(ff{gw, 0.0f}, ff_mul(Tf, ff{s.alpha, 0.0f})) : ff{0.0f, 0.0f};
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const ff y = shfl_up_ff(incl, o);

@@ -135,6 +135,31 @@ def test_renderer_forward_backward_matches_oracle(scene, method):
         assert grad_err(n, cpu(a), b.numpy()) < 2e-3, n
 
 
+def clip_boundary_points(ref, S, P, inv_s, band=1e-6):
+    """Field points of the samples whose unclipped NeuS ratio
+    q = (c0 - c1 + 1e-5) / (c0 + 1e-5) lies within ``band`` of alpha's clip
+    bounds 0 and 1 (models/renderer.py:177-179), from the oracle's float64
+    values.  There the float32 kernel and the float64 oracle may clip on
+    different sides (q's float32 rounding error is ~1e-7), so d alpha / d q is
+    passed by one and zeroed by the other; those points' sdf gradients are
+    left out of a max-relative comparison.  Returns a mask over all field
+    points (start points of every sample, then end points of diff samples)."""
+    sdf = ref["sdf"].detach().numpy().reshape(-1, P)
+    diff = np.asarray(ref["diff"])
+    s0 = sdf[:S]
+    s1 = np.concatenate([s0[1:], s0[-1:]], 0)
+    s1[diff] = sdf[S:]
+    sig = lambda z: 1.0 / (1.0 + np.exp(-z))
+    c, n = sig(s0 * inv_s), sig(s1 * inv_s)
+    q = (c - n + 1e-5) / (c + 1e-5)
+    ii, kk = np.nonzero((np.abs(q) < band) | (np.abs(q - 1.0) < band))
+    mask = np.zeros(sdf.shape, bool)
+    mask[ii, kk] = True
+    end_row = np.where(diff, S + np.cumsum(diff) - 1, np.minimum(np.arange(S) + 1, S - 1))
+    mask[end_row[ii], kk] = True
+    return mask.ravel()
+
+
 class _FixedSdf:
     """sdf_network stand-in returning given values (a leaf) at the query points."""
 
@@ -162,7 +187,9 @@ def test_patch_adjoint_matches_oracle_on_fixed_sdf(scene, method, step, outputs,
     5e-5; with the normal loss, the dfd differences (s1 - s0) / dt and
     (s_r - s_l) / (dx_l + dx_r) of float32 sdf values ~0.5 over steps of 2e-3
     lose ~eps * 0.5 / 2e-3 ~ 3e-5 relative in float32, in the reference's own
-    float32 arithmetic as here, hence 1e-3."""
+    float32 arithmetic as here, hence 1e-3.  Points of samples at alpha's clip
+    boundary (float32 and float64 clip differently there) are left out of the
+    sdf comparison; they are a small fraction of the points."""
     from supernormal_gb300.renderer import NeuSRenderer, near_far_from_sphere
 
     net, var = make()
@@ -205,8 +232,14 @@ def test_patch_adjoint_matches_oracle_on_fixed_sdf(scene, method, step, outputs,
     Lr = ((ref["comp_normal"] * gc.cpu().double()).sum() + (ref["weight_sum"] * gw.cpu().double()).sum()
           + (ref["gradients"] * gg.cpu().double()).sum())
     refg = torch.autograd.grad(Lr, [v64, var64] + ([e64] if e64 is not None else []))
+    inv_s = float(OR.inv_s_of(var64.detach(), torch.float64))
+    edge = clip_boundary_points(ref, S, P, inv_s)
+    assert edge.mean() < 0.01
     for name, a, b in zip(["sdf", "variance", "gradients"], got, refg):
-        assert rel_err(cpu(a).ravel(), b.numpy().ravel()) < tol, name
+        a, b = cpu(a).ravel(), b.numpy().ravel()
+        if name == "sdf":
+            a, b = a[~edge], b[~edge]
+        assert rel_err(a, b) < tol, name
 
 
 def _trainer(scene, B=128, **kw):
