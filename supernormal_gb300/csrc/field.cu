@@ -76,30 +76,16 @@ __device__ __forceinline__ float hidden_pre(const float* s_w0, const float* s_b0
   return h;
 }
 
-// Shared by the SIMT kernels of SDFNetwork.gradient below.
-constexpr int kBwdThreads = 128;
-
 constexpr size_t kFwdSmem = kSmemMlpFloats * sizeof(float);
 
 // ---------------------------------------------------------------------------
-// d sdf / d x (SDFNetwork.gradient, models/fields.py:107-119) and its adjoint
+// d sdf / d x (SDFNetwork.gradient, models/fields.py:107-119)
 // ---------------------------------------------------------------------------
 // With in = [x, e(x)], h = W0 in + b0, s = w1 . softplus(h) + b1 (w1 = row 0 of W1):
 //   u = w1 * softplus'(h),  grad = W0x^T u + E^T (W0e^T u),  E = d e / d x,
 // where e_{l,f} = sum_c w_c T_{c,f} and E_{l,f,d} = sum_c T_{c,f} d w_c / d x_d.
-// The adjoint of a loss L(grad, s) with gamma = dL/dgrad, rho = dL/ds:
-//   eta = E gamma,  zeta = [gamma, eta],  mu = W0 zeta,
-//   delta = mu * w1 * softplus''(h) + rho * w1 * softplus'(h)      (= dL/dh)
-//   dW0 += delta in^T + u zeta^T,  db0 += delta,
-//   dw1 += mu * softplus'(h) + rho * softplus(h),  db1 += rho,
-//   dT_{c,f} += (W0e^T delta)_{l,f} w_c + (W0e^T u)_{l,f} (gamma . d w_c / d x).
-__device__ __forceinline__ float softplus_grad2(float x, float beta, float threshold) {
-  const float bx = x * beta;
-  if (bx > threshold) return 0.0f;
-  const float s = 1.0f / (1.0f + expf(-bx));
-  return beta * s * (1.0f - s);
-}
-
+// Its adjoint (the double backward of create_graph=True) is the tensor-core
+// kernel field_grad_bwd_tc_kernel (field_tc.cu).
 __global__ void __launch_bounds__(128) field_grad_fwd_kernel(FieldArgs a, float* __restrict__ out_sdf,
                                                              float* __restrict__ out_grad) {
   extern __shared__ float4 smem4[];
@@ -162,221 +148,6 @@ __global__ void __launch_bounds__(128) field_grad_fwd_kernel(FieldArgs a, float*
   }
 }
 
-struct GradBwdArgs {
-  const float* gamma;  // (n, 3) dL / d grad
-  const float* rho;    // (n) dL / d sdf, nullable
-};
-
-__global__ void __launch_bounds__(kBwdThreads) field_grad_bwd_kernel(FieldArgs a, GradBwdArgs b) {
-  extern __shared__ float4 smem4[];
-  float* s_w0 = reinterpret_cast<float*>(smem4);
-  float* s_b0 = s_w0 + kH * kDinPad;
-  float* s_w1 = s_b0 + kH;
-  float* s_b1 = s_w1 + kDoutMax * kH;
-  float* s_in = s_b1 + kDoutMax;                 // [128][kDinPad]
-  float* s_z = s_in + kBwdThreads * kDinPad;     // [128][kDinPad]  zeta = [gamma, eta]
-  float* s_u = s_z + kBwdThreads * kDinPad;      // [128][64]
-  float* s_d = s_u + kBwdThreads * kH;           // [128][64]      delta
-  float* s_dw1 = s_d + kBwdThreads * kH;         // [128][64]
-  float* s_rho = s_dw1 + kBwdThreads * kH;       // [128]
-  load_mlp(a, s_w0, s_b0, s_w1, s_b1);
-  __syncthreads();
-  const int64_t n = effective_n(a);
-  const int n_in4 = (3 + 2 * a.active + 3) / 4;
-  const int din_used = 3 + 2 * a.active;
-  const int t = threadIdx.x, lane = t & 31;
-  const int rg = t >> 3, cg = t & 7;
-  float acc_w0[4][5], acc_b0[4], acc_w1[4];
-  float acc_b1 = 0.0f;
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    acc_b0[r] = 0.0f;
-    acc_w1[r] = 0.0f;
-#pragma unroll
-    for (int m = 0; m < 5; ++m) acc_w0[r][m] = 0.0f;
-  }
-  const float2* t2 = reinterpret_cast<const float2*>(a.table);
-  float2* gt2 = reinterpret_cast<float2*>(a.grad_table);
-  const int64_t stride = (int64_t)gridDim.x * kBwdThreads;
-  for (int64_t base = (int64_t)blockIdx.x * kBwdThreads; base < n; base += stride) {
-    const int64_t p = base + t;
-    const bool live = p < n;
-    float in[kDinPad], z[kDinPad];
-#pragma unroll
-    for (int i = 0; i < kDinPad; ++i) {
-      in[i] = 0.0f;
-      z[i] = 0.0f;
-    }
-    float rho = 0.0f;
-    if (live) {
-      in[0] = a.x[3 * p];
-      in[1] = a.x[3 * p + 1];
-      in[2] = a.x[3 * p + 2];
-      z[0] = b.gamma[3 * p];
-      z[1] = b.gamma[3 * p + 1];
-      z[2] = b.gamma[3 * p + 2];
-      rho = b.rho ? b.rho[p] : 0.0f;
-    }
-    // phase 0: encoding e and eta = E gamma
-    {
-      const float x[3] = {in[0], in[1], in[2]};
-#pragma unroll
-      for (int l = 0; l < kMaxL; ++l) {
-        if (l < a.active && live) {
-          LevelCorners c;
-          level_corners(a.g, l, x, c);
-          float e0 = 0.0f, e1 = 0.0f, h0 = 0.0f, h1 = 0.0f;
-#pragma unroll
-          for (int k = 0; k < 8; ++k) {
-            const float2 tv = __ldg(t2 + c.idx[k]);
-            const float sc = a.g.scale[l];
-            const float wg = z[0] * corner_dw(c, k, 0, sc) + z[1] * corner_dw(c, k, 1, sc) +
-                             z[2] * corner_dw(c, k, 2, sc);
-            e0 = fmaf(c.w[k], tv.x, e0);
-            e1 = fmaf(c.w[k], tv.y, e1);
-            h0 = fmaf(wg, tv.x, h0);
-            h1 = fmaf(wg, tv.y, h1);
-          }
-          in[3 + 2 * l] = e0;
-          in[4 + 2 * l] = e1;
-          z[3 + 2 * l] = h0;
-          z[4 + 2 * l] = h1;
-        }
-      }
-    }
-    // phase 1: hidden layer; delta, u, dw1; de = W0e^T delta, v = W0e^T u
-    float de[2 * kMaxL], vv[2 * kMaxL];
-#pragma unroll
-    for (int k = 0; k < 2 * kMaxL; ++k) {
-      de[k] = 0.0f;
-      vv[k] = 0.0f;
-    }
-#pragma unroll 1
-    for (int j = 0; j < kH; ++j) {
-      const float h = hidden_pre(s_w0, s_b0, j, in, n_in4);
-      const float w1 = s_w1[j];
-      const float g1 = softplus_grad(h, a.beta, a.thresh);
-      const float u = w1 * g1;
-      const float4* wr = reinterpret_cast<const float4*>(s_w0 + j * kDinPad);
-      float mu = 0.0f;
-#pragma unroll
-      for (int q = 0; q < kDinPad / 4; ++q) {
-        if (q < n_in4) {
-          const float4 w = wr[q];
-          mu = fmaf(w.x, z[4 * q], mu);
-          mu = fmaf(w.y, z[4 * q + 1], mu);
-          mu = fmaf(w.z, z[4 * q + 2], mu);
-          mu = fmaf(w.w, z[4 * q + 3], mu);
-        }
-      }
-      const float delta = mu * w1 * softplus_grad2(h, a.beta, a.thresh) + rho * w1 * g1;
-      s_u[t * kH + j] = u;
-      s_d[t * kH + j] = delta;
-      s_dw1[t * kH + j] = mu * g1 + rho * softplus_fwd(h, a.beta, a.thresh);
-#pragma unroll
-      for (int q = 0; q < kDinPad / 4; ++q) {
-        if (q < n_in4) {
-          const float4 w4 = wr[q];
-          const float wc[4] = {w4.x, w4.y, w4.z, w4.w};
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const int k = 4 * q + e - 3;  // encoding feature of input column 4q+e
-            if (k >= 0 && k < 2 * kMaxL) {
-              de[k] = fmaf(wc[e], delta, de[k]);
-              vv[k] = fmaf(wc[e], u, vv[k]);
-            }
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < kDinPad; ++i) {
-      s_in[t * kDinPad + i] = in[i];
-      s_z[t * kDinPad + i] = z[i];
-    }
-    s_rho[t] = rho;
-    // phase 2: table gradient (first- and second-order terms)
-    if (gt2) {
-      const float x[3] = {in[0], in[1], in[2]};
-#pragma unroll
-      for (int l = 0; l < kMaxL; ++l) {
-        if (l < a.active) {
-          LevelCorners c;
-          level_corners(a.g, l, x, c);
-          const float sc = a.g.scale[l];
-          const bool uni = warp_same_cell(c);
-#pragma unroll
-          for (int k = 0; k < 8; ++k) {
-            const float wg = z[0] * corner_dw(c, k, 0, sc) + z[1] * corner_dw(c, k, 1, sc) +
-                             z[2] * corner_dw(c, k, 2, sc);
-            float g0 = live ? de[2 * l] * c.w[k] + vv[2 * l] * wg : 0.0f;
-            float g1 = live ? de[2 * l + 1] * c.w[k] + vv[2 * l + 1] * wg : 0.0f;
-            if (uni) {
-#pragma unroll
-              for (int o = 16; o > 0; o >>= 1) {
-                g0 += __shfl_xor_sync(0xffffffffu, g0, o);
-                g1 += __shfl_xor_sync(0xffffffffu, g1, o);
-              }
-              if (lane == k) atomicAdd(gt2 + c.idx[k], make_float2(g0, g1));
-            } else if (live) {
-              atomicAdd(gt2 + c.idx[k], make_float2(g0, g1));
-            }
-          }
-        }
-      }
-    }
-    __syncthreads();
-    // phase 3: weight gradients over the batch
-    const int batch = (int)((n - base) < kBwdThreads ? (n - base) : kBwdThreads);
-    for (int q = 0; q < batch; ++q) {
-      const float4 dq = reinterpret_cast<const float4*>(s_d + q * kH)[rg];
-      const float4 uq = reinterpret_cast<const float4*>(s_u + q * kH)[rg];
-      const float4 wq = reinterpret_cast<const float4*>(s_dw1 + q * kH)[rg];
-      const float dr[4] = {dq.x, dq.y, dq.z, dq.w};
-      const float ur[4] = {uq.x, uq.y, uq.z, uq.w};
-      const float wr1[4] = {wq.x, wq.y, wq.z, wq.w};
-      const float* iq = s_in + q * kDinPad;
-      const float* zq = s_z + q * kDinPad;
-#pragma unroll
-      for (int m = 0; m < 5; ++m) {
-        const int i = cg + 8 * m;
-        if (i < din_used) {
-          const float iv = iq[i], zv = zq[i];
-#pragma unroll
-          for (int r = 0; r < 4; ++r) acc_w0[r][m] = fmaf(dr[r], iv, fmaf(ur[r], zv, acc_w0[r][m]));
-        }
-      }
-      if (cg == 0) {
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          acc_b0[r] += dr[r];
-          acc_w1[r] += wr1[r];
-        }
-      }
-      if (t == 0) acc_b1 += s_rho[q];
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int j = 4 * rg + r;
-    if (a.grad_w0) {
-#pragma unroll
-      for (int m = 0; m < 5; ++m) {
-        const int i = cg + 8 * m;
-        if (i < din_used && acc_w0[r][m] != 0.0f) atomicAdd(a.grad_w0 + j * a.din + i, acc_w0[r][m]);
-      }
-    }
-    if (cg == 0) {
-      if (a.grad_b0 && acc_b0[r] != 0.0f) atomicAdd(a.grad_b0 + j, acc_b0[r]);
-      if (a.grad_w1 && acc_w1[r] != 0.0f) atomicAdd(a.grad_w1 + j, acc_w1[r]);
-    }
-  }
-  if (a.grad_b1 && t == 0 && acc_b1 != 0.0f) atomicAdd(a.grad_b1, acc_b1);
-}
-
-constexpr size_t kGradBwdSmem =
-    (kSmemMlpFloats + kBwdThreads * (2 * kDinPad + 3 * kH + 1)) * sizeof(float);
 
 // --- standalone encoding (tcnn.Encoding forward / backward) -----------------
 __global__ void hashgrid_fwd_kernel(int64_t n, const float* __restrict__ x,
@@ -672,12 +443,9 @@ int sn_field_grad_bwd(int64_t n, const int32_t* count, const float* x, const flo
   a.grad_b0 = grad_b0;
   a.grad_w1 = grad_w1;
   a.grad_b1 = grad_b1;
+  a.pair16 = (reinterpret_cast<uintptr_t>(grad_table) & 15u) == 0;
   if (n == 0) return SN_OK;
-  GradBwdArgs b{grad_grad, grad_sdf};
-  SN_TRY(ensure_smem_limit(reinterpret_cast<const void*>(field_grad_bwd_kernel), kGradBwdSmem, "field_grad_bwd_kernel"));
-  field_grad_bwd_kernel<<<stride_grid(n, kBwdThreads, 1), kBwdThreads, kGradBwdSmem,
-                          as_stream(stream)>>>(a, b);
-  return check_launch("field_grad_bwd");
+  return field_grad_bwd_tc(a, grad_grad, grad_sdf, as_stream(stream));
 }
 
 int sn_weightnorm_fwd(int rows, int cols, const float* v, const float* g, float* w, float* norms,

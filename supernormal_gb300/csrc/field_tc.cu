@@ -890,6 +890,461 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
 }
 
 
+// ---------------------------------------------------------------------------
+// second-order adjoint of d sdf / d x (SDFNetwork.gradient with create_graph)
+// ---------------------------------------------------------------------------
+// With IN = [e, x] and Z = [eta, gamma] in the permuted input order (eta = E
+// gamma, E = d e / d x), h = IN W0^T + b0 and the sdf row w1 of W1:
+//   H = IN W0^T, MU = Z W0^T                                  (first MMAs)
+//   u = w1 softplus'(h), delta = MU w1 softplus''(h) + rho w1 softplus'(h)
+//   DE = delta W0, VV = u W0 (encoding columns)               (second MMAs)
+//   dT_{c,f} += DE_{l,f} w_c + VV_{l,f} (gamma . d w_c / d x)  (scatter)
+//   dW0 += delta^T IN + u^T Z over the CTA's points           (third MMAs)
+//   db0 += delta (row of ones in IN^T, zero in Z^T),
+//   dw1 += MU softplus'(h) + rho softplus(h), db1 += rho.
+// The third MMAs run in two halves through the same shared-memory operands
+// (delta with IN^T, then u with Z^T), each waited for before its operands
+// are overwritten.
+//
+// TMEM columns (512): H [0,64), later DE [0,32); MU [64,128), later VV
+// [64,96); IN rows hi/lo [128,208) and Z rows hi/lo [208,288), and after the
+// first MMAs delta hi/lo [128,256) and u hi/lo [256,384) (A of the second
+// MMAs); dW0 accumulates in [384,432).
+constexpr uint32_t kGColH = 0, kGColMu = 64, kGColInHi = 128, kGColInLo = 128 + kK1, kGColZHi = 208,
+                   kGColZLo = 208 + kK1, kGColDHi = 128, kGColDLo = 192, kGColUHi = 256, kGColULo = 320,
+                   kGColDw0 = 384;
+constexpr int kGradMembers = 8;
+
+struct GradSmem {
+  static constexpr uint32_t b1_hi = 0, b1_lo = 10240, b2_hi = 20480, b2_lo = 32768, a3 = 45056,
+                            b3_hi = a3 + 16 * kSboP, b3_lo = b3_hi + 6 * kSboP, w1 = b3_lo + 6 * kSboP,
+                            b0 = w1 + kH * 4, dw1 = b0 + kH * 4, db1 = dw1 + kH * 4, bar = db1 + 16,
+                            bar3 = bar + 8, slot = bar3 + 8, end = slot + 8;
+};
+constexpr size_t kGradSmemBytes = GradSmem::end;
+static_assert(GradSmem::end <= 227 * 1024, "second-order shared memory map");
+
+// Table-gradient contributions of the warp's points at one level with given
+// per-corner values v[k] (the same lane grouping and atomics as scatter_level).
+__device__ __forceinline__ void scatter_level_values(const GridDev& gd, int l, const LevelCorners& c,
+                                                     const float2 v[8], bool live, bool pair16, float2* gt2,
+                                                     int lane) {
+  constexpr unsigned kAll = 0xffffffffu;
+  unsigned rest = __ballot_sync(kAll, live);
+  for (int it = 0; it < kMaxCellGroups && rest != 0u; ++it) {
+    const int ld = __ffs(rest) - 1;
+    const uint32_t c0 = __shfl_sync(kAll, c.cell[0], ld);
+    const uint32_t c1 = __shfl_sync(kAll, c.cell[1], ld);
+    const uint32_t c2 = __shfl_sync(kAll, c.cell[2], ld);
+    const bool in = ((rest >> lane) & 1u) & (c.cell[0] == c0) & (c.cell[1] == c1) & (c.cell[2] == c2);
+    const unsigned gm = __ballot_sync(kAll, in);
+    if (__popc(gm) < kMinGroupLanes) break;  // the same decision on every lane
+    float s[16];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      s[2 * k] = in ? v[k].x : 0.0f;
+      s[2 * k + 1] = in ? v[k].y : 0.0f;
+    }
+    float a8[8], a4[4], a2[2];
+    bool up = lane & 16;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a8[i] = (up ? s[i + 8] : s[i]) + __shfl_xor_sync(kAll, up ? s[i] : s[i + 8], 16);
+    up = lane & 8;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a4[i] = (up ? a8[i + 4] : a8[i]) + __shfl_xor_sync(kAll, up ? a8[i] : a8[i + 4], 8);
+    up = lane & 4;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) a2[i] = (up ? a4[i + 2] : a4[i]) + __shfl_xor_sync(kAll, up ? a4[i] : a4[i + 2], 4);
+#pragma unroll
+    for (int sft = 2; sft > 0; sft >>= 1) {
+      a2[0] += __shfl_xor_sync(kAll, a2[0], sft);
+      a2[1] += __shfl_xor_sync(kAll, a2[1], sft);
+    }
+    const int k = lane >> 2;  // corner summed into lanes 4k..4k+3
+    if ((lane & 3) == 0)
+      atomicAdd(gt2 + corner_index(gd, l, c0 + (k & 1), c1 + ((k >> 1) & 1), c2 + (k >> 2)),
+                make_float2(a2[0], a2[1]));
+    rest &= ~gm;
+  }
+  if ((rest >> lane) & 1u) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const uint32_t i0 = c.idx[2 * m], i1 = c.idx[2 * m + 1];
+      const float2 v0 = v[2 * m], v1 = v[2 * m + 1];
+      if (pair16 && i1 == (i0 ^ 1u)) {
+        const float4 q = (i0 & 1u) ? make_float4(v1.x, v1.y, v0.x, v0.y) : make_float4(v0.x, v0.y, v1.x, v1.y);
+        atomicAdd(reinterpret_cast<float4*>(gt2 + (i0 & ~1u)), q);
+      } else {
+        atomicAdd(gt2 + i0, v0);
+        atomicAdd(gt2 + i1, v1);
+      }
+    }
+  }
+}
+
+// gamma . d w_k / d x for the 8 corners (trilinear weight derivatives).
+__device__ __forceinline__ void corner_dir_derivs(const LevelCorners& c, float s, const float gam[3], float wg[8]) {
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    wg[k] = gam[0] * corner_dw(c, k, 0, s) + gam[1] * corner_dw(c, k, 1, s) + gam[2] * corner_dw(c, k, 2, s);
+}
+
+// Member g's levels of point x: encoding e and eta = E gamma.
+template <int M>
+__device__ __forceinline__ void encode_eta_group(const FieldArgs& a, int g, bool live, const float x[3],
+                                                 const float gam[3], float e[2 * (16 / M)],
+                                                 float eta[2 * (16 / M)]) {
+  constexpr int kLpm = 16 / M;
+#pragma unroll
+  for (int i = 0; i < kLpm; ++i) {
+    const int l = level_of<M>(g, i);
+    float e0 = 0.0f, e1 = 0.0f, h0 = 0.0f, h1 = 0.0f;
+    if (live && l < a.active) {
+      LevelCorners c;
+      level_corners(a.g, l, x, c);
+      float2 tv[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) tv[k] = load_entry(a, c.idx[k]);
+      float wg[8];
+      corner_dir_derivs(c, a.g.scale[l], gam, wg);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        e0 = __fmaf_rn(c.w[k], tv[k].x, e0);
+        e1 = __fmaf_rn(c.w[k], tv[k].y, e1);
+        h0 = fmaf(wg[k], tv[k].x, h0);
+        h1 = fmaf(wg[k], tv[k].y, h1);
+      }
+    }
+    e[2 * i] = e0;
+    e[2 * i + 1] = e1;
+    eta[2 * i] = h0;
+    eta[2 * i + 1] = h1;
+  }
+}
+
+// A = [rows hi; rows lo] of a3 (M = 128, K = the tile's points) times B = the
+// staged transposed inputs (N = 48) hi and lo, accumulated into dW0.
+__device__ __forceinline__ void issue_grad_mma3(uint32_t tbase, const uint8_t* sm, bool fresh, bool one_pass) {
+  const uint32_t idesc = tc::idesc_tf32(kTile, kN2);
+  const uint32_t d3 = tc::taddr(tbase, 0, kGColDw0);
+  const uint64_t da = tc::smem_desc(tc::smem_u32(sm + GradSmem::a3), kLboP, kSboP),
+                 dbh = tc::smem_desc(tc::smem_u32(sm + GradSmem::b3_hi), kLboP, kSboP),
+                 dbl = tc::smem_desc(tc::smem_u32(sm + GradSmem::b3_lo), kLboP, kSboP);
+  for (int ks = 0; ks < kTile / 8; ++ks) {
+    const uint64_t k0 = (2u * kLboP * ks) >> 4;
+    tc::mma_ss(d3, da + k0, dbh + k0, idesc, (fresh && ks == 0) ? 0u : 1u);
+    if (!one_pass) tc::mma_ss(d3, da + k0, dbl + k0, idesc, 1);
+  }
+}
+
+// 3xTF32 D = A W^T with A in TMEM (hi at a_hi, lo at a_lo), W staged hi/lo.
+__device__ __forceinline__ void mma_3x(uint32_t d, uint32_t a_hi, uint32_t a_lo, uint64_t w_hi, uint64_t w_lo,
+                                       int ksteps, uint32_t idesc) {
+  mma_chain(d, a_hi, w_hi, ksteps, idesc, true);
+  mma_chain(d, a_lo, w_hi, ksteps, idesc, false);
+  mma_chain(d, a_hi, w_lo, ksteps, idesc, false);
+}
+
+// Writes v (hi/lo) as row `row` (hi) and row + kH (lo) of a3, column pt.
+__device__ __forceinline__ void st_a3(uint8_t* a3, int row, int pt, float v) {
+  uint32_t hi, lo;
+  tc::tf32_split(v, hi, lo);
+  st_smem_u32(a3, tc::kmajor_offset_strided(row, pt, kLboP, kSboP), hi);
+  st_smem_u32(a3, tc::kmajor_offset_strided(kH + row, pt, kLboP, kSboP), lo);
+}
+// Writes v (hi/lo) as row `row` of the transposed inputs, column pt.
+__device__ __forceinline__ void st_b3(uint8_t* b3_hi, uint8_t* b3_lo, int row, int pt, float v) {
+  uint32_t hi, lo;
+  tc::tf32_split(v, hi, lo);
+  const uint32_t off = tc::kmajor_offset_strided(row, pt, kLboP, kSboP);
+  st_smem_u32(b3_hi, off, hi);
+  st_smem_u32(b3_lo, off, lo);
+}
+
+template <int M>
+__global__ void __launch_bounds__(128 * M, 1)
+field_grad_bwd_tc_kernel(FieldArgs a, const float* __restrict__ gamma, const float* __restrict__ rho_in) {
+  constexpr int kNt = 128 * M;
+  constexpr int kLpm = 16 / M;
+  constexpr int kFpm = 2 * kLpm;
+  constexpr int kHpm = kH / M;
+  static_assert(kHpm == 8 && kFpm == 4, "eight members per quadrant");
+  extern __shared__ __align__(1024) uint8_t sm[];
+  float* s_w1 = reinterpret_cast<float*>(sm + GradSmem::w1);
+  float* s_b0 = reinterpret_cast<float*>(sm + GradSmem::b0);
+  float* s_dw1 = reinterpret_cast<float*>(sm + GradSmem::dw1);
+  float* s_db1 = reinterpret_cast<float*>(sm + GradSmem::db1);
+  uint8_t* a3 = sm + GradSmem::a3;
+  uint8_t* b3_hi = sm + GradSmem::b3_hi;
+  uint8_t* b3_lo = sm + GradSmem::b3_lo;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + GradSmem::bar);
+  uint64_t* bar3 = reinterpret_cast<uint64_t*>(sm + GradSmem::bar3);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + GradSmem::slot);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int q = warp & 3, g = warp >> 2;
+  const int pt = 32 * q + lane;
+  const bool want_table = a.grad_table != nullptr;
+
+  stage_w0<M>(a, sm + GradSmem::b1_hi, sm + GradSmem::b1_lo, sm + GradSmem::b2_hi, sm + GradSmem::b2_lo);
+  if (t < kH) {
+    s_w1[t] = a.w1[t];  // the sdf row of W1
+    s_b0[t] = a.b0[t];
+    s_dw1[t] = 0.0f;
+  }
+  if (t == 0) s_db1[0] = 0.0f;
+  // constant rows of the transposed inputs: zeros above the ones row (row
+  // kOnesRow is written per tile: one for IN^T, zero for Z^T)
+  for (int e = t; e < (kN2 - kOnesRow - 1) * kTile; e += kNt) {
+    const int r = kOnesRow + 1 + e / kTile, c = e % kTile;
+    const uint32_t off = tc::kmajor_offset_strided(r, c, kLboP, kSboP);
+    st_smem_u32(b3_hi, off, 0u);
+    st_smem_u32(b3_lo, off, 0u);
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(slot, kBwdCols);
+    tc::tmem_relinquish();
+  }
+  if (t == 0) {
+    tc::mbar_init(bar, 1);
+    tc::mbar_init(bar3, 1);
+  }
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = *slot;
+  const uint32_t lb = (uint32_t)(32 * q);
+  const uint32_t idesc1 = tc::idesc_tf32(kTile, kH), idesc2 = tc::idesc_tf32(kTile, 32);
+  const uint32_t sbo1 = (kK1 / 4) * 128u, sbo2 = (kH / 4) * 128u;
+  const uint64_t w1_hi = tc::smem_desc(tc::smem_u32(sm + GradSmem::b1_hi), 128u, sbo1),
+                 w1_lo = tc::smem_desc(tc::smem_u32(sm + GradSmem::b1_lo), 128u, sbo1),
+                 w2_hi = tc::smem_desc(tc::smem_u32(sm + GradSmem::b2_hi), 128u, sbo2),
+                 w2_lo = tc::smem_desc(tc::smem_u32(sm + GradSmem::b2_lo), 128u, sbo2);
+  const float inv_beta = 1.0f / a.beta;
+  uint32_t phase = 0, phase3 = 0;
+  bool ok = true, first = true, pending3 = false;
+
+  const int64_t n = effective_n(a);
+  const int64_t n_tiles = (n + kTile - 1) / kTile;
+  float xn[3], gn[3], rn = 0.0f;
+  auto load_next = [&](int64_t p) {
+    load_point(a, p, n, xn);
+    const bool in = p < n;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) gn[d] = in ? gamma[3 * p + d] : 0.0f;
+    rn = (in && rho_in) ? rho_in[p] : 0.0f;
+  };
+  load_next((int64_t)blockIdx.x * kTile + pt);
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int64_t p = tile * kTile + pt;
+    const bool live = p < n;
+    const float x[3] = {xn[0], xn[1], xn[2]};
+    const float gam[3] = {gn[0], gn[1], gn[2]};
+    const float rho = rn;
+    load_next((tile + gridDim.x) * kTile + pt);
+    // ---- IN and Z rows (TMEM, A of the first MMAs), IN^T (B of the third) ----
+    float eta[kFpm];
+    bool ok3 = true;
+    {
+      float e[kFpm];
+      encode_eta_group<M>(a, g, live, x, gam, e, eta);
+      st_split<kFpm>(tc::taddr(tbase, lb, kGColInHi + kFpm * g), tc::taddr(tbase, lb, kGColInLo + kFpm * g), e);
+      st_split<kFpm>(tc::taddr(tbase, lb, kGColZHi + kFpm * g), tc::taddr(tbase, lb, kGColZLo + kFpm * g), eta);
+      if (g == 0) {
+        const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        const float gv[8] = {gam[0], gam[1], gam[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        st_split8(tc::taddr(tbase, lb, kGColInHi + kXCol), tc::taddr(tbase, lb, kGColInLo + kXCol), xv);
+        st_split8(tc::taddr(tbase, lb, kGColZHi + kXCol), tc::taddr(tbase, lb, kGColZLo + kXCol), gv);
+      }
+      // the previous tile's u^T Z MMAs still read a3 and the transposed inputs
+      if (pending3) {
+        ok3 = tc::mbar_wait_bounded(bar3, phase3);
+        if (ok3) {
+          phase3 ^= 1u;
+          pending3 = false;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kFpm; ++i) st_b3(b3_hi, b3_lo, kFpm * g + i, pt, e[i]);
+      if (g == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) st_b3(b3_hi, b3_lo, kXCol + d, pt, x[d]);
+        const uint32_t off = tc::kmajor_offset_strided(kOnesRow, pt, kLboP, kSboP);
+        st_smem_u32(b3_hi, off, __float_as_uint(1.0f));
+        st_smem_u32(b3_lo, off, 0u);
+      }
+    }
+    tc::tmem_wait_st();
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    if (!__syncthreads_and(ok3)) {
+      ok = false;
+      break;
+    }
+    if (t == 0) {  // H = IN W0^T, MU = Z W0^T (M=128, N=64, K=40)
+      tc::fence_after_sync();
+      mma_3x(tc::taddr(tbase, 0, kGColH), tc::taddr(tbase, 0, kGColInHi), tc::taddr(tbase, 0, kGColInLo), w1_hi,
+             w1_lo, kK1 / 8, idesc1);
+      mma_3x(tc::taddr(tbase, 0, kGColMu), tc::taddr(tbase, 0, kGColZHi), tc::taddr(tbase, 0, kGColZLo), w1_hi,
+             w1_lo, kK1 / 8, idesc1);
+      tc::mma_commit(bar);
+    }
+    bool got = tc::mbar_wait_bounded(bar, phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(got)) {
+      ok = false;
+      break;
+    }
+    tc::fence_after_sync();
+    // ---- u, delta, dw1 for this member's hidden units 8g .. 8g + 7 ----
+    float u[kHpm];
+    {
+      float h[kHpm], mu[kHpm];
+      tc::tmem_ld8(tc::taddr(tbase, lb, kGColH + kHpm * g), h);
+      tc::tmem_ld8(tc::taddr(tbase, lb, kGColMu + kHpm * g), mu);
+      tc::tmem_wait_ld();
+      float dl[kHpm], v[kHpm];
+#pragma unroll
+      for (int i = 0; i < kHpm; ++i) {
+        const int j = kHpm * g + i;
+        const float pre = h[i] + s_b0[j];
+        float act, s1;
+        softplus_fwd_grad_fast(pre, a.beta, inv_beta, a.thresh, act, s1);
+        const float s2 = pre * a.beta > a.thresh ? 0.0f : a.beta * s1 * (1.0f - s1);
+        const float w1 = s_w1[j];
+        u[i] = live ? w1 * s1 : 0.0f;
+        dl[i] = live ? fmaf(mu[i] * w1, s2, rho * w1 * s1) : 0.0f;
+        v[i] = live ? fmaf(mu[i], s1, rho * act) : 0.0f;
+      }
+      const float r = warp_reduce_scatter8(v, lane);
+      if ((lane & 3) == 0) atomicAdd(s_dw1 + kHpm * g + (lane >> 2), r);
+      if (g == 0) {
+        float rs = live ? rho : 0.0f;
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, s);
+        if (lane == 0) atomicAdd(s_db1, rs);
+      }
+      st_split8(tc::taddr(tbase, lb, kGColDHi + kHpm * g), tc::taddr(tbase, lb, kGColDLo + kHpm * g), dl);
+      st_split8(tc::taddr(tbase, lb, kGColUHi + kHpm * g), tc::taddr(tbase, lb, kGColULo + kHpm * g), u);
+#pragma unroll
+      for (int i = 0; i < kHpm; ++i) st_a3(a3, kHpm * g + i, pt, dl[i]);
+    }
+    tc::tmem_wait_st();
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (t == 0) {  // DE = delta W0, VV = u W0 (M=128, N=32 encoding columns, K=64)
+      tc::fence_after_sync();
+      mma_3x(tc::taddr(tbase, 0, kGColH), tc::taddr(tbase, 0, kGColDHi), tc::taddr(tbase, 0, kGColDLo), w2_hi,
+             w2_lo, kH / 8, idesc2);
+      mma_3x(tc::taddr(tbase, 0, kGColMu), tc::taddr(tbase, 0, kGColUHi), tc::taddr(tbase, 0, kGColULo), w2_hi,
+             w2_lo, kH / 8, idesc2);
+      tc::mma_commit(bar);
+    } else if (t == 32) {  // dW0 += delta^T IN (db0 from the ones row)
+      tc::fence_after_sync();
+      issue_grad_mma3(tbase, sm, first, false);
+      tc::mma_commit(bar3);
+    }
+    first = false;
+    pending3 = true;
+    got = tc::mbar_wait_bounded(bar, phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(got)) {
+      ok = false;
+      break;
+    }
+    tc::fence_after_sync();
+    // ---- table gradient for this member's levels ----
+    if (want_table) {
+      float de[kFpm], vv[kFpm];
+      tc::tmem_ld4(tc::taddr(tbase, lb, kGColH + kFpm * g), de);
+      tc::tmem_ld4(tc::taddr(tbase, lb, kGColMu + kFpm * g), vv);
+      tc::tmem_wait_ld();
+      float2* gt2 = reinterpret_cast<float2*>(a.grad_table);
+#pragma unroll
+      for (int i = 0; i < kLpm; ++i) {
+        const int l = level_of<M>(g, i);
+        if (l < a.active) {
+          LevelCorners c;
+          level_corners(a.g, l, x, c);
+          float wg[8];
+          corner_dir_derivs(c, a.g.scale[l], gam, wg);
+          float2 v[8];
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            v[k] = live ? make_float2(fmaf(de[2 * i], c.w[k], vv[2 * i] * wg[k]),
+                                      fmaf(de[2 * i + 1], c.w[k], vv[2 * i + 1] * wg[k]))
+                        : make_float2(0.0f, 0.0f);
+          scatter_level_values(a.g, l, c, v, live, a.pair16, gt2, lane);
+        }
+      }
+    }
+    // ---- dW0 += u^T Z: wait for delta^T IN, then reuse its operands ----
+    ok3 = tc::mbar_wait_bounded(bar3, phase3);
+    if (ok3) {
+      phase3 ^= 1u;
+      pending3 = false;
+    }
+    if (ok3) {
+#pragma unroll
+      for (int i = 0; i < kHpm; ++i) st_a3(a3, kHpm * g + i, pt, u[i]);
+#pragma unroll
+      for (int i = 0; i < kFpm; ++i) st_b3(b3_hi, b3_lo, kFpm * g + i, pt, eta[i]);
+      if (g == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) st_b3(b3_hi, b3_lo, kXCol + d, pt, gam[d]);
+        const uint32_t off = tc::kmajor_offset_strided(kOnesRow, pt, kLboP, kSboP);
+        st_smem_u32(b3_hi, off, 0u);
+        st_smem_u32(b3_lo, off, 0u);
+      }
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    if (!__syncthreads_and(ok3)) {
+      ok = false;
+      break;
+    }
+    if (t == 32) {
+      tc::fence_after_sync();
+      issue_grad_mma3(tbase, sm, false, false);
+      tc::mma_commit(bar3);
+    }
+    pending3 = true;
+  }
+  if (!ok) (void)tc::mbar_wait_bounded(bar, phase ^ 1u);  // drain a timed-out first/second MMA
+  if (pending3) ok = tc::mbar_wait_bounded(bar3, phase3) && ok;
+  ok = __syncthreads_and(ok);
+  if (!ok && t == 0 && a.status) atomicOr(a.status, SN_STATUS_TIMEOUT);
+  tc::fence_after_sync();
+  if (ok && !first) {
+    // dW0 / db0: lanes 0..63 hold the hi rows, 64..127 the lo rows
+    if (g == 0) {
+      const int j = pt & (kH - 1);
+#pragma unroll
+      for (int c0 = 0; c0 < kN2; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tc::taddr(tbase, lb, kGColDw0 + c0), v);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int c = c0 + i;
+          if (c == kOnesRow) {
+            if (a.grad_b0) atomicAdd(a.grad_b0 + j, v[i]);
+          } else if (c < kK1 && a.grad_w0) {
+            const int col = w0_col<M>(c, a.g.L);
+            if (col >= 0 && v[i] != 0.0f) atomicAdd(a.grad_w0 + j * a.din + col, v[i]);
+          }
+        }
+      }
+    }
+    if (a.grad_w1 && t < kH && s_dw1[t] != 0.0f) atomicAdd(a.grad_w1 + t, s_dw1[t]);
+    if (a.grad_b1 && t == 0 && s_db1[0] != 0.0f) atomicAdd(a.grad_b1, s_db1[0]);
+  }
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tbase, kBwdCols);
+}
+
 }  // namespace
 
 // Launchers used by sn_field_fwd / sn_field_bwd (field.cu).
@@ -921,6 +1376,17 @@ int field_fwd_tc_segments(const FieldArgs* segs, int n_seg, cudaStream_t st) {
 }
 
 int field_fwd_tc(const FieldArgs& a, cudaStream_t st) { return field_fwd_tc_segments(&a, 1, st); }
+
+int field_grad_bwd_tc(const FieldArgs& a, const float* gamma, const float* rho, cudaStream_t st) {
+  constexpr int M = kGradMembers;
+  const void* fn = reinterpret_cast<const void*>(field_grad_bwd_tc_kernel<M>);
+  SN_TRY(ensure_smem_limit(fn, kGradSmemBytes, "field_grad_bwd"));
+  const int64_t n_tiles = (a.cap + kTile - 1) / kTile;
+  const int64_t cap = num_sms();
+  const unsigned grid = (unsigned)(n_tiles < cap ? n_tiles : cap);
+  field_grad_bwd_tc_kernel<M><<<grid, 128 * M, kGradSmemBytes, st>>>(a, gamma, rho);
+  return check_launch("field_grad_bwd");
+}
 
 int field_bwd_tc(const FieldArgs& a, cudaStream_t st) {
   constexpr int M = kBwdMembers;
