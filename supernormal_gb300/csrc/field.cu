@@ -28,127 +28,6 @@
 
 namespace sn {
 
-// Load W0 (row stride kDinPad, zero padded), b0, W1 rows < out_cols, b1.
-__device__ void load_mlp(const FieldArgs& a, float* s_w0, float* s_b0, float* s_w1, float* s_b1) {
-  for (int t = threadIdx.x; t < kH * kDinPad; t += blockDim.x) {
-    const int j = t / kDinPad, i = t - j * kDinPad;
-    s_w0[t] = i < a.din ? a.w0[j * a.din + i] : 0.0f;
-  }
-  for (int t = threadIdx.x; t < kH; t += blockDim.x) s_b0[t] = a.b0[t];
-  for (int t = threadIdx.x; t < kDoutMax * kH; t += blockDim.x) {
-    const int o = t / kH;
-    s_w1[t] = o < a.out_cols ? a.w1[t] : 0.0f;
-  }
-  for (int t = threadIdx.x; t < kDoutMax; t += blockDim.x) s_b1[t] = t < a.out_cols ? a.b1[t] : 0.0f;
-}
-
-constexpr int kSmemMlpFloats = kH * kDinPad + kH + kDoutMax * kH + kDoutMax;
-
-__device__ __forceinline__ void build_input(const FieldArgs& a, int64_t p, float in[kDinPad]) {
-  const float x[3] = {a.x[3 * p], a.x[3 * p + 1], a.x[3 * p + 2]};
-  in[0] = x[0];
-  in[1] = x[1];
-  in[2] = x[2];
-#pragma unroll
-  for (int l = 0; l < kMaxL; ++l) {
-    float e0 = 0.0f, e1 = 0.0f;
-    if (l < a.active) encode_level(a.table, a.g, l, x, e0, e1);
-    in[3 + 2 * l] = e0;
-    in[4 + 2 * l] = e1;
-  }
-  in[kDinPad - 1] = 0.0f;
-}
-
-__device__ __forceinline__ float hidden_pre(const float* s_w0, const float* s_b0, int j,
-                                            const float in[kDinPad], int n_in4) {
-  const float4* wr = reinterpret_cast<const float4*>(s_w0 + j * kDinPad);
-  float h = s_b0[j];
-#pragma unroll
-  for (int q = 0; q < kDinPad / 4; ++q) {
-    if (q < n_in4) {
-      const float4 w = wr[q];
-      h = fmaf(w.x, in[4 * q], h);
-      h = fmaf(w.y, in[4 * q + 1], h);
-      h = fmaf(w.z, in[4 * q + 2], h);
-      h = fmaf(w.w, in[4 * q + 3], h);
-    }
-  }
-  return h;
-}
-
-constexpr size_t kFwdSmem = kSmemMlpFloats * sizeof(float);
-
-// ---------------------------------------------------------------------------
-// d sdf / d x (SDFNetwork.gradient, models/fields.py:107-119)
-// ---------------------------------------------------------------------------
-// With in = [x, e(x)], h = W0 in + b0, s = w1 . softplus(h) + b1 (w1 = row 0 of W1):
-//   u = w1 * softplus'(h),  grad = W0x^T u + E^T (W0e^T u),  E = d e / d x,
-// where e_{l,f} = sum_c w_c T_{c,f} and E_{l,f,d} = sum_c T_{c,f} d w_c / d x_d.
-// Its adjoint (the double backward of create_graph=True) is the tensor-core
-// kernel field_grad_bwd_tc_kernel (field_tc.cu).
-__global__ void __launch_bounds__(128) field_grad_fwd_kernel(FieldArgs a, float* __restrict__ out_sdf,
-                                                             float* __restrict__ out_grad) {
-  extern __shared__ float4 smem4[];
-  float* s_w0 = reinterpret_cast<float*>(smem4);
-  float* s_b0 = s_w0 + kH * kDinPad;
-  float* s_w1 = s_b0 + kH;
-  float* s_b1 = s_w1 + kDoutMax * kH;
-  load_mlp(a, s_w0, s_b0, s_w1, s_b1);
-  __syncthreads();
-  const int64_t n = effective_n(a);
-  const int n_in4 = (3 + 2 * a.active + 3) / 4;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    float in[kDinPad];
-    build_input(a, p, in);
-    float v[kDinPad];  // W0^T u: [0..2] linear part of the gradient, [3..] per-feature weights
-#pragma unroll
-    for (int i = 0; i < kDinPad; ++i) v[i] = 0.0f;
-    float s = s_b1[0];
-#pragma unroll 2
-    for (int j = 0; j < kH; ++j) {
-      const float h = hidden_pre(s_w0, s_b0, j, in, n_in4);
-      const float w1 = s_w1[j];
-      s = fmaf(w1, softplus_fwd(h, a.beta, a.thresh), s);
-      const float u = w1 * softplus_grad(h, a.beta, a.thresh);
-      const float4* wr = reinterpret_cast<const float4*>(s_w0 + j * kDinPad);
-#pragma unroll
-      for (int q = 0; q < kDinPad / 4; ++q) {
-        if (q < n_in4) {
-          const float4 w = wr[q];
-          v[4 * q + 0] = fmaf(w.x, u, v[4 * q + 0]);
-          v[4 * q + 1] = fmaf(w.y, u, v[4 * q + 1]);
-          v[4 * q + 2] = fmaf(w.z, u, v[4 * q + 2]);
-          v[4 * q + 3] = fmaf(w.w, u, v[4 * q + 3]);
-        }
-      }
-    }
-    float gx[3] = {v[0], v[1], v[2]};
-    const float x[3] = {in[0], in[1], in[2]};
-    const float2* t2 = reinterpret_cast<const float2*>(a.table);
-#pragma unroll
-    for (int l = 0; l < kMaxL; ++l) {
-      if (l < a.active) {
-        LevelCorners c;
-        level_corners(a.g, l, x, c);
-        const float v0 = v[3 + 2 * l], v1 = v[4 + 2 * l];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          const float2 tv = __ldg(t2 + c.idx[k]);
-          const float gk = v0 * tv.x + v1 * tv.y;
-#pragma unroll
-          for (int d = 0; d < 3; ++d) gx[d] = fmaf(gk, corner_dw(c, k, d, a.g.scale[l]), gx[d]);
-        }
-      }
-    }
-    if (out_sdf) out_sdf[p] = s;
-    out_grad[3 * p + 0] = gx[0];
-    out_grad[3 * p + 1] = gx[1];
-    out_grad[3 * p + 2] = gx[2];
-  }
-}
-
-
 // --- standalone encoding (tcnn.Encoding forward / backward) -----------------
 __global__ void hashgrid_fwd_kernel(int64_t n, const float* __restrict__ x,
                                     const float* __restrict__ table, GridDev g, int active,
@@ -422,9 +301,7 @@ int sn_field_grad_fwd(int64_t n, const int32_t* count, const float* x, const flo
   }
   SN_REQUIRE(grad != nullptr, "field_grad_fwd: grad is null");
   if (n == 0) return SN_OK;
-  SN_TRY(ensure_smem_limit(reinterpret_cast<const void*>(field_grad_fwd_kernel), kFwdSmem, "field_grad_fwd_kernel"));
-  field_grad_fwd_kernel<<<stride_grid(n, 128, 8), 128, kFwdSmem, as_stream(stream)>>>(a, sdf, grad);
-  return check_launch("field_grad_fwd");
+  return field_grad_fwd_tc(a, sdf, grad, as_stream(stream));
 }
 
 int sn_field_grad_bwd(int64_t n, const int32_t* count, const float* x, const float* grad_grad,

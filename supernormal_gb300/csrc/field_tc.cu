@@ -1345,6 +1345,199 @@ field_grad_bwd_tc_kernel(FieldArgs a, const float* __restrict__ gamma, const flo
   if (warp == 0) tc::tmem_dealloc(tbase, kBwdCols);
 }
 
+// ---------------------------------------------------------------------------
+// d sdf / d x (SDFNetwork.gradient): sdf and grad = W0x^T u + E^T (W0e^T u)
+// ---------------------------------------------------------------------------
+// H = IN W0^T (first MMA), u = w1 softplus'(H + b0), sdf = w1 . softplus + b1,
+// V = u W0 (second MMA, all 48 input columns), and per point
+// grad = V_x + sum over levels and corners of (V_{l,0} T_{c,0} + V_{l,1} T_{c,1}) d w_c / d x.
+// TMEM columns (256, two CTAs per SM): H [0,64); IN rows hi/lo [64,144), after
+// the first MMA u hi/lo [64,192) (A of the second); V [192,240).
+constexpr uint32_t kFColH = 0, kFColInHi = 64, kFColInLo = 64 + kK1, kFColUHi = 64, kFColULo = 128,
+                   kFColV = 192;
+constexpr int kGradFwdMembers = 4;
+
+template <int M>
+struct GradFwdSmem {
+  static constexpr uint32_t b1_hi = 0, b1_lo = 10240, b2_hi = 20480, b2_lo = 32768, w1 = 45056, b0 = w1 + kH * 4,
+                            part = b0 + kH * 4, bar = part + M * kTile * 16, slot = bar + 8, end = slot + 8;
+  // more than 228/3 KB, so at most two CTAs (2 x 256 TMEM columns) per SM
+  static constexpr size_t bytes = 80 * 1024;
+};
+static_assert(GradFwdSmem<kGradFwdMembers>::end <= GradFwdSmem<kGradFwdMembers>::bytes, "gradient shared memory map");
+
+template <int M>
+__global__ void __launch_bounds__(128 * M, 2)
+field_grad_fwd_tc_kernel(FieldArgs a, float* __restrict__ out_sdf, float* __restrict__ out_grad) {
+  constexpr int kLpm = 16 / M;
+  constexpr int kFpm = 2 * kLpm;
+  constexpr int kHpm = kH / M;
+  static_assert(kFpm == 8 && kHpm == 16, "four members per quadrant");
+  using Sm = GradFwdSmem<M>;
+  extern __shared__ __align__(1024) uint8_t sm[];
+  float* s_w1 = reinterpret_cast<float*>(sm + Sm::w1);
+  float* s_b0 = reinterpret_cast<float*>(sm + Sm::b0);
+  float4* s_part = reinterpret_cast<float4*>(sm + Sm::part);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + Sm::bar);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + Sm::slot);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int q = warp & 3, g = warp >> 2;
+  const int pt = 32 * q + lane;
+
+  stage_w0<M>(a, sm + Sm::b1_hi, sm + Sm::b1_lo, sm + Sm::b2_hi, sm + Sm::b2_lo);
+  if (t < kH) {
+    s_w1[t] = a.w1[t];  // the sdf row of W1
+    s_b0[t] = a.b0[t];
+  }
+  const float b1v = a.b1[0];
+  if (warp == 0) {
+    tc::tmem_alloc(slot, kCols);
+    tc::tmem_relinquish();
+  }
+  if (t == 0) tc::mbar_init(bar, 1);
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = *slot;
+  const uint32_t lb = (uint32_t)(32 * q);
+  const uint32_t idesc1 = tc::idesc_tf32(kTile, kH), idesc2 = tc::idesc_tf32(kTile, kN2);
+  const uint32_t sbo1 = (kK1 / 4) * 128u, sbo2 = (kH / 4) * 128u;
+  const uint64_t w1_hi = tc::smem_desc(tc::smem_u32(sm + Sm::b1_hi), 128u, sbo1),
+                 w1_lo = tc::smem_desc(tc::smem_u32(sm + Sm::b1_lo), 128u, sbo1),
+                 w2_hi = tc::smem_desc(tc::smem_u32(sm + Sm::b2_hi), 128u, sbo2),
+                 w2_lo = tc::smem_desc(tc::smem_u32(sm + Sm::b2_lo), 128u, sbo2);
+  const float inv_beta = 1.0f / a.beta;
+  uint32_t phase = 0;
+  bool ok = true;
+
+  const int64_t n = effective_n(a);
+  const int64_t n_tiles = (n + kTile - 1) / kTile;
+  float xn[3];
+  load_point(a, (int64_t)blockIdx.x * kTile + pt, n, xn);
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int64_t p = tile * kTile + pt;
+    const bool live = p < n;
+    const float x[3] = {xn[0], xn[1], xn[2]};
+    load_point(a, (tile + gridDim.x) * kTile + pt, n, xn);
+    {
+      float e[kFpm];
+      encode_group<false, M>(a, g, live, x, e);
+      st_split<kFpm>(tc::taddr(tbase, lb, kFColInHi + kFpm * g), tc::taddr(tbase, lb, kFColInLo + kFpm * g), e);
+      if (g == 0) {
+        const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        st_split8(tc::taddr(tbase, lb, kFColInHi + kXCol), tc::taddr(tbase, lb, kFColInLo + kXCol), xv);
+      }
+    }
+    tc::tmem_wait_st();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (t == 0) {  // H = IN W0^T (M=128, N=64, K=40)
+      tc::fence_after_sync();
+      mma_3x(tc::taddr(tbase, 0, kFColH), tc::taddr(tbase, 0, kFColInHi), tc::taddr(tbase, 0, kFColInLo), w1_hi,
+             w1_lo, kK1 / 8, idesc1);
+      tc::mma_commit(bar);
+    }
+    bool got = tc::mbar_wait_bounded(bar, phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(got)) {
+      ok = false;
+      break;
+    }
+    tc::fence_after_sync();
+    // u and the sdf partial for hidden units kHpm g .. kHpm g + kHpm - 1
+    float sdf_part = 0.0f;
+    {
+      float h[kHpm], u[kHpm];
+      tc::tmem_ld16(tc::taddr(tbase, lb, kFColH + kHpm * g), h);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int i = 0; i < kHpm; ++i) {
+        const int j = kHpm * g + i;
+        float act, s1;
+        softplus_fwd_grad_fast(h[i] + s_b0[j], a.beta, inv_beta, a.thresh, act, s1);
+        u[i] = s_w1[j] * s1;
+        sdf_part = fmaf(s_w1[j], act, sdf_part);
+      }
+      st_split<kHpm>(tc::taddr(tbase, lb, kFColUHi + kHpm * g), tc::taddr(tbase, lb, kFColULo + kHpm * g), u);
+    }
+    tc::tmem_wait_st();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (t == 0) {  // V = u W0 (M=128, N=48, K=64)
+      tc::fence_after_sync();
+      mma_3x(tc::taddr(tbase, 0, kFColV), tc::taddr(tbase, 0, kFColUHi), tc::taddr(tbase, 0, kFColULo), w2_hi,
+             w2_lo, kH / 8, idesc2);
+      tc::mma_commit(bar);
+    }
+    got = tc::mbar_wait_bounded(bar, phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(got)) {
+      ok = false;
+      break;
+    }
+    tc::fence_after_sync();
+    // gradient partial: this member's levels (+ the linear x part for member 0)
+    {
+      float v[kFpm], vx[8];
+      tc::tmem_ld8(tc::taddr(tbase, lb, kFColV + kFpm * g), v);
+      tc::tmem_ld8(tc::taddr(tbase, lb, kFColV + kXCol), vx);
+      tc::tmem_wait_ld();
+      float gx[3] = {0.0f, 0.0f, 0.0f};
+      if (g == 0) {
+        gx[0] = vx[0];
+        gx[1] = vx[1];
+        gx[2] = vx[2];
+      }
+      if (live) {
+#pragma unroll
+        for (int i = 0; i < kLpm; ++i) {
+          const int l = level_of<M>(g, i);
+          if (l < a.active) {
+            LevelCorners c;
+            level_corners(a.g, l, x, c);
+            float2 tv[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) tv[k] = load_entry(a, c.idx[k]);
+            const float s = a.g.scale[l];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              const float gk = v[2 * i] * tv[k].x + v[2 * i + 1] * tv[k].y;
+#pragma unroll
+              for (int d = 0; d < 3; ++d) gx[d] = fmaf(gk, corner_dw(c, k, d, s), gx[d]);
+            }
+          }
+        }
+      }
+      s_part[g * kTile + pt] = make_float4(sdf_part, gx[0], gx[1], gx[2]);
+    }
+    __syncthreads();
+    // (the next tile writes s_part only after two more barriers)
+    if (g == 0 && live) {
+      float4 s = s_part[pt];
+#pragma unroll
+      for (int m = 1; m < M; ++m) {
+        const float4 o = s_part[m * kTile + pt];
+        s.x += o.x;
+        s.y += o.y;
+        s.z += o.z;
+        s.w += o.w;
+      }
+      if (out_sdf) out_sdf[p] = s.x + b1v;
+      out_grad[3 * p + 0] = s.y;
+      out_grad[3 * p + 1] = s.z;
+      out_grad[3 * p + 2] = s.w;
+    }
+  }
+  if (!ok) {
+    if (t == 0 && a.status) atomicOr(a.status, SN_STATUS_TIMEOUT);
+    (void)tc::mbar_wait_bounded(bar, phase ^ 1u);
+  }
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tbase, kCols);
+}
+
 }  // namespace
 
 // Launchers used by sn_field_fwd / sn_field_bwd (field.cu).
@@ -1376,6 +1569,18 @@ int field_fwd_tc_segments(const FieldArgs* segs, int n_seg, cudaStream_t st) {
 }
 
 int field_fwd_tc(const FieldArgs& a, cudaStream_t st) { return field_fwd_tc_segments(&a, 1, st); }
+
+int field_grad_fwd_tc(const FieldArgs& a, float* sdf, float* grad, cudaStream_t st) {
+  constexpr int M = kGradFwdMembers;
+  constexpr size_t smem = GradFwdSmem<M>::bytes;
+  const void* fn = reinterpret_cast<const void*>(field_grad_fwd_tc_kernel<M>);
+  SN_TRY(ensure_smem_limit(fn, smem, "field_grad_fwd"));
+  const int64_t n_tiles = (a.cap + kTile - 1) / kTile;
+  const int64_t cap = 2LL * num_sms();
+  const unsigned grid = (unsigned)(n_tiles < cap ? n_tiles : cap);
+  field_grad_fwd_tc_kernel<M><<<grid, 128 * M, smem, st>>>(a, sdf, grad);
+  return check_launch("field_grad_fwd");
+}
 
 int field_grad_bwd_tc(const FieldArgs& a, const float* gamma, const float* rho, cudaStream_t st) {
   constexpr int M = kGradMembers;
