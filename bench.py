@@ -422,6 +422,8 @@ def run_ours(args, world, rank, local):
         out["kernels_vs_reference"] = reference_kernels_leg(tr, pool[0])
     if not args.no_ad and tr.cfg.precision == "fp32":
         out["ad_step"] = ad_step_leg(args, tr, pool)
+    if tr.cfg.precision == "fp32":
+        out["mlp_precision"] = mlp_precision_leg(tr)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, budget_s=20.0)
     if args.serve != "off":
@@ -464,6 +466,52 @@ def ad_step_leg(args, tr, pool, steps: int = 10) -> dict:
     return {"ms_per_step": ms, "rays_per_s": args.batch * tr.P / (ms / 1e3), "steps": steps,
             "stages_ms_per_step": {k: v / steps for k, v in st.items()},
             "gradient_method": "ad (SDFNetwork.gradient with the second-order adjoint)"}
+
+
+def mlp_precision_leg(tr, reps: int = 20, rounds: int = 3) -> dict:
+    """The field forward over the last step's training points with the
+    first layer's tensor-core products in FP32-accurate 3xTF32 (the training
+    path), one TF32 pass (the mixed-precision path) and one BF16 pass, FP32
+    table: CUDA-event time per launch (variants interleaved) and the sdf
+    difference from 3xTF32."""
+    import ctypes as Ct
+
+    from supernormal_gb300._lib import SN_FIELD_MLP_BF16, SN_FIELD_MLP_TF32, call, stream_handle
+
+    n = int(tr.q1.item())
+    if n == 0:
+        return {"points": 0}
+    st = stream_handle()
+    table = tr.views["table"]
+    variants = {"fp32_3xtf32": 0, "tf32": SN_FIELD_MLP_TF32, "bf16": SN_FIELD_MLP_BF16}
+    outs = {k: torch.empty((n, 1), device=tr.device) for k in variants}
+    descs = {}
+    for k, f in variants.items():
+        d = tr._mlp()
+        d.flags = f
+        descs[k] = d
+    times = {k: [] for k in variants}
+    for r in range(rounds):
+        for k in variants:
+            for _ in range(3 if r == 0 else 0):
+                call("sn_field_fwd", n, None, tr.xyz1, table, Ct.byref(tr.net.encoding.desc),
+                     tr.net.active_levels(), Ct.byref(descs[k]), 1, outs[k], st)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                call("sn_field_fwd", n, None, tr.xyz1, table, Ct.byref(tr.net.encoding.desc),
+                     tr.net.active_levels(), Ct.byref(descs[k]), 1, outs[k], st)
+            e1.record()
+            torch.cuda.synchronize()
+            times[k].append(e0.elapsed_time(e1) / reps)
+    tr.check_status()
+    ref = outs["fp32_3xtf32"].double()
+    out = {"points": n, "table": "fp32", "note": "field forward over the last step's training points; "
+           "min over rounds of the mean launch time; sdf differences against the 3xTF32 launch"}
+    for k in variants:
+        diff = (outs[k].double() - ref).abs()
+        out[k] = {"ms": min(times[k]), "max_abs_diff": float(diff.max()), "rms_diff": float(diff.pow(2).mean().sqrt())}
+    return out
 
 
 def run_quality(iters: int, dev) -> dict:

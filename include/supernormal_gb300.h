@@ -269,9 +269,13 @@ typedef struct sn_mlp_desc {
  * SN_FIELD_TABLE_FP16 -- the `table` pointer addresses the hash table as FP16
  *   pairs (an FP16 copy of FP32 master weights; gradients stay FP32);
  * SN_FIELD_MLP_TF32 -- the MLP's tensor-core products in one TF32 pass
- *   instead of the FP32-accurate three. */
+ *   instead of the FP32-accurate three;
+ * SN_FIELD_MLP_BF16 -- sn_field_fwd only: the first layer's products in one
+ *   BF16 pass (inputs and W0 rounded to BF16, FP32 accumulation); the
+ *   backward and gradient entry points reject it. */
 #define SN_FIELD_TABLE_FP16 1u
 #define SN_FIELD_MLP_TF32 2u
+#define SN_FIELD_MLP_BF16 4u
 
 /* sn_mlp_desc.enc_cache (no reference counterpart; the reference's autograd
  * keeps tcnn's encoding output alive between forward and backward in the

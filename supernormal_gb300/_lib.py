@@ -24,6 +24,7 @@ SN_STATUS_CAPACITY = 2
 SN_STATUS_TIMEOUT = 4
 SN_FIELD_TABLE_FP16 = 1
 SN_FIELD_MLP_TF32 = 2
+SN_FIELD_MLP_BF16 = 4
 SN_MAX_LEVELS = 32
 
 

@@ -165,6 +165,7 @@ int fill_field_args(FieldArgs& a, int64_t n, const int32_t* count, const float* 
   a.status = mlp->status;
   a.table_half = (mlp->flags & SN_FIELD_TABLE_FP16) != 0;
   a.one_pass = (mlp->flags & SN_FIELD_MLP_TF32) != 0;
+  a.bf16 = (mlp->flags & SN_FIELD_MLP_BF16) != 0;
   return SN_OK;
 }
 
@@ -273,6 +274,10 @@ int sn_field_bwd(int64_t n, const int32_t* count, const float* x, const float* g
                  float* grad_w1, float* grad_b1, float* grad_x, void* stream) {
   FieldArgs a;
   SN_TRY(fill_field_args(a, n, count, x, table, grid, active_levels, mlp, out_cols));
+  if (a.bf16) {
+    set_error("field_bwd: SN_FIELD_MLP_BF16 is supported by sn_field_fwd only");
+    return SN_ERR_UNSUPPORTED;
+  }
   SN_REQUIRE(grad_out != nullptr, "field_bwd: grad_out is null");
   a.grad_out = grad_out;
   a.grad_table = grad_table;
@@ -295,7 +300,7 @@ int sn_field_grad_fwd(int64_t n, const int32_t* count, const float* x, const flo
                       float* sdf, float* grad, void* stream) {
   FieldArgs a;
   SN_TRY(fill_field_args(a, n, count, x, table, grid, active_levels, mlp, 1));
-  if (a.table_half || a.one_pass) {
+  if (a.table_half || a.one_pass || a.bf16) {
     set_error("field_grad: SN_FIELD_* precision flags are supported by the fused field forward/backward only");
     return SN_ERR_UNSUPPORTED;
   }
@@ -310,7 +315,7 @@ int sn_field_grad_bwd(int64_t n, const int32_t* count, const float* x, const flo
                       float* grad_b0, float* grad_w1, float* grad_b1, void* stream) {
   FieldArgs a;
   SN_TRY(fill_field_args(a, n, count, x, table, grid, active_levels, mlp, 1));
-  if (a.table_half || a.one_pass) {
+  if (a.table_half || a.one_pass || a.bf16) {
     set_error("field_grad: SN_FIELD_* precision flags are supported by the fused field forward/backward only");
     return SN_ERR_UNSUPPORTED;
   }

@@ -158,6 +158,7 @@ struct FieldArgs {
   bool pair16;            // grad_table is 16-byte aligned: entry pairs may be added as float4
   bool table_half;        // table holds FP16 pairs (SN_FIELD_TABLE_FP16)
   bool one_pass;          // single-pass TF32 MLP products (SN_FIELD_MLP_TF32)
+  bool bf16;              // forward: single-pass BF16 first layer (SN_FIELD_MLP_BF16)
   float2* enc_out;        // forward: level l of point p written at enc_out[l * cap + p]
   const float2* enc_in;   // backward: the encoding read from there instead of gathered
 };

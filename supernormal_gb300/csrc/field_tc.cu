@@ -24,6 +24,8 @@
 #include "field_common.cuh"
 #include "tc.cuh"
 
+#include <cuda_bf16.h>
+
 #include <string.h>
 
 namespace sn {
@@ -172,6 +174,30 @@ __device__ void stage_w0(const FieldArgs& a, uint8_t* b1_hi, uint8_t* b1_lo, uin
       *reinterpret_cast<uint32_t*>(b2_hi + o2) = hi;
       *reinterpret_cast<uint32_t*>(b2_lo + o2) = lo;
     }
+  }
+}
+
+// BF16 first-layer operands: K padded to 48, core matrices of 8 rows x 8
+// elements (16 bytes), K-adjacent core matrices contiguous (LBO 128 bytes),
+// 8-row groups kBf16Sbo bytes apart.
+constexpr int kK1b = 48;
+constexpr uint32_t kBf16Sbo = (kK1b / 8) * 128u;
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // .x (lower K) in the low half
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// W0 (64, din) -> B (N = 64 hidden, K = 48 permuted inputs, K-major), BF16.
+template <int M>
+__device__ void stage_w0_bf16(const FieldArgs& a, uint8_t* b) {
+  for (int e = threadIdx.x; e < kH * kK1b; e += blockDim.x) {
+    const int j = e / kK1b, c = e - j * kK1b;
+    const int src = c < kK1 ? w0_col<M>(c, a.g.L) : -1;
+    const float v = src >= 0 ? a.w0[j * a.din + src] : 0.0f;
+    const uint32_t off = (uint32_t)(j >> 3) * kBf16Sbo + (uint32_t)(c >> 3) * 128u + (uint32_t)(j & 7) * 16u +
+                         (uint32_t)(c & 7) * 2u;
+    *reinterpret_cast<__nv_bfloat16*>(b + off) = __float2bfloat16_rn(v);
   }
 }
 
@@ -399,7 +425,11 @@ field_fwd_tc_kernel(const __grid_constant__ FieldSegments segs) {
     const int oc = a.out_cols;
     const float inv_beta = 1.0f / a.beta;
     if (si > 0) __syncthreads();     // the previous segment's last tile is done with the weights
-    stage_w0<M>(a, sm + Sm::b1_hi, sm + Sm::b1_lo, nullptr, nullptr);
+    if (a.bf16) {
+      if constexpr (M == 4) stage_w0_bf16<M>(a, sm + Sm::b1_hi);
+    } else {
+      stage_w0<M>(a, sm + Sm::b1_hi, sm + Sm::b1_lo, nullptr, nullptr);
+    }
     for (int e = t; e < kDoutMax * kH; e += kNt) s_w1[e] = e / kH < oc ? a.w1[e] : 0.0f;
     if (t < kH) s_b0[t] = a.b0[t];
     if (t < kDoutMax) s_b1[t] = t < oc ? a.b1[t] : 0.0f;
@@ -429,25 +459,49 @@ field_fwd_tc_kernel(const __grid_constant__ FieldSegments segs) {
             if (l < a.active) __stcs(a.enc_out + (int64_t)l * a.cap + p, make_float2(e[2 * i], e[2 * i + 1]));
           }
         }
-        st_split<kFpm>(tc::taddr(tbase, lb, kFwdColInHi + kFpm * g), tc::taddr(tbase, lb, kFwdColInLo + kFpm * g), e);
-        if (g == 0) {
-          const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-          st_split8(tc::taddr(tbase, lb, kFwdColInHi + kXCol), tc::taddr(tbase, lb, kFwdColInLo + kXCol), xv);
+        if (a.bf16) {
+          // BF16 pairs: member g's 8 features in columns 4g .. 4g + 3, x (and
+          // the zero padding up to K = 48) in columns 16 .. 23
+          if constexpr (M == 4) {
+            uint32_t pk[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) pk[i] = pack_bf16(e[2 * i], e[2 * i + 1]);
+            tc::tmem_st4(tc::taddr(tbase, lb, kFwdColInHi + 4 * g), pk);
+            if (g == 0) {
+              const uint32_t xp[8] = {pack_bf16(x[0], x[1]), pack_bf16(x[2], 0.0f), 0u, 0u, 0u, 0u, 0u, 0u};
+              tc::tmem_st8(tc::taddr(tbase, lb, kFwdColInHi + kXCol / 2), xp);
+            }
+          }
+        } else {
+          st_split<kFpm>(tc::taddr(tbase, lb, kFwdColInHi + kFpm * g), tc::taddr(tbase, lb, kFwdColInLo + kFpm * g), e);
+          if (g == 0) {
+            const float xv[8] = {x[0], x[1], x[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            st_split8(tc::taddr(tbase, lb, kFwdColInHi + kXCol), tc::taddr(tbase, lb, kFwdColInLo + kXCol), xv);
+          }
         }
       }
       tc::tmem_wait_st();
       tc::fence_before_sync();
       __syncthreads();
-      if (t == 0 || t == 32) {  // H = IN W0^T, M=128, N=64, K=40
+      if (t == 0 || t == 32) {  // H = IN W0^T, M=128, N=64, K=40 (BF16: K=48, three K=16 steps)
         tc::fence_after_sync();
-        const uint32_t idesc = tc::idesc_tf32(kTile, kH);
-        const uint32_t sbo = (kK1 / 4) * 128u;
-        const uint64_t w_hi = tc::smem_desc(s_b1_hi, 128u, sbo), w_lo = tc::smem_desc(s_b1_lo, 128u, sbo);
-        if (t == 0) {
-          mma_chain(tc::taddr(tbase, 0, kFwdColH0), tc::taddr(tbase, 0, kFwdColInHi), w_hi, kK1 / 8, idesc, true);
-        } else if (!a.one_pass) {
-          mma_chain(tc::taddr(tbase, 0, kFwdColH1), tc::taddr(tbase, 0, kFwdColInLo), w_hi, kK1 / 8, idesc, true);
-          mma_chain(tc::taddr(tbase, 0, kFwdColH1), tc::taddr(tbase, 0, kFwdColInHi), w_lo, kK1 / 8, idesc, false);
+        if (a.bf16) {
+          if (t == 0) {
+            const uint64_t wb = tc::smem_desc(s_b1_hi, 128u, kBf16Sbo);
+            for (int ks = 0; ks < kK1b / 16; ++ks)
+              tc::mma_ts_f16(tc::taddr(tbase, 0, kFwdColH0), tc::taddr(tbase, 0, kFwdColInHi + 8u * ks),
+                             wb + (uint64_t)((256u * ks) >> 4), tc::idesc_bf16(kTile, kH), ks > 0 ? 1u : 0u);
+          }
+        } else {
+          const uint32_t idesc = tc::idesc_tf32(kTile, kH);
+          const uint32_t sbo = (kK1 / 4) * 128u;
+          const uint64_t w_hi = tc::smem_desc(s_b1_hi, 128u, sbo), w_lo = tc::smem_desc(s_b1_lo, 128u, sbo);
+          if (t == 0) {
+            mma_chain(tc::taddr(tbase, 0, kFwdColH0), tc::taddr(tbase, 0, kFwdColInHi), w_hi, kK1 / 8, idesc, true);
+          } else if (!a.one_pass) {
+            mma_chain(tc::taddr(tbase, 0, kFwdColH1), tc::taddr(tbase, 0, kFwdColInLo), w_hi, kK1 / 8, idesc, true);
+            mma_chain(tc::taddr(tbase, 0, kFwdColH1), tc::taddr(tbase, 0, kFwdColInHi), w_lo, kK1 / 8, idesc, false);
+          }
         }
         tc::mma_commit(bar);
       }
@@ -461,7 +515,7 @@ field_fwd_tc_kernel(const __grid_constant__ FieldSegments segs) {
       // hidden units kHpm g .. kHpm g + kHpm - 1 of this point -> partial outputs
       float h[kHpm];
       tmem_ld_n<kHpm>(tc::taddr(tbase, lb, kFwdColH0 + kHpm * g), h);
-      if (!a.one_pass) {
+      if (!a.one_pass && !a.bf16) {
         float h1[kHpm];
         tmem_ld_n<kHpm>(tc::taddr(tbase, lb, kFwdColH1 + kHpm * g), h1);
         tc::tmem_wait_ld();

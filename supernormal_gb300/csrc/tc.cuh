@@ -146,6 +146,16 @@ __host__ __device__ constexpr uint32_t idesc_tf32(uint32_t M, uint32_t N) {
          | ((M >> 4) << 24);  // M / 16
 }
 
+// Instruction descriptor of kind::f16 with BF16 A and B (both the same type)
+// and fp32 accumulation, both operands K-major, shape M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t M, uint32_t N) {
+  return (1u << 4)            // D format: f32
+         | (1u << 7)          // A format: bf16
+         | (1u << 10)         // B format: bf16
+         | ((N >> 3) << 17)   // N / 8
+         | ((M >> 4) << 24);  // M / 16
+}
+
 // Shared-memory matrix descriptor, no swizzle.  K-major canonical layout:
 // 8-row x 16-byte core matrices (8 x 4 tf32), each stored as 128 contiguous
 // bytes; `lbo` = byte distance between core matrices adjacent along K,
@@ -180,6 +190,18 @@ __device__ __forceinline__ void mma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// D[tmem] (+)= A[tmem] * B[smem]^T for 16-bit A and B (kind::f16), one K = 16
+// step: A's K elements packed two per 32-bit TMEM column (lower K in the low
+// half), so a step spans 8 columns.  Issued by one thread.
+__device__ __forceinline__ void mma_ts_f16(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
+                                           uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
       "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
       : "memory");
 }

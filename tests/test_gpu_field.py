@@ -302,3 +302,42 @@ def test_state_dict_keys_match_reference(built_lib):
     assert keys == {"encoding.params", "lin0.bias", "lin0.weight_g", "lin0.weight_v",
                     "lin1.bias", "lin1.weight_g", "lin1.weight_v"}
     assert net.encoding.params.numel() == int(OF.grid_geometry(14, 2, 19, 32, 1.3195079107728942)[0][-1]) * 2
+
+
+@pytest.mark.parametrize("d_out,active", [(1, 16), (16, 11)])
+def test_bf16_first_layer_forward(built_lib, d_out, active):
+    """SN_FIELD_MLP_BF16 (forward only): the first layer's inputs and W0 are
+    rounded to BF16 (round to nearest even) and their products accumulated in
+    FP32 on the tensor cores.  Checked against that arithmetic emulated in
+    float64 from the same rounded operands; the backward entry points reject
+    the flag."""
+    import ctypes as C
+
+    from supernormal_gb300._lib import SN_ERR_UNSUPPORTED, SN_FIELD_MLP_BF16, SupernormalError, call, stream_handle
+
+    net = make_net(ENC1, d_out=d_out, table_scale=1e3)
+    n = 3000
+    x = torch.rand((n, 3), device="cuda") * 2 - 1
+    w0, b0, w1, b1 = (t.detach().contiguous() for t in net.mlp_tensors())
+    desc = net._mlp_desc(w0, b0, w1, b1)
+    desc.flags = SN_FIELD_MLP_BF16
+    gd, st = C.byref(net.encoding.desc), stream_handle()
+    table = net.encoding.params.detach()
+    out = torch.zeros((n, d_out), device="cuda")
+    call("sn_field_fwd", n, None, x, table, gd, active, C.byref(desc), d_out, out, st)
+    enc = net.encoding(x, active_levels=active).detach()
+    inp = torch.cat([x, enc], 1).to(torch.bfloat16).double()
+    h = inp @ w0.to(torch.bfloat16).double().t() + b0.double()
+    ref = torch.nn.functional.softplus(h, beta=100.0, threshold=20.0) @ w1.double().t() + b1.double()
+    err = (out.double() - ref).abs().max().item()
+    assert err < 2e-5 * max(1.0, ref.abs().max().item()), err
+    # the rounding is visible: BF16 differs from the FP32-accurate forward
+    plain = net._mlp_desc(w0, b0, w1, b1)
+    out32 = torch.zeros_like(out)
+    call("sn_field_fwd", n, None, x, table, gd, active, C.byref(plain), d_out, out32, st)
+    assert (out - out32).abs().max().item() > 1e-5
+    go = torch.ones_like(out)
+    with pytest.raises(SupernormalError) as e:
+        call("sn_field_bwd", n, None, x, go, d_out, table, gd, active, C.byref(desc), torch.zeros_like(table),
+             None, None, None, None, None, st)
+    assert e.value.status == SN_ERR_UNSUPPORTED
