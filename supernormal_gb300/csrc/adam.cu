@@ -84,14 +84,17 @@ __global__ void __launch_bounds__(256) adam_kernel(AdamArgs a) {
   float4* v4 = reinterpret_cast<float4*>(a.v);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
-    float4 p = p4[i], g = g4[i], m = m4[i], v = v4[i];
+    // the moments are next read by the next step's Adam: streamed (evict
+    // first), so the table and its gradient, which the field kernels gather
+    // and reduce into next, keep their L2 lines
+    float4 p = p4[i], g = g4[i], m = __ldcs(m4 + i), v = __ldcs(v4 + i);
     adam_one(p.x, m.x, v.x, g.x, omb1, a.beta2, omb2, step_size, bc2s, a.eps);
     adam_one(p.y, m.y, v.y, g.y, omb1, a.beta2, omb2, step_size, bc2s, a.eps);
     adam_one(p.z, m.z, v.z, g.z, omb1, a.beta2, omb2, step_size, bc2s, a.eps);
     adam_one(p.w, m.w, v.w, g.w, omb1, a.beta2, omb2, step_size, bc2s, a.eps);
     p4[i] = p;
-    m4[i] = m;
-    v4[i] = v;
+    __stcs(m4 + i, m);
+    __stcs(v4 + i, v);
     if (a.zero_grad) g4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (a.p_half) {
       __half2* h2 = reinterpret_cast<__half2*>(a.p_half) + 2 * i;

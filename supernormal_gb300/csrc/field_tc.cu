@@ -93,8 +93,12 @@ __device__ __forceinline__ int w0_col(int c, int L) {
 //    corner, issued together by lanes 0, 4, ..., 28; up to kMaxCellGroups cells.
 //  * The lanes left add their own 8 corners; an x-adjacent corner pair that
 //    occupies one aligned pair of entries goes out as one 16-byte atomic.
-constexpr int kMaxCellGroups = 4;
-constexpr int kMinGroupLanes = 4;
+// Measured on the bench workload's backward (two rounds each): groups of
+// >= 8 lanes, at most 2 per level, beat >= 4 lanes / 4 groups by 2 %, and
+// smaller groups or more of them were slower (their shuffles cost more than
+// the L2 requests they save).
+constexpr int kMaxCellGroups = 2;
+constexpr int kMinGroupLanes = 8;
 
 __device__ __forceinline__ void scatter_level(const GridDev& gd, int l, const LevelCorners& c, float d0,
                                               float d1, bool live, bool pair16, float2* gt2, int lane) {
