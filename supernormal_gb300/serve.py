@@ -305,8 +305,11 @@ class Server:
         if self.device:
             self.mark = self._record_event
             self.wait = lambda ev: ev.synchronize()
-            self.recon_stream = torch.cuda.Stream()
-            self.req_stream = torch.cuda.Stream()
+            # requests on a higher-priority stream: when both streams have
+            # work ready, the GPU schedules the request's blocks first, so a
+            # render or query beside a reconstruction slice is slowed less
+            self.recon_stream = torch.cuda.Stream(priority=0)
+            self.req_stream = torch.cuda.Stream(priority=-1)
         else:                     # host-only tests: no device work to wait for
             self.mark = lambda: None
             self.wait = lambda ev: None
