@@ -309,13 +309,16 @@ def test_trainer_loss_and_grads_match_oracle(scene, method):
     _check_trainer_step(tr, net, var, scene.gen_random_patches(128, generator=g), method, 300)
 
 
-def test_trainer_step_at_benchmark_shapes_matches_oracle(built_lib):
+@pytest.mark.parametrize("method", ["dfd", "ad"])
+def test_trainer_step_at_benchmark_shapes_matches_oracle(built_lib, method):
     """The benchmark's configuration: displaced torus seen by 612x512 views on
     an elevated ring, hash grid 16 levels x 2 features x 2^19 entries, MLP
     35 -> 64 -> 16, 128^3 occupancy grid (warm-up sweep, then updates every 8
     iterations), marching step 2/1024, FP32, here 256 patches.  After 24
     training iterations from the benchmark's initialisation, one iteration
-    against the oracle on the kept samples."""
+    against the oracle on the kept samples; 'ad' takes the normals' gradients
+    from SDFNetwork.gradient, so the tensor-core gradient forward and
+    second-order adjoint run at these sizes too."""
     from supernormal_gb300 import scenes
     from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
     from supernormal_gb300.trainer import FusedTrainer, TrainConfig
@@ -329,13 +332,13 @@ def test_trainer_step_at_benchmark_shapes_matches_oracle(built_lib):
     var = SingleVarianceNetwork(0.5).cuda()
     net.bindwidth = 16
     cfg = TrainConfig(batch_size=256, step_size=2.0 / 1024, occ_update_freq=8, occ_threshold=0.1,
-                      increase_bandwidth_every=0, end_iter=5000)
+                      increase_bandwidth_every=0, end_iter=5000, gradient_method=method)
     tr = FusedTrainer(net, var, cfg)
     g = torch.Generator(device="cuda").manual_seed(21)
     for _ in range(24):
         tr.train_step(*ds.gen_random_patches(256, generator=g))
     tr.check_status()
-    _check_trainer_step(tr, net, var, ds.gen_random_patches(256, generator=g), "dfd", 256 * 8)
+    _check_trainer_step(tr, net, var, ds.gen_random_patches(256, generator=g), method, 256 * 8)
 
 
 def test_adam_matches_torch(built_lib):
