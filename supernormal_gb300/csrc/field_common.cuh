@@ -1,4 +1,5 @@
-// Definitions shared by the SIMT and tensor-core field kernels: hash-grid
+// Definitions shared by the standalone encoding kernels (field.cu) and the
+// tensor-core field kernels (field_tc.cu): hash-grid
 // level geometry in tiny-cuda-nn's conventions (see field.cu), the 8-corner
 // lookup of one level, and the argument block of the fused field kernels.
 #pragma once
