@@ -836,21 +836,13 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
     tc::fence_proxy_async_smem();
     tc::fence_before_sync();
     __syncthreads();
-    // dIN (needed next) and the weight-gradient MMAs are issued by two threads
-    // of different warps, each committing its own to its own mbarrier, so the
-    // dIN chain is queued without waiting behind the longer dW0 issue
+    // dIN (needed next): its three parts from three threads of different warps
     if (t == 0 || t == 32 || t == 64) {
       const int part = t >> 5;
       tc::fence_after_sync();
       if (part == 0 || !a.one_pass) issue_mma2_part(tbase, sm, part);
       tc::mma_commit(bar);
-    } else if (t == 96) {
-      tc::fence_after_sync();
-      issue_mma3(tbase, sm, first, a.one_pass);
-      tc::mma_commit(bar3);
     }
-    first = false;
-    pending3 = true;
     got = tc::mbar_wait_bounded(bar, phase);
     phase ^= 1u;
     if (!__syncthreads_and(got)) {
@@ -858,6 +850,15 @@ __global__ void __launch_bounds__(128 * M, 1) field_bwd_tc_kernel(FieldArgs a) {
       break;
     }
     tc::fence_after_sync();
+    // the weight-gradient MMAs only now: issued beside dIN they were queued
+    // ahead of it in the tensor pipe and delayed it; they run during the
+    // scatter and are waited for before the next tile rewrites their operands
+    if (t == 96) {
+      issue_mma3(tbase, sm, first, a.one_pass);
+      tc::mma_commit(bar3);
+    }
+    first = false;
+    pending3 = true;
     // ---- dIN: table-gradient scatter for this member's levels, dL/dx ----
     {
       float din[kFpm];
@@ -1298,13 +1299,7 @@ field_grad_bwd_tc_kernel(FieldArgs a, const float* __restrict__ gamma, const flo
       mma_3x(tc::taddr(tbase, 0, kGColMu), tc::taddr(tbase, 0, kGColUHi), tc::taddr(tbase, 0, kGColULo), w2_hi,
              w2_lo, kH / 8, idesc2);
       tc::mma_commit(bar);
-    } else if (t == 32) {  // dW0 += delta^T IN (db0 from the ones row)
-      tc::fence_after_sync();
-      issue_grad_mma3(tbase, sm, first, false);
-      tc::mma_commit(bar3);
     }
-    first = false;
-    pending3 = true;
     got = tc::mbar_wait_bounded(bar, phase);
     phase ^= 1u;
     if (!__syncthreads_and(got)) {
@@ -1312,6 +1307,12 @@ field_grad_bwd_tc_kernel(FieldArgs a, const float* __restrict__ gamma, const flo
       break;
     }
     tc::fence_after_sync();
+    if (t == 32) {  // dW0 += delta^T IN (db0 from the ones row), behind the second MMAs
+      issue_grad_mma3(tbase, sm, first, false);
+      tc::mma_commit(bar3);
+    }
+    first = false;
+    pending3 = true;
     // ---- table gradient for this member's levels ----
     if (want_table) {
       float de[kFpm], vv[kFpm];
