@@ -281,15 +281,33 @@ def _check_trainer_step(tr, net, var, batch, method, min_samples, table_tol=2e-3
         assert abs(lo[i] - Lr[k].item()) <= 1e-4 * max(abs(Lr[k].item()), 1e-6), (k, lo[i], Lr[k].item())
     names = ["table", "v0", "g0", "b0", "v1", "g1", "b1"]
     rgrads = torch.autograd.grad(Lr["total"], [prm[n] for n in names] + [var_ref])
+    rg = dict(zip(names + ["variance"], rgrads))
     errs = {}
-    for n, r in zip(names + ["variance"], rgrads):
+    for n, r in rg.items():
         got = cpu(tr.gviews[n])
         errs[n] = grad_err(n, got, r.numpy().reshape(got.shape))
         if n == "table":
             errs["table_levels"] = _table_level_errors(net, got, r.numpy())
+        if n in ("g0", "g1"):
+            errs[n] = weight_g_err(got, r, prm["v" + n[1]], prm[n], rg["v" + n[1]])
     for n in names + ["variance"]:
         assert errs[n] < table_tol if n == "table" else errs[n] < 2e-3, (n, errs)
     return errs
+
+
+def weight_g_err(got, ref_g, v, g, ref_v):
+    """Error of d L / d g of a weight-normed layer (w_o = g_o v_o / |v_o|)
+    relative to the size of the effective-weight gradient it is a projection
+    of: d L / d g_o = <d L / d w_o, v_o / |v_o|> can cancel far below
+    |d L / d w_o|, and the float32 atomics sums of d L / d w are accurate to a
+    fraction of |d L / d w|, not of their projection.  |d L / d w_o|^2 =
+    (|v_o| / g_o)^2 |d L / d v_o|^2 + (d L / d g_o)^2 (the two are orthogonal)."""
+    v, g = v.detach().double(), g.detach().double().reshape(-1)
+    rv, rgg = ref_v.detach().double(), ref_g.detach().double().reshape(-1)
+    nv = v.norm(dim=1)
+    dw = torch.sqrt((nv / g) ** 2 * rv.pow(2).sum(1) + rgg ** 2)
+    diff = np.abs(np.asarray(got, np.float64).reshape(-1) - rgg.numpy())
+    return float(diff.max() / max(float(dw.max()), 1e-30))
 
 
 def _table_level_errors(net, got, ref):
