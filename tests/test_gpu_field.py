@@ -341,3 +341,86 @@ def test_bf16_first_layer_forward(built_lib, d_out, active):
         call("sn_field_bwd", n, None, x, go, d_out, table, gd, active, C.byref(desc), torch.zeros_like(table),
              None, None, None, None, None, st)
     assert e.value.status == SN_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("count", [700, 0])
+def test_gradient_kernels_bounded_by_device_count(built_lib, count):
+    """sn_field_grad_fwd / sn_field_grad_bwd with a device count below the
+    capacity (a graph-captured step's live points): outputs past the count are
+    not written, and the parameter gradients are those of the first `count`
+    points alone (atomics order aside); a count of 0 writes and adds nothing."""
+    import ctypes as C
+
+    from supernormal_gb300._lib import call, stream_handle
+
+    net = make_net(ENC1, d_out=16, table_scale=1e3)
+    cap, active = 1500, 16
+    x = torch.rand((cap, 3), device="cuda") * 2 - 1
+    w0, b0, w1, b1 = (t.detach().contiguous() for t in net.mlp_tensors())
+    desc = net._mlp_desc(w0, b0, w1, b1)
+    gd, st = C.byref(net.encoding.desc), stream_handle()
+    table = net.encoding.params.detach()
+    cnt = torch.tensor([count], dtype=torch.int32, device="cuda")
+    sdf = torch.full((cap,), float("nan"), device="cuda")
+    grad = torch.full((cap, 3), float("nan"), device="cuda")
+    call("sn_field_grad_fwd", cap, cnt, x, table, gd, active, C.byref(desc), sdf, grad, st)
+    sdf_n = torch.empty((max(count, 1),), device="cuda")
+    grad_n = torch.empty((max(count, 1), 3), device="cuda")
+    if count:
+        call("sn_field_grad_fwd", count, None, x[:count].contiguous(), table, gd, active, C.byref(desc),
+             sdf_n, grad_n, st)
+    torch.cuda.synchronize()
+    assert torch.isnan(sdf[count:]).all() and torch.isnan(grad[count:]).all()
+    if count:
+        assert torch.equal(sdf[:count], sdf_n) and torch.equal(grad[:count], grad_n)
+    gamma = torch.randn((cap, 3), device="cuda")
+    rho = torch.randn((cap,), device="cuda")
+
+    def bwd(n, counter):
+        gs = [torch.zeros_like(table), torch.zeros_like(w0), torch.zeros_like(b0), torch.zeros_like(w1),
+              torch.zeros_like(b1)]
+        call("sn_field_grad_bwd", n, counter, x[:n].contiguous(), gamma[:n].contiguous(), rho[:n].contiguous(),
+             table, gd, active, C.byref(desc), *gs, st)
+        return gs
+
+    got = bwd(cap, cnt)
+    torch.cuda.synchronize()
+    if count == 0:
+        assert all(float(t.abs().max()) == 0.0 for t in got)
+        return
+    want = bwd(count, None)
+    torch.cuda.synchronize()
+    for u, v in zip(got, want):
+        scale = max(float(v.abs().max()), 1e-30)
+        assert float((u - v).abs().max()) <= 1e-5 * scale
+
+
+def test_field_batch_skips_empty_segments(built_lib):
+    """sn_field_fwd_batch with a zero-point segment between two others: the
+    others' outputs are their own sn_field_fwd launches' bit for bit."""
+    import ctypes as C
+
+    from supernormal_gb300._lib import FieldSegment, call, stream_handle
+
+    nets = [make_net(ENC1, d_out=1, seed=s, table_scale=1e3) for s in (0, 1, 2)]
+    ns = [1300, 0, 517]
+    xs = [torch.rand((max(n, 1), 3), device="cuda") * 2 - 1 for n in ns]
+    st = stream_handle()
+    keep, segs, outs, want = [], (FieldSegment * 3)(), [], []
+    for k, (net, n, x) in enumerate(zip(nets, ns, xs)):
+        w0, b0, w1, b1 = (t.detach().contiguous() for t in net.mlp_tensors())
+        d = net._mlp_desc(w0, b0, w1, b1)
+        keep.append((w0, b0, w1, b1, d))
+        out = torch.full((max(n, 1), 1), float("nan"), device="cuda")
+        outs.append(out)
+        segs[k] = FieldSegment(n, x.data_ptr(), net.encoding.params.data_ptr(), C.pointer(net.encoding.desc),
+                               16, C.pointer(d), out.data_ptr())
+        ref = torch.zeros((max(n, 1), 1), device="cuda")
+        if n:
+            call("sn_field_fwd", n, None, x, net.encoding.params.detach(), C.byref(net.encoding.desc), 16,
+                 C.byref(d), 1, ref, st)
+        want.append(ref)
+    call("sn_field_fwd_batch", 3, segs, 1, st)
+    torch.cuda.synchronize()
+    assert torch.equal(outs[0], want[0]) and torch.equal(outs[2], want[2])
+    assert torch.isnan(outs[1]).all()
