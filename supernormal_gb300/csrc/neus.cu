@@ -180,10 +180,13 @@ __global__ void scale_count_kernel(const int32_t* __restrict__ in, int32_t mul, 
 }
 
 // mask := (mask > 0.5) as float, out = sum(mask) + 1e-5 (exp_runner.py:169-175).
-__global__ void __launch_bounds__(256)
+// One block (no second pass); the sum of 0/1 values is exact in float below
+// 2^24 elements, so the block size does not change it.
+constexpr int kMaskThreads = 1024;
+__global__ void __launch_bounds__(kMaskThreads)
 mask_prep_kernel(int64_t n, const float* __restrict__ mask_in, float* __restrict__ mask_out,
                  float* __restrict__ mask_sum) {
-  __shared__ float red[8];
+  __shared__ float red[kMaskThreads / 32];
   float s = 0.0f;
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
     const float m = mask_in[i] > 0.5f ? 1.0f : 0.0f;
@@ -368,7 +371,7 @@ int sn_scale_count(const int32_t* in, int32_t mul, int32_t add, int32_t* out, vo
 
 int sn_mask_prep(int64_t n, const float* mask_in, float* mask_out, float* mask_sum, void* stream) {
   SN_REQUIRE(n >= 0, "mask_prep: n < 0");
-  mask_prep_kernel<<<1, 256, 0, as_stream(stream)>>>(n, mask_in, mask_out, mask_sum);
+  mask_prep_kernel<<<1, kMaskThreads, 0, as_stream(stream)>>>(n, mask_in, mask_out, mask_sum);
   return check_launch("mask_prep");
 }
 
