@@ -129,10 +129,15 @@ def test_renderer_forward_backward_matches_oracle(scene, method):
     grads = torch.autograd.grad(Lg["total"], params, allow_unused=True)
     names = ["table", "v0", "g0", "b0", "v1", "g1", "b1"]
     rgrads = torch.autograd.grad(Lr["total"], [prm[n] for n in names] + [var_ref], allow_unused=True)
+    rg = dict(zip(names + ["variance"], rgrads))
     for n, a, b in zip(names + ["variance"], grads, rgrads):
         if b is None:
             continue
-        assert grad_err(n, cpu(a), b.numpy()) < 2e-3, n
+        if n in ("g0", "g1"):
+            err = weight_g_err(cpu(a), b, prm["v" + n[1]], prm[n], rg["v" + n[1]])
+        else:
+            err = grad_err(n, cpu(a), b.numpy())
+        assert err < 2e-3, (n, err)
 
 
 def clip_boundary_points(ref, S, P, inv_s, band=1e-6):
