@@ -308,3 +308,49 @@ def test_pack_counts_bounded_by_device_count(nf, cap, live):
         assert torch.equal(packed[:live], want_p[:live])
     if cap > live:
         assert (packed[live:cap] == -5).all()
+
+
+def test_marcher_limits_report_status_without_faulting(nf):
+    """Failure detection through the device status word, with no GPU fault:
+    a marching iteration limit below what the rays need sets
+    SN_STATUS_MARCH_LIMIT (each ray stops where the limit struck, the call
+    itself succeeds); per-ray slots shorter than a ray's samples set
+    SN_STATUS_CAPACITY and keep the samples that fit, which equal the
+    unbounded marcher's first samples; a status word is only ever OR-ed."""
+    from supernormal_gb300._lib import SN_STATUS_CAPACITY, SN_STATUS_MARCH_LIMIT, call, stream_handle
+
+    o, d, near, far, grid, jitter = _march_case(21)
+    step = 2.0 / 1024
+    g = _grid(nf, grid)
+    n = o.shape[0]
+    st = stream_handle()
+    roi, binary, rx, ry, rz, ct = nf._grid_args(g, "cuda")
+    args = (T(o), T(d), T(near), T(far), T(jitter), roi, binary, rx, ry, rz, ct, step)
+    full = torch.empty(n, dtype=torch.int32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    call("sn_march_count", n, *args, 0.0, 0, full, status, st)
+    assert int(status.item()) == 0 and int(full.max().item()) > 8
+    # iteration limit
+    limited = torch.empty_like(full)
+    call("sn_march_count", n, *args, 0.0, 4, limited, status, st)
+    assert int(status.item()) & SN_STATUS_MARCH_LIMIT
+    assert bool((limited <= full).all()) and bool((limited < full).any())
+    # slot capacity: slots of 8 samples
+    stride = 8
+    counts = torch.empty_like(full)
+    rp = torch.full((n * stride,), -1, dtype=torch.int64, device="cuda")
+    tsp = torch.empty(n * stride, device="cuda")
+    tep = torch.empty(n * stride, device="cuda")
+    status2 = torch.full((1,), 0x100, dtype=torch.int32, device="cuda")     # an unrelated bit, kept
+    call("sn_march_padded", n, *args, None, 0.0, 0, stride, counts, rp, tsp, tep, status2, st)
+    s2 = int(status2.item())
+    assert s2 & SN_STATUS_CAPACITY and s2 & 0x100
+    packed, ri, ts, te = nf.march_packed(T(o), T(d), T(near), T(far), g, step, 0.0, jitter=T(jitter))
+    pk = packed.cpu().numpy()
+    rpv, tsv = rp.view(n, stride).cpu().numpy(), tsp.view(n, stride).cpu().numpy()
+    tsr = ts.ravel().cpu().numpy()
+    for r in range(n):
+        b, c = pk[r]
+        k = min(c, stride)
+        assert (rpv[r, :k] == r).all()
+        assert np.array_equal(tsv[r, :k], tsr[b:b + k])

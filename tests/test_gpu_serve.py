@@ -284,3 +284,25 @@ def test_query_batch_matches_per_object(built_lib):
     assert not torch.equal(got[0], got[1])
     one = query_batch(objs[2:], res)
     assert torch.equal(one[0], want[2])
+
+
+def test_trainer_check_status_reports_each_condition(built_lib):
+    """The trainer's status word (OR-ed by its kernels) surfaces on the host:
+    each SN_STATUS bit raises its own error from check_status, and a clean
+    word raises nothing."""
+    from supernormal_gb300._lib import SN_STATUS_CAPACITY, SN_STATUS_MARCH_LIMIT, SN_STATUS_TIMEOUT
+    from supernormal_gb300.fields import SDFNetwork, SingleVarianceNetwork
+    from supernormal_gb300.trainer import FusedTrainer, TrainConfig
+
+    enc = dict(otype="HashGrid", n_levels=16, n_features_per_level=2, log2_hashmap_size=15,
+               base_resolution=16, per_level_scale=1.447)
+    net = SDFNetwork(3, 16, 64, 1, skip_in=(-1,), bias=0.5, encoding_config=enc, input_concat=True).cuda()
+    tr = FusedTrainer(net, SingleVarianceNetwork(0.3).cuda(), TrainConfig(batch_size=32, step_size=1.0 / 64))
+    tr.status.zero_()
+    tr.check_status()
+    for bit, words in ((SN_STATUS_MARCH_LIMIT, "iteration limit"), (SN_STATUS_CAPACITY, "capacity"),
+                       (SN_STATUS_TIMEOUT, "timed out")):
+        tr.status.fill_(bit)
+        with pytest.raises(RuntimeError, match=words):
+            tr.check_status()
+    tr.status.zero_()
