@@ -337,6 +337,15 @@ int sn_field_bwd(int64_t n, const int32_t* count, const float* x,
                  const sn_mlp_desc* mlp, float* grad_table, float* grad_w0,
                  float* grad_b0, float* grad_w1, float* grad_b1,
                  float* grad_x, void* stream);
+/* Self-test of the failure path of the tensor-core field kernels (no
+ * reference counterpart): one thread block waits, with the bounded mbarrier
+ * wait those kernels use, on an mbarrier that nothing arrives at, for `polls`
+ * polls (0: the kernels' own limit, sn_bounded_wait_polls()).  The wait gives
+ * up, SN_STATUS_TIMEOUT is OR-ed into *status (device word) and the kernel
+ * returns; the context stays usable.  This is the report a field kernel makes
+ * when its MMAs never complete. */
+int sn_selftest_bounded_wait(uint32_t polls, int32_t* status, void* stream);
+uint32_t sn_bounded_wait_polls(void);
 /* sdf (nullable, n) and grad = d sdf / d x (n, 3) in one pass: replaces
  * SDFNetwork.gradient's autograd.grad (models/fields.py:107-119). */
 int sn_field_grad_fwd(int64_t n, const int32_t* count, const float* x,

@@ -127,6 +127,8 @@ SIGNATURES: dict[str, tuple] = {
     "sn_field_bwd": (_I, [_I64, _P, _P, _P, _I, _P, _GD, _I, _MD, _P, _P, _P, _P, _P, _P, _P]),
     "sn_field_grad_fwd": (_I, [_I64, _P, _P, _P, _GD, _I, _MD, _P, _P, _P]),
     "sn_field_grad_bwd": (_I, [_I64, _P, _P, _P, _P, _P, _GD, _I, _MD, _P, _P, _P, _P, _P, _P]),
+    "sn_selftest_bounded_wait": (_I, [C.c_uint32, _P, _P]),
+    "sn_bounded_wait_polls": (C.c_uint32, []),
     "sn_weightnorm_fwd": (_I, [_I, _I, _P, _P, _P, _P, _P]),
     "sn_weightnorm_bwd": (_I, [_I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "sn_end_diff": (_I, [_I64, _P, _P, _P, _P, _P]),

@@ -345,4 +345,11 @@ int sn_weightnorm_bwd(int rows, int cols, const float* v, const float* g, const 
   return check_launch("weightnorm_bwd");
 }
 
+int sn_selftest_bounded_wait(uint32_t polls, int32_t* status, void* stream) {
+  SN_REQUIRE(status != nullptr, "selftest_bounded_wait: status is null");
+  return bounded_wait_selftest(status, polls, as_stream(stream));
+}
+
+uint32_t sn_bounded_wait_polls(void) { return bounded_wait_limit(); }
+
 }  // extern "C"

@@ -198,6 +198,8 @@ __device__ __forceinline__ int64_t effective_n(const FieldArgs& a) {
 int field_fwd_tc(const FieldArgs& a, cudaStream_t st);
 int field_fwd_tc_segments(const FieldArgs* segs, int n_seg, cudaStream_t st);
 int field_bwd_tc(const FieldArgs& a, cudaStream_t st);
+int bounded_wait_selftest(int32_t* status, uint32_t polls, cudaStream_t st);
+uint32_t bounded_wait_limit();
 int field_grad_fwd_tc(const FieldArgs& a, float* sdf, float* grad, cudaStream_t st);
 int field_grad_bwd_tc(const FieldArgs& a, const float* gamma, const float* rho, cudaStream_t st);
 

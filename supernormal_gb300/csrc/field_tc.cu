@@ -1603,7 +1603,25 @@ field_grad_fwd_tc_kernel(FieldArgs a, float* __restrict__ out_sdf, float* __rest
   if (warp == 0) tc::tmem_dealloc(tbase, kCols);
 }
 
+// The bounded mbarrier wait of the tensor-core kernels, on an mbarrier that
+// nothing arrives at, for `polls` polls (0: the kernels' own limit): the wait
+// gives up and the timeout is reported through the status word, as a kernel
+// whose MMAs never completed reports it.  The kernel then returns normally.
+__global__ void bounded_wait_selftest_kernel(int32_t* status, uint32_t polls) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) tc::mbar_init(&bar, 1);
+  __syncthreads();
+  const bool got = tc::mbar_wait_polls(&bar, 0, polls ? polls : tc::kWaitLimit);
+  if (!got && threadIdx.x == 0) atomicOr(status, SN_STATUS_TIMEOUT);
+}
+
 }  // namespace
+
+int bounded_wait_selftest(int32_t* status, uint32_t polls, cudaStream_t st) {
+  bounded_wait_selftest_kernel<<<1, 32, 0, st>>>(status, polls);
+  return check_launch("bounded_wait_selftest");
+}
+uint32_t bounded_wait_limit() { return tc::kWaitLimit; }
 
 // Launchers used by sn_field_fwd / sn_field_bwd (field.cu).
 int field_fwd_tc_segments(const FieldArgs* segs, int n_seg, cudaStream_t st) {

@@ -17,7 +17,10 @@ namespace tc {
 
 // Bound on mbarrier polls before a wait is declared failed (then the kernel
 // reports SN_STATUS_TIMEOUT, drains and frees its tensor memory, and returns).
-constexpr uint32_t kWaitLimit = 1u << 22;
+// A poll of an incomplete phase suspends the thread for ~4 us on a GB300
+// (measured by sn_selftest_bounded_wait), so 2^18 polls give up after ~1 s;
+// an MMA completes in microseconds.
+constexpr uint32_t kWaitLimit = 1u << 18;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -128,11 +131,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return done != 0;
 }
-// Polls up to kWaitLimit times; false if the phase never completed.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kWaitLimit; ++i)
+// Polls up to `polls` times; false if the phase never completed.
+__device__ __forceinline__ bool mbar_wait_polls(uint64_t* bar, uint32_t parity, uint32_t polls) {
+  for (uint32_t i = 0; i < polls; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
+}
+// Polls up to kWaitLimit times; false if the phase never completed.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  return mbar_wait_polls(bar, parity, kWaitLimit);
 }
 
 // ---- MMA -------------------------------------------------------------------------

@@ -15,7 +15,7 @@ def _declarations():
     text = HEADER.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     decls = {}
-    for m in re.finditer(r"(?:^|\n)\s*(?:const\s+)?(?:int|size_t|uint64_t|char\s*\*)\s*\*?\s*(sn_\w+)\s*\(([^;]*?)\)\s*;",
+    for m in re.finditer(r"(?:^|\n)\s*(?:const\s+)?(?:int|size_t|uint32_t|uint64_t|char\s*\*)\s*\*?\s*(sn_\w+)\s*\(([^;]*?)\)\s*;",
                          text):
         name, params = m.group(1), m.group(2).strip()
         n = 0 if params in ("", "void") else len([p for p in params.split(",") if p.strip()])

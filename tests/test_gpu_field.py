@@ -424,3 +424,39 @@ def test_field_batch_skips_empty_segments(built_lib):
     torch.cuda.synchronize()
     assert torch.equal(outs[0], want[0]) and torch.equal(outs[2], want[2])
     assert torch.isnan(outs[1]).all()
+
+
+def test_bounded_wait_reports_timeout_and_the_context_survives(built_lib):
+    """The failure path of the tensor-core field kernels, without a GPU fault:
+    a bounded mbarrier wait on a barrier that nothing arrives at gives up,
+    SN_STATUS_TIMEOUT reaches the status word, and the context keeps working.
+    The time per poll bounds how long the kernels' own limit lets a stuck MMA
+    wait before they report it."""
+    import ctypes as C
+
+    from supernormal_gb300._lib import SN_STATUS_TIMEOUT, call, lib, stream_handle
+
+    st = stream_handle()
+    polls = 1 << 12
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    call("sn_selftest_bounded_wait", polls, status, st)
+    e1.record()
+    torch.cuda.synchronize()
+    assert int(status.item()) & SN_STATUS_TIMEOUT
+    ms = e0.elapsed_time(e1)
+    limit = int(lib().sn_bounded_wait_polls())
+    print(f"bounded wait: {polls} polls in {ms:.3f} ms; the kernels' limit of {limit} polls ~ {ms * limit / polls / 1e3:.2f} s")
+    assert ms * limit / polls < 3_000.0        # the kernels give up within a few seconds
+    # the context is intact: a field forward afterwards gives the oracle's values
+    net = make_net(ENC1, d_out=1, table_scale=1e3)
+    x = torch.rand((777, 3), device="cuda") * 2 - 1
+    w0, b0, w1, b1 = (t.detach().contiguous() for t in net.mlp_tensors())
+    d = net._mlp_desc(w0, b0, w1, b1)
+    out = torch.zeros((777, 1), device="cuda")
+    call("sn_field_fwd", 777, None, x, net.encoding.params.detach(), C.byref(net.encoding.desc), 16, C.byref(d), 1,
+         out, st)
+    prm = OF.params_from_module(net)
+    ref = OF.sdf_network(x.cpu().double(), **prm, geom=OF.geometry_from_module(net), active_levels=16, out_cols=1)
+    assert np.abs(out.cpu().numpy() - ref.detach().numpy()).max() < 2e-5
